@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 power-spectrum hot path.
+
+Workload (default): 512^3 particles on a lattice displaced by the Zel'dovich
+approximation (P(k) ~ k^-2 exp(-(k/k_c)^2), k_c = k_Nyq/2, RMS displacement 0.3
+lattice spacings), L = 100000 kpc/h, equal masses 1.0, FP32 512^3 grid, 64
+log-k bins.  One step = one spectrum: zero the grid, CIC-deposit all
+particles, r2c FFT, fused deconvolution + binning, read the 64 bins back.
+
+  value      particles/s with the particles resident in HBM (Np / device time
+             of one step, CUDA events on the library's stream), summed over
+             ranks (each rank an independent box: replicas, weak scaling).
+  e2e        the same through the C ABI from pinned host buffers: the H2D copy
+             of the positions and the D2H of the bins are inside each step.
+  roofline   HBM roofline of the deposit pass (the dominant stage): algorithmic
+             bytes Np*12 + 4*N^2*2(N/2+1) over its device time; also the
+             binning kernel and deposit+binning together.
+  cpu_baseline  the FP64 oracle port (OpenMP, all host cores) on the same
+             particles: deposit + FP64 r2c (pocketfft) + binning.
+
+``--impl reference`` times the CPU implementation of the reference's algorithm
+(the oracle port: the reference sources are not available on the GPU host) on
+the same config and prints one line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("particles/s + ms/spectrum at 512^3 grid vs FP64 oracle; "
+          "fwd+adjoint/fwd time ratio")
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+# dram bytes per launch of the deposit pass from an ncu capture of this
+# workload (sum over its kernels); None until a capture is recorded.
+NCU_DEPOSIT_TRAFFIC = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--nside", type=int, default=512, help="particles per lattice side")
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--nrbins", type=int, default=64)
+    ap.add_argument("--box", type=float, default=100000.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.dev), "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                    power.append(float(parts[3]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax),
+                "power_w_max": max(power), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup(backend):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def algorithmic_bytes(np_, n, var_masses=False):
+    cells = 4 * n * n * 2 * (n // 2 + 1)
+    dep = np_ * (12 + (4 if var_masses else 0)) + cells
+    binb = 8 * n * n * (n // 2 + 1)
+    return dep, binb
+
+
+# ---------------------------------------------------------------------------
+# CPU leg (oracle port): used for cpu_baseline and for the reference arm
+# ---------------------------------------------------------------------------
+
+def cpu_pipeline(pos_host, box, n, nrbins, mass, sample=None):
+    """FP64 deposit (+ FFT + binning) on the host cores.  Returns (power, count,
+    timings dict, particles deposited)."""
+    from oracle import oracle as O
+    import scipy.fft as sfft
+    port = O.port()
+    cores = port.num_threads()
+    sub = pos_host if sample is None else pos_host[:sample]
+    grid = O.zeros_grid(n)
+    t0 = time.perf_counter()
+    port.fieldize(box, n, grid, sub, None, mass, 1)
+    t1 = time.perf_counter()
+    f = sfft.rfftn(grid[:, :, :n], workers=cores)
+    t2 = time.perf_counter()
+    m = O.total_mass(len(pos_host), None, mass)
+    p, c, k = port.powerspectrum(n, f, f, nrbins, m, m)
+    t3 = time.perf_counter()
+    return p, c, {"deposit": t1 - t0, "fft": t2 - t1, "bin": t3 - t2, "cores": cores}, len(sub)
+
+
+def reference_arm(args):
+    world, rank, _ = dist_setup("gloo")
+    if rank != 0:
+        return
+    from genpk_gb300 import synth
+    n, nside = args.grid, args.nside
+    npart = nside ** 3
+    pos = synth.zeldovich(nside, args.box, seed=1)
+    sample = min(npart, 1 << 24)
+    times = []
+    cores = 1
+    for it in range(args.warmup + args.steps):
+        _, _, t, ndep = cpu_pipeline(pos, args.box, n, args.nrbins, 1.0, sample=sample)
+        cores = t["cores"]
+        full = t["deposit"] * npart / ndep + t["fft"] + t["bin"]
+        if it >= args.warmup:
+            times.append(full)
+    tstep = float(np.mean(times))
+    value = npart / tstep
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "particles/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tstep * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice)",
+        "config": config_dict(args, npart),
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
+                         "sample": f"each step: deposit of the first {sample} particles "
+                                   f"(scaled to {npart}), full {n}^3 FP64 r2c and binning"},
+        "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, npart):
+    return {"workload": (f"Zel'dovich lattice {args.nside}^3 particles, L={args.box:g} kpc/h, "
+                         f"FP32 {args.grid}^3 grid, {args.nrbins} log-k bins, auto spectrum"),
+            "particles": npart, "grid": args.grid, "nrbins": args.nrbins, "boxsize": args.box,
+            "l2": f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions per step)",
+            "parallelism": "replicas (one independent box per GPU)"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    world, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    import genpk_gb300 as gp
+    from genpk_gb300 import synth
+    from oracle import oracle as O
+
+    n, nrbins, box, nside = args.grid, args.nrbins, args.box, args.nside
+    npart = nside ** 3
+    mass = 1.0
+    m_norm = O.total_mass(npart, None, mass)
+    dpos = synth.zeldovich(nside, box, seed=1 + rank, device="cuda")
+    torch.cuda.synchronize()
+    ctx = gp.Context(n, nrbins, timing=True)
+
+    def step(src):
+        ctx.timing_reset()
+        ctx.zero(0)
+        ctx.deposit(0, box, src, None, mass)
+        p, c, k = ctx.power(0, 0, m_norm, m_norm)
+        return p, c, ctx.stage_times()
+
+    for _ in range(args.warmup):
+        step(dpos)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    launches0 = ctx.launches
+    t0 = time.perf_counter()
+    dev_ms, stages = [], {}
+    for _ in range(args.steps):
+        p, c, st = step(dpos)
+        dev_ms.append(sum(st.values()))
+        for key, v in st.items():
+            stages[key] = stages.get(key, 0.0) + v
+    barrier()
+    wall = time.perf_counter() - t0
+    launches = ctx.launches - launches0
+    clk = clocks.stop()
+    ms_step = float(np.mean(dev_ms))
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    stages = {k: v / args.steps for k, v in stages.items()}
+    value = npart * world / (ms_step * 1e-3)
+
+    # roofline of the deposit pass (dominant stage) and of the binning kernel
+    pk_, pk_src = peaks()
+    peak = float(pk_["hbm_gbs"])
+    b_dep, b_bin = algorithmic_bytes(npart, n)
+    t_dep = sum(v for k, v in stages.items() if k.startswith("dep_")) * 1e-3
+    t_bin = stages.get("bin", 0.0) * 1e-3
+    ach_dep = b_dep / t_dep / 1e9
+    ach_bin = b_bin / t_bin / 1e9 if t_bin > 0 else None
+    roofline = {"kernel": "deposit pass (k_sort_hist .. k_halo_merge)", "bound": "hbm",
+                "achieved": ach_dep, "peak": peak, "unit": "GB/s", "frac": ach_dep / peak,
+                "peak_source": pk_src, "traffic": NCU_DEPOSIT_TRAFFIC,
+                "algorithmic_bytes": b_dep,
+                "bin": {"achieved": ach_bin, "frac": (ach_bin / peak) if ach_bin else None,
+                        "algorithmic_bytes": b_bin},
+                "deposit_plus_bin_frac": (b_dep + b_bin) / (t_dep + t_bin) / 1e9 / peak}
+
+    line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded Zel'dovich lattice generated on the GPU",
+            "config": config_dict(args, npart), "ms_per_spectrum": ms_step,
+            "wall_ms_per_step": wall / args.steps * 1e3,
+            "stages_ms": {k: round(v, 5) for k, v in stages.items()},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk}
+
+    # forward + adjoint / forward
+    if not args.no_adjoint:
+        g = np.linspace(1.0, -1.0, nrbins) / np.maximum(np.abs(p), 1e-30)
+        gpos = torch.empty((npart, 3), device="cuda", dtype=torch.float32)
+        fwd, adj, adj_rc = [], [], []
+        for it in range(4):
+            _, _, st = step(dpos)
+            ctx.timing_reset()
+            ctx.adjoint(0, box, dpos, g, m_norm, mass=mass, grad_pos=gpos)
+            sa = ctx.stage_times()
+            ctx.timing_reset()
+            ctx.adjoint(0, box, dpos, g, m_norm, mass=mass, grad_pos=gpos, recompute=True)
+            sr = ctx.stage_times()
+            if it:
+                fwd.append(sum(st.values()))
+                adj.append(sum(sa.values()))
+                adj_rc.append(sum(sr.values()))
+        f_ms = float(np.mean(fwd))
+        line["fwd_adj_ratio"] = (f_ms + float(np.mean(adj))) / f_ms
+        line["fwd_adj_recompute_ratio"] = (f_ms + float(np.mean(adj_rc))) / f_ms
+        line["adjoint_ms"] = float(np.mean(adj))
+        del gpos
+
+    # end to end through the C ABI from pinned host memory
+    if not args.no_e2e:
+        hpos = dpos.cpu().pin_memory()
+        for _ in range(2):
+            step(hpos)
+        torch.cuda.synchronize()
+        e2e_t = []
+        for _ in range(max(3, min(args.steps, 20))):
+            t1 = time.perf_counter()
+            step(hpos)
+            e2e_t.append(time.perf_counter() - t1)
+        e = float(np.mean(e2e_t))
+        line["e2e"] = {"value": npart * world / e, "unit": "particles/s",
+                       "h2d_bytes_per_step": npart * 12, "d2h_bytes_per_step": nrbins * 8,
+                       "ms_per_step": e * 1e3}
+        del hpos
+
+    # FP64 oracle on the same particles (rank 0): parity at full size + CPU baseline
+    if rank == 0 and not args.no_cpu:
+        hp = dpos.cpu().numpy()
+        pr, cr, t, nd = cpu_pipeline(hp, box, n, nrbins, mass)
+        ok = cr > 0
+        rel = np.abs(p[ok] - pr[ok]) / np.abs(pr[ok])
+        line["parity"] = {"max_bin_rel_err": float(rel.max()),
+                          "counts_bit_exact": bool(np.array_equal(c, cr)),
+                          "oracle": "FP64 CIC (oracle port) + FP64 pocketfft r2c + binning"}
+        tcpu = t["deposit"] + t["fft"] + t["bin"]
+        line["cpu_baseline"] = {"value": npart / tcpu, "unit": "particles/s",
+                                "cores": t["cores"], "kind": "port",
+                                "sample": f"full workload once ({nd} particles): deposit "
+                                          f"{t['deposit']:.2f} s, FP64 r2c {t['fft']:.2f} s, "
+                                          f"binning {t['bin']:.2f} s"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,10 @@
+"""GB300 (sm_103a) implementation of GenPK's power-spectrum hot path.
+
+CIC deposit -> FP32 r2c FFT (cuFFT) -> fused CIC deconvolution + log-k shell
+binning, plus the adjoint of a P(k) loss, behind the C ABI in
+include/genpk_gb300.h.  See genpk_gb300.api for the Python mirror.
+"""
+from .api import (Context, GenPKError, fieldize, geometry, invwindow,  # noqa: F401
+                  powerspectrum)
+
+__all__ = ["Context", "GenPKError", "fieldize", "geometry", "invwindow", "powerspectrum"]

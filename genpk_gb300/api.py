@@ -1,0 +1,265 @@
+"""Python mirror of GenPK's hot-path interface, running on the GB300 library.
+
+Module-level functions keep the reference's names, argument meaning and
+return conventions:
+
+  fieldize(boxsize, dims, out, pos, masses, mass, extra)   fieldize.cpp:46
+  invwindow(kx, ky, kz, n)                                  fieldize.cpp:125
+  powerspectrum(dims, outfield, outfield2, nrbins, M1, M2)  powerspectrum.c:35
+
+``Context`` is the device-resident interface the C ABI exposes (grids stay in
+HBM; the FFT and binning run on the GPU).  Arrays may be numpy arrays or torch
+tensors (host or CUDA); torch is only used as a container for device memory.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+
+GENPK_FLAG_TIMING = 0x1
+
+
+class GenPKError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"genpk status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _arg(x, np_dtype, torch_dtype_name):
+    """(address, keep-alive object, is_device) for a numpy array or torch tensor."""
+    if x is None:
+        return None, None, False
+    if _is_torch(x):
+        import torch
+        t = x.detach()
+        want = getattr(torch, torch_dtype_name)
+        if t.dtype != want:
+            t = t.to(want)
+        t = t.contiguous()
+        return t.data_ptr(), t, t.is_cuda
+    a = np.ascontiguousarray(x, dtype=np_dtype)
+    return a.ctypes.data, a, False
+
+
+def _check(lib, ctx, rc):
+    if rc != 0:
+        msg = lib.genpk_last_error(ctx).decode() if ctx else ""
+        if not msg:
+            msg = lib.genpk_status_string(rc).decode()
+        raise GenPKError(rc, msg)
+
+
+class Context:
+    """Device-resident grids for one grid size (replaces fftw_malloc + plan)."""
+
+    def __init__(self, dims: int, nrbins: int, nfields: int = 1, timing: bool = False):
+        self.lib = native.load()
+        self.dims = int(dims)
+        self.nrbins = int(nrbins)
+        self.nfields = int(nfields)
+        self.row = 2 * (self.dims // 2 + 1)
+        h = ctypes.c_void_p()
+        rc = self.lib.genpk_ctx_create(self.dims, self.nrbins, self.nfields,
+                                       GENPK_FLAG_TIMING if timing else 0, ctypes.byref(h))
+        if rc != 0:
+            msg = self.lib.genpk_last_error(h).decode() if h.value else ""
+            if h.value:
+                self.lib.genpk_ctx_destroy(h)
+            raise GenPKError(rc, msg or self.lib.genpk_status_string(rc).decode())
+        self.h = h
+
+    # -- life cycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.genpk_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, rc):
+        _check(self.lib, self.h, rc)
+
+    # -- grids ----------------------------------------------------------------
+    def zero(self, field: int = 0):
+        self._chk(self.lib.genpk_zero(self.h, field))
+
+    def deposit(self, field, boxsize, pos, masses=None, mass=0.0):
+        """+= CIC deposit of particles (fieldize semantics)."""
+        pp, pk, _ = _arg(pos, np.float32, "float32")
+        n = (pk.numel() if _is_torch(pk) else pk.size) // 3
+        mp, mk, _ = _arg(masses, np.float32, "float32")
+        self._chk(self.lib.genpk_deposit(self.h, field, float(boxsize), pp, mp, float(mass), n))
+        return self
+
+    def sync(self):
+        self._chk(self.lib.genpk_sync(self.h))
+
+    def read_field(self, field: int = 0) -> np.ndarray:
+        out = np.empty((self.dims, self.dims, self.row), dtype=np.float64)
+        self._chk(self.lib.genpk_read_field(self.h, field,
+                                            out.ctypes.data_as(native.c_f64p)))
+        return out
+
+    def load_spectrum(self, field, spec):
+        spec = np.ascontiguousarray(spec, dtype=np.complex128)
+        self._chk(self.lib.genpk_load_spectrum(self.h, field,
+                                               spec.ctypes.data_as(native.c_f64p)))
+
+    # -- spectra --------------------------------------------------------------
+    def power(self, field_a=0, field_b=None, mass_a=1.0, mass_b=None):
+        """(power, count, keffs) like powerspectrum(); FFTs the grids if needed."""
+        field_b = field_a if field_b is None else field_b
+        mass_b = mass_a if mass_b is None else mass_b
+        p = np.zeros(self.nrbins)
+        c = np.zeros(self.nrbins, dtype=np.int32)
+        k = np.zeros(self.nrbins)
+        self._chk(self.lib.genpk_power(self.h, field_a, field_b, float(mass_a), float(mass_b),
+                                       p.ctypes.data_as(native.c_f64p),
+                                       c.ctypes.data_as(native.c_i32p),
+                                       k.ctypes.data_as(native.c_f64p)))
+        return p, c, k
+
+    def power_multi(self, pairs, pair_masses):
+        pairs = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        pm = np.ascontiguousarray(np.asarray(pair_masses, dtype=np.float64).reshape(-1, 2))
+        npair = pairs.shape[0]
+        p = np.zeros((npair, self.nrbins))
+        c = np.zeros(self.nrbins, dtype=np.int32)
+        k = np.zeros(self.nrbins)
+        self._chk(self.lib.genpk_power_multi(self.h, npair, pairs.ctypes.data_as(native.c_i32p),
+                                             pm.ctypes.data_as(native.c_f64p),
+                                             p.ctypes.data_as(native.c_f64p),
+                                             c.ctypes.data_as(native.c_i32p),
+                                             k.ctypes.data_as(native.c_f64p)))
+        return p, c, k
+
+    # -- adjoint --------------------------------------------------------------
+    def adjoint(self, field, boxsize, pos, dl_dp, mass_norm, masses=None, mass=0.0,
+                recompute=False, grad_pos=None, grad_mass=None):
+        """dL/dpos [n,3], dL/dmass [n] (or None) and dL/dM for the auto spectrum of
+        `field`; outputs live where `pos` lives (host numpy or CUDA tensor)."""
+        pp, pk, dev = _arg(pos, np.float32, "float32")
+        n = (pk.numel() if _is_torch(pk) else pk.size) // 3
+        mp, mk, _ = _arg(masses, np.float32, "float32")
+        if dev:
+            import torch
+            gp = grad_pos if grad_pos is not None else torch.empty((n, 3), dtype=torch.float32,
+                                                                     device=pk.device)
+            gm = None
+            if masses is not None:
+                gm = grad_mass if grad_mass is not None else torch.empty(
+                    n, dtype=torch.float32, device=pk.device)
+            gpp, gmp = gp.data_ptr(), (gm.data_ptr() if gm is not None else None)
+        else:
+            gp = np.empty((n, 3), dtype=np.float32)
+            gm = np.empty(n, dtype=np.float32) if masses is not None else None
+            gpp, gmp = gp.ctypes.data, (gm.ctypes.data if gm is not None else None)
+        g = np.ascontiguousarray(dl_dp, dtype=np.float64)
+        dldm = ctypes.c_double(0.0)
+        self._chk(self.lib.genpk_adjoint(self.h, field, float(boxsize), pp, mp, float(mass), n,
+                                         float(mass_norm), g.ctypes.data_as(native.c_f64p),
+                                         gpp, gmp, ctypes.byref(dldm), 1 if recompute else 0))
+        return gp, gm, dldm.value
+
+    # -- introspection --------------------------------------------------------
+    def timing_reset(self):
+        self._chk(self.lib.genpk_timing_reset(self.h))
+
+    def stage_times(self) -> dict:
+        """{kernel/stage name: ms} since the last timing_reset (CUDA events)."""
+        names = (ctypes.c_char_p * 64)()
+        ms = (ctypes.c_float * 64)()
+        k = self.lib.genpk_stage_times(self.h, names, ms, 64)
+        out = {}
+        for i in range(k):
+            key = names[i].decode() if names[i] else f"stage{i}"
+            out[key] = out.get(key, 0.0) + ms[i]
+        return out
+
+    def deposit_config(self) -> dict:
+        v = [ctypes.c_int() for _ in range(4)]
+        self._chk(self.lib.genpk_deposit_config(self.h, *[ctypes.byref(x) for x in v]))
+        return {"tile": (v[0].value, v[1].value, v[2].value), "sort_ctas": v[3].value}
+
+    def set_tile(self, tx: int, ty: int, tz: int):
+        self._chk(self.lib.genpk_set_deposit_tile(self.h, tx, ty, tz))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.genpk_kernel_launches(self.h))
+
+    def bin_of(self, kk2: int) -> int:
+        return int(self.lib.genpk_bin_of(self.h, int(kk2)))
+
+
+# ---------------------------------------------------------------------------
+# Reference-named functions
+# ---------------------------------------------------------------------------
+
+def invwindow(kx, ky, kz, n) -> float:
+    """fieldize.cpp:125-133."""
+    return native.load().genpk_invwindow(int(kx), int(ky), int(kz), int(n))
+
+
+def geometry(dims, nrbins):
+    """Weighted mode counts and mean |k| per bin (host only, no GPU)."""
+    lib = native.load()
+    c = np.zeros(nrbins, dtype=np.int32)
+    k = np.zeros(nrbins)
+    _check(lib, None, lib.genpk_geometry(int(dims), int(nrbins), c.ctypes.data_as(native.c_i32p),
+                                         k.ctypes.data_as(native.c_f64p)))
+    return c, k
+
+
+def fieldize(boxsize, dims, out, pos, masses=None, mass=0.0, extra=1) -> int:
+    """fieldize.cpp:46: += CIC deposit into the float64 host array `out`
+    (size dims*dims*2*(dims/2+extra)), computed on the GPU.  Returns 0."""
+    lib = native.load_compat()
+    assert out.dtype == np.float64 and out.flags.c_contiguous
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1)
+    mp = None
+    if masses is not None:
+        masses = np.ascontiguousarray(masses, dtype=np.float32)
+        mp = masses.ctypes.data_as(native.c_f32p)
+    rc = lib.fieldize(float(boxsize), int(dims), out.ctypes.data_as(native.c_f64p),
+                      pos.size // 3, pos.ctypes.data_as(native.c_f32p), mp, float(mass),
+                      int(extra))
+    _check(native.load(), None, rc)
+    return rc
+
+
+def powerspectrum(dims, outfield, outfield2, nrbins, total_mass, total_mass2):
+    """powerspectrum.c:35 on the caller's half-complex spectra (complex128,
+    dims x dims x dims/2+1), binned on the GPU.  Returns (power, count, keffs)."""
+    lib = native.load_compat()
+    f1 = np.ascontiguousarray(outfield, dtype=np.complex128)
+    f2 = f1 if outfield2 is None or outfield2 is outfield else np.ascontiguousarray(
+        outfield2, dtype=np.complex128)
+    p = np.zeros(nrbins)
+    c = np.zeros(nrbins, dtype=np.int32)
+    k = np.zeros(nrbins)
+    rc = lib.powerspectrum(int(dims), f1.ctypes.data_as(native.c_f64p),
+                           f2.ctypes.data_as(native.c_f64p), int(nrbins),
+                           p.ctypes.data_as(native.c_f64p), c.ctypes.data_as(native.c_i32p),
+                           k.ctypes.data_as(native.c_f64p), float(total_mass),
+                           float(total_mass2))
+    _check(native.load(), None, rc)
+    return p, c, k

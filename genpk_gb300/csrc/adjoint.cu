@@ -1,0 +1,183 @@
+// adjoint.cu -- gradient of a P(k) loss with respect to particle positions and
+// masses.  The reference computes no derivative; this is the exact adjoint of
+// the forward path in deposit.cu / spectrum.cu:
+//
+//   P_b = S_b / (M^2 C_b),  S_b = sum_{m in b} c_m |F_m|^2 V_m,  F = r2c(rho)
+//   dL/drho(x) = sum_m (2 g_b c_m V_m / (M^2 C_b)) Re(F_m e^{ikx}),  g_b = dL/dP_b
+//
+// evaluated as an unnormalised c2r of H_m = G_b * V_m * (c_m / mult_m) * F_m with
+// G_b = 2 g_b / (M^2 C_b) and mult_m the c2r multiplicity of the mode (1 on the
+// self-conjugate kz = 0 and, for even N, kz = N/2 planes, 2 elsewhere).  The
+// position and mass gradients are then the CIC gather (transpose of the
+// deposit) of dL/drho.
+#include "common.cuh"
+#include "internal.h"
+
+#include <algorithm>
+
+namespace genpk {
+namespace {
+
+__device__ __forceinline__ int kval_adj(int i, int dims)
+{
+    return i <= dims / 2 ? i : i - dims;
+}
+
+struct ModeGradParams {
+    int dims, hc, half;
+    int nrbins;
+    float bpu_half;
+    int64_t nmodes;
+};
+
+__global__ void __launch_bounds__(256)
+    k_mode_gradient(ModeGradParams p, float2 *__restrict__ spec, const uint32_t *__restrict__ thr_g,
+                    const float *__restrict__ iw, const float *__restrict__ gcoef)
+{
+    extern __shared__ uint32_t thr[];
+    for (int i = threadIdx.x; i <= p.nrbins; i += blockDim.x)
+        thr[i] = thr_g[i];
+    __syncthreads();
+    const bool even = (p.dims & 1) == 0;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < p.nmodes;
+         m += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = m / p.hc;
+        const int kz = (int)(m - r * p.hc);
+        const int i = (int)(r / p.dims), j = (int)(r - (int64_t)i * p.dims);
+        const int ki = kval_adj(i, p.dims), kj = kval_adj(j, p.dims);
+        const uint32_t kk2 = (uint32_t)(ki * ki + kj * kj + kz * kz);
+        float2 h = make_float2(0.f, 0.f);
+        if (kk2 != 0) {
+            int b = (int)(p.bpu_half * __logf((float)kk2));
+            b = max(0, min(p.nrbins - 1, b));
+            while (b + 1 < p.nrbins && kk2 >= thr[b + 1])
+                b++;
+            while (b > 0 && kk2 < thr[b])
+                b--;
+            const float pz = (__ldg(iw + i) * __ldg(iw + j)) * __ldg(iw + kz);
+            const float p2 = pz * pz;
+            const bool edge = (kz == 0 || kz == p.half);        // reference weight 1
+            const bool selfconj = (kz == 0) || (even && kz == p.half);  // c2r counts once
+            const float cm = edge ? 1.f : 2.f;
+            const float mult = selfconj ? 1.f : 2.f;
+            const float s = __ldg(gcoef + b) * (p2 * p2) * (cm / mult);
+            const float2 f = spec[m];
+            h = make_float2(s * f.x, s * f.y);
+        }
+        spec[m] = h;
+    }
+}
+
+struct GatherParams {
+    int dims;
+    int64_t plane;
+    int row;
+    float uh, ul;
+    float units;
+    float mass;
+    float dl_dm;
+    int64_t n;
+};
+
+template <bool VARMASS>
+__global__ void __launch_bounds__(256)
+    k_gather(GatherParams p, const float *__restrict__ grid, const float *__restrict__ pos,
+             const float *__restrict__ masses, float *__restrict__ gpos, float *__restrict__ gmass)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const float m = VARMASS ? masses[i] : p.mass;
+        if (!finite3(x, y, z)) {
+            gpos[3 * i] = gpos[3 * i + 1] = gpos[3 * i + 2] = 0.f;
+            if (VARMASS)
+                gmass[i] = 0.f;
+            continue;
+        }
+        int c[3];
+        float d[3];
+        split_cell(x, p.uh, p.ul, p.dims, c[0], d[0]);
+        split_cell(y, p.uh, p.ul, p.dims, c[1], d[1]);
+        split_cell(z, p.uh, p.ul, p.dims, c[2], d[2]);
+        int h[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            h[a] = c[a] + 1 == p.dims ? 0 : c[a] + 1;
+        float g[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            g[k] = __ldg(grid + cell_index(p.plane, p.row, (k & 1) ? h[0] : c[0],
+                                           (k & 2) ? h[1] : c[1], (k & 4) ? h[2] : c[2]));
+        const float t0 = 1.f - d[0], t1 = 1.f - d[1], t2 = 1.f - d[2];
+        // Interpolate along z first, then y, then x; derivatives from the same tree.
+        const float g00 = fmaf(d[2], g[4] - g[0], g[0]);  // (x0,y0)
+        const float g10 = fmaf(d[2], g[5] - g[1], g[1]);  // (x1,y0)
+        const float g01 = fmaf(d[2], g[6] - g[2], g[2]);  // (x0,y1)
+        const float g11 = fmaf(d[2], g[7] - g[3], g[3]);  // (x1,y1)
+        const float gx0 = fmaf(d[1], g01 - g00, g00);
+        const float gx1 = fmaf(d[1], g11 - g10, g10);
+        const float val = fmaf(d[0], gx1 - gx0, gx0);
+        const float dgx = gx1 - gx0;
+        const float gy0 = fmaf(d[0], g10 - g00, g00);
+        const float gy1 = fmaf(d[0], g11 - g01, g01);
+        const float dgy = gy1 - gy0;
+        // d/dz: bilinear in (x, y) of the z-differences.
+        const float e00 = g[4] - g[0], e10 = g[5] - g[1], e01 = g[6] - g[2], e11 = g[7] - g[3];
+        const float dgz = t0 * (t1 * e00 + d[1] * e01) + d[0] * (t1 * e10 + d[1] * e11);
+        (void)t2;
+        const float s = m * p.units;
+        gpos[3 * i] = s * dgx;
+        gpos[3 * i + 1] = s * dgy;
+        gpos[3 * i + 2] = s * dgz;
+        if (VARMASS)
+            gmass[i] = val + p.dl_dm;
+    }
+}
+
+}  // namespace
+
+cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                                       float2 *spec, const float *gcoef_dev, cudaStream_t stream,
+                                       int64_t *launches)
+{
+    ModeGradParams p;
+    p.dims = g.dims;
+    p.hc = g.hc;
+    p.half = g.half;
+    p.nrbins = t.nrbins;
+    p.bpu_half = (float)(0.5 * t.binsperunit);
+    p.nmodes = (int64_t)g.dims * g.dims * g.hc;
+    const int blocks = (int)std::min<int64_t>((p.nmodes + 255) / 256, 152 * 16);
+    k_mode_gradient<<<blocks, 256, sizeof(uint32_t) * (t.nrbins + 1), stream>>>(p, spec, d.thr,
+                                                                              d.iw, gcoef_dev);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t adjoint_gather(const GridGeom &g, float units_hi, float units_lo, const float *grid,
+                           const float *pos, const float *masses, float mass, int64_t n,
+                           float *grad_pos, float *grad_mass, float dl_dmass_norm,
+                           cudaStream_t stream, int64_t *launches)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    GatherParams p;
+    p.dims = g.dims;
+    p.plane = g.plane;
+    p.row = g.row;
+    p.uh = units_hi;
+    p.ul = units_lo;
+    p.units = units_hi + units_lo;
+    p.mass = mass;
+    p.dl_dm = dl_dmass_norm;
+    p.n = n;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
+    if (masses)
+        k_gather<true><<<blocks, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);
+    else
+        k_gather<false><<<blocks, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+}  // namespace genpk

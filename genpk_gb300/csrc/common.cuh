@@ -1,0 +1,80 @@
+// common.cuh -- device helpers shared by the deposit, binning and adjoint kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace genpk {
+
+// Position -> (wrapped cell, fraction) for one axis, as fieldize.cpp:66-76
+// computes it in FP64: x = pos*units, f = floor(x), d = x - f, f wrapped mod N.
+//
+// units = dims/boxsize is carried as an unevaluated float sum hi + lo, and the
+// product pos*units is formed exactly as xh + xl with one FMA (Dekker's
+// two-product), so d is accurate to ~1e-7 of a cell even where a plain FP32
+// product of a box-sized coordinate is only good to ~3e-5 of a cell.  The
+// integer part comes from xh; the carry into or out of [0,1) is fixed up.
+__device__ __forceinline__ void split_cell(float p, float uh, float ul, int dims, int &cell,
+                                           float &frac)
+{
+    const float xh = __fmul_rn(p, uh);
+    const float xe = fmaf(p, uh, -xh);  // exact rounding error of p*uh
+    const float xl = fmaf(p, ul, xe);
+    const float f = floorf(xh);
+    float d = __fadd_rn(__fsub_rn(xh, f), xl);
+    int fi = (int)f;
+    if (d < 0.f) {
+        d = __fadd_rn(d, 1.f);
+        fi -= 1;
+    }
+    if (d >= 1.f) {
+        d = __fsub_rn(d, 1.f);
+        fi += 1;
+    }
+    fi %= dims;
+    if (fi < 0)
+        fi += dims;
+    cell = fi;
+    frac = d;
+}
+
+// 24-bit fixed point of a fraction in [0,1); exact in FP32 on the way back.
+__device__ __forceinline__ uint32_t frac_to_q24(float d)
+{
+    uint32_t q = (uint32_t)(d * 16777216.f);
+    return q > 0xFFFFFFu ? 0xFFFFFFu : q;
+}
+
+__device__ __forceinline__ float q24_to_frac(uint32_t w)
+{
+    return (float)(w & 0xFFFFFFu) * (1.f / 16777216.f);
+}
+
+__device__ __forceinline__ bool finite3(float a, float b, float c)
+{
+    return isfinite(a) && isfinite(b) && isfinite(c);
+}
+
+// Index of the float at cell (x, y, z) of the padded grid.
+__device__ __forceinline__ size_t cell_index(int64_t plane, int row, int x, int y, int z)
+{
+    return (size_t)x * (size_t)plane + (size_t)y * (size_t)row + (size_t)z;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace genpk

@@ -1,0 +1,965 @@
+// genpk.cpp -- the C ABI (include/genpk_gb300.h): context, grid state, staging
+// of host particles, cuFFT plans and the orchestration of the kernels in
+// deposit.cu, spectrum.cu and adjoint.cu.
+//
+// Grid life cycle (per field):
+//   CLEAN     after create / genpk_zero: contents undefined; the next deposit
+//             pass overwrites instead of adding (no memset needed).
+//   DENSITY   holds the mean-subtracted CIC density (FP32, padded layout).
+//   SPECTRUM  holds its r2c transform in place (after genpk_power*).
+//   GRADIENT  holds dL/drho after genpk_adjoint; must be zeroed before reuse.
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/genpk_gb300.h"
+#include "internal.h"
+
+using namespace genpk;
+
+namespace {
+
+enum FieldState { F_CLEAN = 0, F_DENSITY = 1, F_SPECTRUM = 2, F_GRADIENT = 3 };
+
+constexpr int kMaxStages = 64;
+
+struct Pending {
+    bool active = false;
+    int field = -1;
+    double boxsize = 0.0;
+    bool varmass = false;
+    float mass = 0.f;
+};
+
+}  // namespace
+
+struct genpk_ctx {
+    int64_t dims = 0;
+    int nrbins = 0;
+    int nfields = 0;
+    unsigned flags = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    GridGeom gg{};
+
+    float *grids = nullptr;  // nfields contiguous grids of gg.nfloat floats
+    std::vector<int> state;
+    double *d_field_mass = nullptr;  // [nfields]
+    DeviceStatus *d_status = nullptr;
+
+    BinTables tables;
+    BinDevice bdev;
+
+    // cuFFT: r2c plans by batch size, one c2r plan; one shared work area.
+    std::map<int, cufftHandle> r2c;
+    cufftHandle c2r = 0;
+    bool c2r_made = false;
+    void *fft_work = nullptr;
+    size_t fft_work_size = 0;
+
+    // deposit
+    TileShape tile{16, 16, 16};
+    DepositScratch dscr;
+
+    // staging of host particles
+    float *stage_pos = nullptr;
+    float *stage_mass = nullptr;
+    int64_t stage_cap = 0;
+    int64_t stage_n = 0;
+    int64_t stage_limit = (int64_t)1 << 28;
+    Pending pend;
+
+    // binning
+    double *d_partial = nullptr;
+    size_t partial_cap = 0;
+    double *d_power = nullptr;
+    size_t power_cap = 0;
+    std::vector<std::vector<double>> auto_power;  // cached auto spectrum per field
+    std::vector<double> auto_mass;
+    std::vector<bool> auto_valid;
+
+    // adjoint scratch
+    float *d_gcoef = nullptr;
+    float *adj_buf = nullptr;  // device staging for host pos/masses/gradients
+    size_t adj_cap = 0;        // floats
+
+    // timing
+    cudaEvent_t ev[kMaxStages + 1] = {};
+    const char *stage_name[kMaxStages] = {};
+    int nev = 0;
+    int64_t launches = 0;
+
+    std::string err;
+};
+
+namespace {
+
+int fail(genpk_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx)
+        ctx->err = msg;
+    return code;
+}
+
+#define GENPK_CUDA(call)                                                                      \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? GENPK_ERR_NOMEM : GENPK_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    } while (0)
+
+#define GENPK_CUFFT(call)                                                                     \
+    do {                                                                                      \
+        cufftResult r_ = (call);                                                              \
+        if (r_ != CUFFT_SUCCESS)                                                              \
+            return fail(ctx, GENPK_ERR_CUFFT,                                                 \
+                        std::string(#call) + ": cufft error " + std::to_string((int)r_));    \
+    } while (0)
+
+#define GENPK_TRY(expr)                                                                       \
+    do {                                                                                      \
+        int s_ = (expr);                                                                      \
+        if (s_ != GENPK_OK)                                                                   \
+            return s_;                                                                        \
+    } while (0)
+
+bool is_device_ptr(const void *p)
+{
+    if (!p)
+        return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+int grow(genpk_ctx *ctx, T **ptr, size_t *cap, size_t need)
+{
+    if (*cap >= need)
+        return GENPK_OK;
+    if (*ptr) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *cap = 0;
+    }
+    GENPK_CUDA(cudaMalloc((void **)ptr, sizeof(T) * need));
+    *cap = need;
+    return GENPK_OK;
+}
+
+float *grid_of(genpk_ctx *ctx, int f)
+{
+    return ctx->grids + (size_t)f * (size_t)ctx->gg.nfloat;
+}
+
+void stage_event(genpk_ctx *ctx, const char *name)
+{
+    if (!(ctx->flags & GENPK_FLAG_TIMING) || ctx->nev > kMaxStages)
+        return;
+    if (ctx->nev > 0)
+        ctx->stage_name[ctx->nev - 1] = name;
+    cudaEventRecord(ctx->ev[ctx->nev], ctx->stream);
+    ctx->nev++;
+}
+
+// Record the start event of a timing window if none is open.  Windows are
+// opened lazily by the first work-issuing call after genpk_timing_reset.
+void timing_touch(genpk_ctx *ctx)
+{
+    if ((ctx->flags & GENPK_FLAG_TIMING) && ctx->nev == 0)
+        stage_event(ctx, nullptr);
+}
+
+void deposit_hook(void *user, const char *name)
+{
+    stage_event(static_cast<genpk_ctx *>(user), name);
+}
+
+int check_field(genpk_ctx *ctx, int f)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (f < 0 || f >= ctx->nfields)
+        return fail(ctx, GENPK_ERR_INVALID, "field index " + std::to_string(f) + " out of range");
+    return GENPK_OK;
+}
+
+// Read back and clear the device status words.
+int collect_status(genpk_ctx *ctx)
+{
+    DeviceStatus st;
+    GENPK_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st.bad_particles || st.timeouts) {
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(DeviceStatus), ctx->stream));
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (st.timeouts)
+            return fail(ctx, GENPK_ERR_TIMEOUT,
+                        std::to_string(st.timeouts) + " bounded device wait(s) gave up");
+        return fail(ctx, GENPK_ERR_BAD_INPUT,
+                    std::to_string(st.bad_particles) +
+                        " particle(s) with non-finite or out-of-range position/mass were skipped");
+    }
+    return GENPK_OK;
+}
+
+DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize)
+{
+    DepositGeom g;
+    g.grid = ctx->gg;
+    g.tx = ctx->tile.tx;
+    g.ty = ctx->tile.ty;
+    g.tz = ctx->tile.tz;
+    const int n = (int)ctx->dims;
+    g.ntx = (n + g.tx - 1) / g.tx;
+    g.nty = (n + g.ty - 1) / g.ty;
+    g.ntz = (n + g.tz - 1) / g.tz;
+    g.ntiles = g.ntx * g.nty * g.ntz;
+    g.halo_per_tile = (g.ty + 1) * (g.tz + 1) + g.tx * (g.tz + 1) + g.tx * g.ty;
+    const double units = (double)ctx->dims / boxsize;
+    g.units_hi = (float)units;
+    g.units_lo = (float)(units - (double)g.units_hi);
+    return g;
+}
+
+// One deposit pass from device particle arrays.
+int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const float *masses,
+                float mass, int64_t n)
+{
+    if (n > 0xffffffffLL - 1)
+        return fail(ctx, GENPK_ERR_UNSUPPORTED, "more than 2^32-1 particles in one pass");
+    const DepositGeom g = deposit_geom(ctx, boxsize);
+    const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
+    if (deposit_hist_smem(g) > 200 * 1024)
+        return fail(ctx, GENPK_ERR_UNSUPPORTED, "too many deposit tiles for the shared histogram");
+    DepositScratch &s = ctx->dscr;
+    GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
+    GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
+    GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
+    GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
+    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, (size_t)g.ntiles * g.halo_per_tile));
+    size_t mp = (size_t)s.mass_part_cap;
+    GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
+    s.mass_part_cap = (int)mp;
+
+    DepositArgs a;
+    a.pos = pos;
+    a.masses = masses;
+    a.mass = mass;
+    a.n = n;
+    a.grid = grid_of(ctx, f);
+    a.field_mass = ctx->d_field_mass + f;
+    a.clean = ctx->state[(size_t)f] == F_CLEAN;
+    timing_touch(ctx);
+    GENPK_CUDA(deposit_pass(g, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
+                            (ctx->flags & GENPK_FLAG_TIMING) ? deposit_hook : nullptr, ctx));
+    ctx->state[(size_t)f] = F_DENSITY;
+    ctx->auto_valid[(size_t)f] = false;
+    return GENPK_OK;
+}
+
+int flush_pending(genpk_ctx *ctx)
+{
+    if (!ctx->pend.active)
+        return GENPK_OK;
+    const Pending p = ctx->pend;
+    const int64_t n = ctx->stage_n;
+    ctx->pend.active = false;
+    ctx->stage_n = 0;
+    return run_deposit(ctx, p.field, p.boxsize, ctx->stage_pos, p.varmass ? ctx->stage_mass : nullptr,
+                       p.mass, n);
+}
+
+int ensure_stage(genpk_ctx *ctx, int64_t need)
+{
+    if (ctx->stage_cap >= need)
+        return GENPK_OK;
+    int64_t cap = std::max<int64_t>(need, std::min<int64_t>(ctx->stage_limit, 2 * ctx->stage_cap));
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    float *np = nullptr, *nm = nullptr;
+    GENPK_CUDA(cudaMalloc(&np, sizeof(float) * 3 * (size_t)cap));
+    if (cudaMalloc(&nm, sizeof(float) * (size_t)cap) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(np);
+        return fail(ctx, GENPK_ERR_NOMEM, "staging allocation failed");
+    }
+    if (ctx->stage_n > 0) {
+        GENPK_CUDA(cudaMemcpyAsync(np, ctx->stage_pos, sizeof(float) * 3 * ctx->stage_n,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+        GENPK_CUDA(cudaMemcpyAsync(nm, ctx->stage_mass, sizeof(float) * ctx->stage_n,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    cudaFree(ctx->stage_pos);
+    cudaFree(ctx->stage_mass);
+    ctx->stage_pos = np;
+    ctx->stage_mass = nm;
+    ctx->stage_cap = cap;
+    return GENPK_OK;
+}
+
+int make_r2c(genpk_ctx *ctx, int batch, cufftHandle *out)
+{
+    auto it = ctx->r2c.find(batch);
+    if (it != ctx->r2c.end()) {
+        *out = it->second;
+        return GENPK_OK;
+    }
+    const long long n = ctx->dims;
+    long long dims3[3] = {n, n, n};
+    long long inembed[3] = {n, n, (long long)ctx->gg.row};
+    long long onembed[3] = {n, n, (long long)ctx->gg.hc};
+    cufftHandle h;
+    GENPK_CUFFT(cufftCreate(&h));
+    GENPK_CUFFT(cufftSetAutoAllocation(h, 0));
+    size_t ws = 0;
+    cufftResult r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat, onembed,
+                                        1, (long long)ctx->gg.nfloat / 2, CUFFT_R2C, batch, &ws);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(ctx, GENPK_ERR_CUFFT, "cufftMakePlanMany64 (r2c) failed: " + std::to_string((int)r));
+    }
+    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
+    if (ws > ctx->fft_work_size) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->fft_work);
+        ctx->fft_work = nullptr;
+        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
+        ctx->fft_work_size = ws;
+        for (auto &kv : ctx->r2c)
+            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
+        if (ctx->c2r_made)
+            GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
+    }
+    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    ctx->r2c[batch] = h;
+    *out = h;
+    return GENPK_OK;
+}
+
+int make_c2r(genpk_ctx *ctx)
+{
+    if (ctx->c2r_made)
+        return GENPK_OK;
+    const long long n = ctx->dims;
+    long long dims3[3] = {n, n, n};
+    long long inembed[3] = {n, n, (long long)ctx->gg.hc};
+    long long onembed[3] = {n, n, (long long)ctx->gg.row};
+    cufftHandle h;
+    GENPK_CUFFT(cufftCreate(&h));
+    GENPK_CUFFT(cufftSetAutoAllocation(h, 0));
+    size_t ws = 0;
+    cufftResult r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat / 2,
+                                        onembed, 1, (long long)ctx->gg.nfloat, CUFFT_C2R, 1, &ws);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(ctx, GENPK_ERR_CUFFT, "cufftMakePlanMany64 (c2r) failed: " + std::to_string((int)r));
+    }
+    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
+    if (ws > ctx->fft_work_size) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->fft_work);
+        ctx->fft_work = nullptr;
+        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
+        ctx->fft_work_size = ws;
+        for (auto &kv : ctx->r2c)
+            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
+    }
+    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    ctx->c2r = h;
+    ctx->c2r_made = true;
+    return GENPK_OK;
+}
+
+// Bring every field in `need` to SPECTRUM form: pending deposits first, then
+// one batched r2c per run of consecutive field indices.
+int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need)
+{
+    GENPK_TRY(flush_pending(ctx));
+    std::vector<int> todo;
+    for (int f : need) {
+        const int st = ctx->state[(size_t)f];
+        if (st == F_GRADIENT)
+            return fail(ctx, GENPK_ERR_STATE,
+                        "field " + std::to_string(f) + " holds an adjoint gradient; zero it first");
+        if (st == F_CLEAN) {
+            GENPK_CUDA(cudaMemsetAsync(grid_of(ctx, f), 0, sizeof(float) * ctx->gg.nfloat,
+                                       ctx->stream));
+            ctx->state[(size_t)f] = F_DENSITY;
+        }
+        if (ctx->state[(size_t)f] == F_DENSITY)
+            todo.push_back(f);
+    }
+    std::sort(todo.begin(), todo.end());
+    todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
+    timing_touch(ctx);
+    stage_event(ctx, "host");
+    size_t i = 0;
+    while (i < todo.size()) {
+        size_t j = i + 1;
+        while (j < todo.size() && todo[j] == todo[j - 1] + 1)
+            j++;
+        const int batch = (int)(j - i);
+        cufftHandle h;
+        GENPK_TRY(make_r2c(ctx, batch, &h));
+        float *base = grid_of(ctx, todo[i]);
+        GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
+        for (size_t k = i; k < j; k++)
+            ctx->state[(size_t)todo[k]] = F_SPECTRUM;
+        i = j;
+    }
+    stage_event(ctx, "fft");
+    return GENPK_OK;
+}
+
+int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
+               double *power, int *count, double *keffs)
+{
+    if (np <= 0 || !pairs || !pair_mass || !power)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_power_multi: bad pair arguments");
+    std::vector<int> fields;
+    for (int q = 0; q < 2 * np; q++) {
+        GENPK_TRY(check_field(ctx, pairs[q]));
+        fields.push_back(pairs[q]);
+    }
+    GENPK_TRY(to_spectrum(ctx, fields));
+    std::sort(fields.begin(), fields.end());
+    fields.erase(std::unique(fields.begin(), fields.end()), fields.end());
+
+    const int nrb = ctx->nrbins;
+    GENPK_TRY(grow(ctx, &ctx->d_power, &ctx->power_cap, (size_t)np * nrb));
+    // Pairs are binned in groups whose fields fit one kernel instantiation.
+    int q0 = 0;
+    while (q0 < np) {
+        BinLaunch l;
+        l.nfields = 0;
+        l.npairs = 0;
+        int q = q0;
+        for (; q < np && l.npairs < kMaxBinPairs; q++) {
+            int slot[2];
+            int added = 0;
+            for (int e = 0; e < 2; e++) {
+                const float2 *fp = (const float2 *)grid_of(ctx, pairs[2 * q + e]);
+                slot[e] = -1;
+                for (int k = 0; k < l.nfields; k++)
+                    if (l.fields[k] == fp)
+                        slot[e] = k;
+                if (slot[e] < 0) {
+                    if (l.nfields + added >= kMaxBinFields) {
+                        slot[e] = -2;
+                    } else {
+                        slot[e] = l.nfields + added;
+                        l.fields[slot[e]] = fp;
+                        added++;
+                    }
+                }
+            }
+            if (slot[0] == -2 || slot[1] == -2)
+                break;
+            l.nfields += added;
+            l.pairs[l.npairs].a = slot[0];
+            l.pairs[l.npairs].b = slot[1];
+            l.pairs[l.npairs].mass_a = pair_mass[2 * q];
+            l.pairs[l.npairs].mass_b = pair_mass[2 * q + 1];
+            l.npairs++;
+        }
+        int warps = 0;
+        size_t smem = 0;
+        const int ctas = bin_ctas(ctx->gg, nrb, l.npairs, l.nfields, ctx->num_sms, &warps, &smem);
+        if (ctas <= 0)
+            return fail(ctx, GENPK_ERR_UNSUPPORTED, "nrbins too large for the binning kernel");
+        GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * l.npairs * nrb));
+        GENPK_CUDA(bin_spectra(ctx->gg, ctx->tables, ctx->bdev, l, ctx->d_partial,
+                               ctx->d_power + (size_t)q0 * nrb, ctas, warps, smem, ctx->stream,
+                               &ctx->launches));
+        q0 = q;
+    }
+    stage_event(ctx, "bin");
+    GENPK_CUDA(cudaMemcpyAsync(power, ctx->d_power, sizeof(double) * np * nrb,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    stage_event(ctx, "d2h");
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int b = 0; b < nrb; b++) {
+        if (count)
+            count[b] = (int)ctx->tables.count[(size_t)b];
+        if (keffs)
+            keffs[b] = ctx->tables.keffs[(size_t)b];
+    }
+    for (int q = 0; q < np; q++) {
+        if (pairs[2 * q] == pairs[2 * q + 1] && pair_mass[2 * q] == pair_mass[2 * q + 1]) {
+            const int f = pairs[2 * q];
+            ctx->auto_power[(size_t)f].assign(power + (size_t)q * nrb, power + (size_t)(q + 1) * nrb);
+            ctx->auto_mass[(size_t)f] = pair_mass[2 * q];
+            ctx->auto_valid[(size_t)f] = true;
+        }
+    }
+    return collect_status(ctx);
+}
+
+// Device copies of particle arrays for the adjoint when the caller passed host memory.
+int adj_stage(genpk_ctx *ctx, size_t floats)
+{
+    return grow(ctx, &ctx->adj_buf, &ctx->adj_cap, floats);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *genpk_status_string(int status)
+{
+    switch (status) {
+    case GENPK_OK: return "ok";
+    case GENPK_ERR_INVALID: return "invalid argument";
+    case GENPK_ERR_CUDA: return "CUDA error";
+    case GENPK_ERR_CUFFT: return "cuFFT error";
+    case GENPK_ERR_NOMEM: return "out of memory";
+    case GENPK_ERR_BAD_INPUT: return "bad particle data";
+    case GENPK_ERR_STATE: return "invalid grid state";
+    case GENPK_ERR_UNSUPPORTED: return "unsupported size or option";
+    case GENPK_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+const char *genpk_last_error(const genpk_ctx *ctx)
+{
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+void genpk_ctx_destroy(genpk_ctx *ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->r2c)
+        cufftDestroy(kv.second);
+    if (ctx->c2r_made)
+        cufftDestroy(ctx->c2r);
+    cudaFree(ctx->fft_work);
+    cudaFree(ctx->grids);
+    cudaFree(ctx->d_field_mass);
+    cudaFree(ctx->d_status);
+    cudaFree(ctx->bdev.thr);
+    cudaFree(ctx->bdev.iw);
+    cudaFree(ctx->bdev.count);
+    cudaFree(ctx->dscr.hist);
+    cudaFree(ctx->dscr.tile_start);
+    cudaFree(ctx->dscr.totals);
+    cudaFree(ctx->dscr.sorted);
+    cudaFree(ctx->dscr.halo);
+    cudaFree(ctx->dscr.mass_part);
+    cudaFree(ctx->stage_pos);
+    cudaFree(ctx->stage_mass);
+    cudaFree(ctx->d_partial);
+    cudaFree(ctx->d_power);
+    cudaFree(ctx->d_gcoef);
+    cudaFree(ctx->adj_buf);
+    for (auto &e : ctx->ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (ctx->stream)
+        cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genpk_ctx **out)
+{
+    if (!out)
+        return GENPK_ERR_INVALID;
+    *out = nullptr;
+    if (dims < 2 || dims > 4096 || nrbins < 1 || nrbins > 65536 || nfields < 1 ||
+        nfields > GENPK_MAX_FIELDS)
+        return GENPK_ERR_INVALID;
+    genpk_ctx *ctx = new genpk_ctx();
+    ctx->dims = dims;
+    ctx->nrbins = nrbins;
+    ctx->nfields = nfields;
+    ctx->flags = flags;
+    ctx->gg = make_grid_geom((int)dims);
+    int rc = GENPK_OK;
+    auto bail = [&](int code) {
+        *out = ctx;  // keep the error message readable; caller destroys
+        return code;
+    };
+    std::string terr;
+    if (!build_bin_tables(dims, nrbins, &ctx->tables, &terr)) {
+        ctx->err = terr;
+        return bail(GENPK_ERR_UNSUPPORTED);
+    }
+#define CREATE_CUDA(call)                                                                     \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                    \
+            return bail(e_ == cudaErrorMemoryAllocation ? GENPK_ERR_NOMEM : GENPK_ERR_CUDA);  \
+        }                                                                                     \
+    } while (0)
+    CREATE_CUDA(cudaGetDevice(&ctx->device));
+    CREATE_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    CREATE_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (auto &e : ctx->ev)
+        CREATE_CUDA(cudaEventCreate(&e));
+    CREATE_CUDA(cudaMalloc(&ctx->grids, sizeof(float) * (size_t)ctx->gg.nfloat * nfields));
+    CREATE_CUDA(cudaMalloc(&ctx->d_field_mass, sizeof(double) * nfields));
+    CREATE_CUDA(cudaMemset(ctx->d_field_mass, 0, sizeof(double) * nfields));
+    CREATE_CUDA(cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)));
+    CREATE_CUDA(cudaMemset(ctx->d_status, 0, sizeof(DeviceStatus)));
+    CREATE_CUDA(cudaMalloc(&ctx->bdev.thr, sizeof(uint32_t) * (nrbins + 1)));
+    CREATE_CUDA(cudaMemcpy(ctx->bdev.thr, ctx->tables.thr.data(), sizeof(uint32_t) * (nrbins + 1),
+                           cudaMemcpyHostToDevice));
+    CREATE_CUDA(cudaMalloc(&ctx->bdev.iw, sizeof(float) * dims));
+    CREATE_CUDA(cudaMemcpy(ctx->bdev.iw, ctx->tables.iw.data(), sizeof(float) * dims,
+                           cudaMemcpyHostToDevice));
+    std::vector<double> cnt((size_t)nrbins);
+    for (int b = 0; b < nrbins; b++)
+        cnt[(size_t)b] = (double)ctx->tables.count[(size_t)b];
+    CREATE_CUDA(cudaMalloc(&ctx->bdev.count, sizeof(double) * nrbins));
+    CREATE_CUDA(cudaMemcpy(ctx->bdev.count, cnt.data(), sizeof(double) * nrbins,
+                           cudaMemcpyHostToDevice));
+    CREATE_CUDA(cudaMalloc(&ctx->d_gcoef, sizeof(float) * nrbins));
+#undef CREATE_CUDA
+    ctx->state.assign((size_t)nfields, F_CLEAN);
+    ctx->auto_power.assign((size_t)nfields, {});
+    ctx->auto_mass.assign((size_t)nfields, 0.0);
+    ctx->auto_valid.assign((size_t)nfields, false);
+    ctx->tile = deposit_default_tile((int)dims, 0);
+    (void)rc;
+    *out = ctx;
+    return GENPK_OK;
+}
+
+int genpk_zero(genpk_ctx *ctx, int field)
+{
+    GENPK_TRY(check_field(ctx, field));
+    cudaSetDevice(ctx->device);
+    if (ctx->pend.active && ctx->pend.field == field)
+        GENPK_TRY(flush_pending(ctx));
+    ctx->state[(size_t)field] = F_CLEAN;
+    ctx->auto_valid[(size_t)field] = false;
+    GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
+    return GENPK_OK;
+}
+
+int genpk_deposit(genpk_ctx *ctx, int field, double boxsize, const float *pos, const float *masses,
+                  double mass, int64_t n)
+{
+    GENPK_TRY(check_field(ctx, field));
+    if (n < 0 || (n > 0 && !pos) || !(boxsize > 0.0) || !isfinite(boxsize))
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_deposit: bad n, pos or boxsize");
+    if (!masses && !isfinite(mass))
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_deposit: non-finite uniform mass");
+    cudaSetDevice(ctx->device);
+    const int st = ctx->state[(size_t)field];
+    if (st == F_SPECTRUM || st == F_GRADIENT)
+        return fail(ctx, GENPK_ERR_STATE,
+                    "field " + std::to_string(field) + " is not a density; call genpk_zero first");
+    if (n == 0)
+        return GENPK_OK;
+    const bool pos_dev = is_device_ptr(pos);
+    const bool mass_dev = masses ? is_device_ptr(masses) : pos_dev;
+    if (pos_dev && mass_dev) {
+        GENPK_TRY(flush_pending(ctx));
+        return run_deposit(ctx, field, boxsize, pos, masses, (float)mass, n);
+    }
+    // Stage host data on the device; merge with the pending pass when compatible.
+    const bool var = masses != nullptr;
+    const Pending &p = ctx->pend;
+    const bool compatible = p.active && p.field == field && p.boxsize == boxsize &&
+                            p.varmass == var && (var || p.mass == (float)mass);
+    if (p.active && (!compatible || ctx->stage_n + n > ctx->stage_limit))
+        GENPK_TRY(flush_pending(ctx));
+    GENPK_TRY(ensure_stage(ctx, ctx->stage_n + n));
+    const int64_t off = ctx->stage_n;
+    GENPK_CUDA(cudaMemcpyAsync(ctx->stage_pos + 3 * off, pos, sizeof(float) * 3 * (size_t)n,
+                               pos_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               ctx->stream));
+    if (var)
+        GENPK_CUDA(cudaMemcpyAsync(ctx->stage_mass + off, masses, sizeof(float) * (size_t)n,
+                                   mass_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    // The caller may free or reuse its host buffers as soon as we return.
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->stage_n += n;
+    ctx->pend.active = true;
+    ctx->pend.field = field;
+    ctx->pend.boxsize = boxsize;
+    ctx->pend.varmass = var;
+    ctx->pend.mass = (float)mass;
+    if (ctx->state[(size_t)field] == F_CLEAN)
+        ctx->auto_valid[(size_t)field] = false;
+    return GENPK_OK;
+}
+
+int genpk_power(genpk_ctx *ctx, int field_a, int field_b, double mass_a, double mass_b,
+                double *power, int *count, double *keffs)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    const int pairs[2] = {field_a, field_b};
+    const double masses[2] = {mass_a, mass_b};
+    return power_impl(ctx, 1, pairs, masses, power, count, keffs);
+}
+
+int genpk_power_multi(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
+                      double *power, int *count, double *keffs)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    return power_impl(ctx, np, pairs, pair_mass, power, count, keffs);
+}
+
+double genpk_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n)
+{
+    return ref_invwindow(kx, ky, kz, n);
+}
+
+int genpk_geometry(int64_t dims, int nrbins, int *count, double *keffs)
+{
+    if (dims < 2 || dims > 4096 || nrbins < 1 || !count || !keffs)
+        return GENPK_ERR_INVALID;
+    BinTables t;
+    std::string err;
+    if (!build_bin_tables(dims, nrbins, &t, &err))
+        return GENPK_ERR_UNSUPPORTED;
+    for (int b = 0; b < nrbins; b++) {
+        count[b] = (int)t.count[(size_t)b];
+        keffs[b] = t.keffs[(size_t)b];
+    }
+    return GENPK_OK;
+}
+
+int genpk_load_spectrum(genpk_ctx *ctx, int field, const double *spectrum)
+{
+    GENPK_TRY(check_field(ctx, field));
+    if (!spectrum)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_load_spectrum: null spectrum");
+    cudaSetDevice(ctx->device);
+    if (ctx->pend.active && ctx->pend.field == field)
+        GENPK_TRY(flush_pending(ctx));
+    const size_t nc = (size_t)ctx->gg.nfloat;  // 2 floats per complex value
+    std::vector<float> tmp(nc);
+    for (size_t i = 0; i < nc; i++)
+        tmp[i] = (float)spectrum[i];
+    GENPK_CUDA(cudaMemcpyAsync(grid_of(ctx, field), tmp.data(), sizeof(float) * nc,
+                               cudaMemcpyHostToDevice, ctx->stream));
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->state[(size_t)field] = F_SPECTRUM;
+    ctx->auto_valid[(size_t)field] = false;
+    return GENPK_OK;
+}
+
+int genpk_bin_of(const genpk_ctx *ctx, int64_t kk2)
+{
+    if (!ctx || kk2 < 0 || kk2 > ctx->tables.kk2max)
+        return -1;
+    return ctx->tables.lut[(size_t)kk2];
+}
+
+int genpk_sync(genpk_ctx *ctx)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    GENPK_TRY(flush_pending(ctx));
+    return collect_status(ctx);
+}
+
+int genpk_read_field(genpk_ctx *ctx, int field, double *out)
+{
+    GENPK_TRY(check_field(ctx, field));
+    if (!out)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_read_field: null output");
+    cudaSetDevice(ctx->device);
+    GENPK_TRY(flush_pending(ctx));
+    const int st = ctx->state[(size_t)field];
+    const size_t nf = (size_t)ctx->gg.nfloat;
+    if (st == F_CLEAN) {
+        memset(out, 0, sizeof(double) * nf);
+        return collect_status(ctx);
+    }
+    if (st != F_DENSITY)
+        return fail(ctx, GENPK_ERR_STATE, "genpk_read_field: field is not a density");
+    std::vector<float> tmp(nf);
+    double mass = 0.0;
+    GENPK_CUDA(cudaMemcpyAsync(tmp.data(), grid_of(ctx, field), sizeof(float) * nf,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    GENPK_CUDA(cudaMemcpyAsync(&mass, ctx->d_field_mass + field, sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    const double n = (double)ctx->dims;
+    const double mean = mass / (n * n * n);
+    const int row = ctx->gg.row, dims = (int)ctx->dims;
+    for (size_t i = 0; i < nf; i++) {
+        const int z = (int)(i % (size_t)row);
+        out[i] = z < dims ? (double)tmp[i] + mean : 0.0;
+    }
+    return collect_status(ctx);
+}
+
+int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, const float *masses,
+                  double mass, int64_t n, double mass_norm, const double *dl_dp, float *grad_pos,
+                  float *grad_mass, double *dl_dmass_norm, int recompute)
+{
+    GENPK_TRY(check_field(ctx, field));
+    if (n < 0 || (n > 0 && (!pos || !grad_pos)) || !dl_dp || !(boxsize > 0.0) ||
+        !(mass_norm != 0.0) || (masses && !grad_mass))
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_adjoint: bad arguments");
+    cudaSetDevice(ctx->device);
+    GENPK_TRY(flush_pending(ctx));
+    const bool dev = is_device_ptr(pos);
+    if (dev != is_device_ptr(grad_pos) || (masses && dev != is_device_ptr(masses)) ||
+        (grad_mass && dev != is_device_ptr(grad_mass)))
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_adjoint: mix of host and device pointers");
+    const int nrb = ctx->nrbins;
+    const float *dpos = pos, *dmass = masses;
+    float *dgpos = grad_pos, *dgmass = grad_mass;
+    if (!dev) {
+        const size_t need = (size_t)n * (3 + 3) + (masses ? 2 * (size_t)n : 0) + 1;
+        GENPK_TRY(adj_stage(ctx, need));
+        float *b = ctx->adj_buf;
+        float *sp = b, *sg = b + 3 * (size_t)n;
+        float *sm = masses ? sg + 3 * (size_t)n : nullptr;
+        float *sgm = masses ? sm + (size_t)n : nullptr;
+        GENPK_CUDA(cudaMemcpyAsync(sp, pos, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+        if (masses)
+            GENPK_CUDA(cudaMemcpyAsync(sm, masses, sizeof(float) * (size_t)n,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        dpos = sp;
+        dmass = sm;
+        dgpos = sg;
+        dgmass = sgm;
+    }
+    const bool have = ctx->state[(size_t)field] == F_SPECTRUM && ctx->auto_valid[(size_t)field] &&
+                      ctx->auto_mass[(size_t)field] == mass_norm;
+    std::vector<double> pw((size_t)nrb);
+    if (recompute || !have) {
+        ctx->state[(size_t)field] = F_CLEAN;
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
+        GENPK_TRY(run_deposit(ctx, field, boxsize, dpos, dmass, (float)mass, n));
+        GENPK_TRY(genpk_power(ctx, field, field, mass_norm, mass_norm, pw.data(), nullptr, nullptr));
+    } else {
+        pw = ctx->auto_power[(size_t)field];
+    }
+    timing_touch(ctx);
+    stage_event(ctx, "host");
+    // dL/dM and the per-bin coefficients G_b = 2 g_b / (M^2 C_b).
+    double dldm = 0.0;
+    std::vector<float> gcoef((size_t)nrb, 0.f);
+    for (int b = 0; b < nrb; b++) {
+        dldm += dl_dp[b] * (-2.0 * pw[(size_t)b] / mass_norm);
+        const double c = (double)ctx->tables.count[(size_t)b];
+        if (c > 0)
+            gcoef[(size_t)b] = (float)(2.0 * dl_dp[b] / (mass_norm * mass_norm * c));
+    }
+    if (dl_dmass_norm)
+        *dl_dmass_norm = dldm;
+    GENPK_CUDA(cudaMemcpyAsync(ctx->d_gcoef, gcoef.data(), sizeof(float) * nrb,
+                               cudaMemcpyHostToDevice, ctx->stream));
+    float *g = grid_of(ctx, field);
+    GENPK_CUDA(adjoint_mode_gradient_coef(ctx->gg, ctx->tables, ctx->bdev, (float2 *)g,
+                                          ctx->d_gcoef, ctx->stream, &ctx->launches));
+    stage_event(ctx, "adj_modes");
+    GENPK_TRY(make_c2r(ctx));
+    GENPK_CUFFT(cufftExecC2R(ctx->c2r, (cufftComplex *)g, (cufftReal *)g));
+    ctx->state[(size_t)field] = F_GRADIENT;
+    ctx->auto_valid[(size_t)field] = false;
+    stage_event(ctx, "adj_c2r");
+    const DepositGeom dg = deposit_geom(ctx, boxsize);
+    GENPK_CUDA(adjoint_gather(ctx->gg, dg.units_hi, dg.units_lo, g, dpos, dmass, (float)mass, n,
+                              dgpos, dgmass, (float)dldm, ctx->stream, &ctx->launches));
+    stage_event(ctx, "adj_gather");
+    if (!dev) {
+        GENPK_CUDA(cudaMemcpyAsync(grad_pos, dgpos, sizeof(float) * 3 * (size_t)n,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        if (masses)
+            GENPK_CUDA(cudaMemcpyAsync(grad_mass, dgmass, sizeof(float) * (size_t)n,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return collect_status(ctx);
+}
+
+int genpk_timing_reset(genpk_ctx *ctx)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    ctx->nev = 0;
+    return GENPK_OK;
+}
+
+int genpk_stage_times(const genpk_ctx *ctx, const char **names, float *ms, int cap)
+{
+    if (!ctx || !(ctx->flags & GENPK_FLAG_TIMING))
+        return 0;
+    int k = 0;
+    for (int i = 0; i + 1 < ctx->nev && k < cap; i++, k++) {
+        float t = 0.f;
+        cudaEventSynchronize(ctx->ev[i + 1]);
+        cudaEventElapsedTime(&t, ctx->ev[i], ctx->ev[i + 1]);
+        if (names)
+            names[k] = ctx->stage_name[i];
+        if (ms)
+            ms[k] = t;
+    }
+    return k;
+}
+
+int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
+                         int *sort_ctas)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (tile_x)
+        *tile_x = ctx->tile.tx;
+    if (tile_y)
+        *tile_y = ctx->tile.ty;
+    if (tile_z)
+        *tile_z = ctx->tile.tz;
+    if (sort_ctas) {
+        DepositGeom g = deposit_geom(const_cast<genpk_ctx *>(ctx), 1.0);
+        *sort_ctas = deposit_sort_ctas(g, (int64_t)1 << 30, ctx->num_sms);
+    }
+    return GENPK_OK;
+}
+
+int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (!deposit_tile_supported(tile_x, tile_y, tile_z))
+        return fail(ctx, GENPK_ERR_UNSUPPORTED, "deposit tile shape not instantiated");
+    GENPK_TRY(flush_pending(ctx));
+    const TileShape old = ctx->tile;
+    ctx->tile = TileShape{tile_x, tile_y, tile_z};
+    if (deposit_hist_smem(deposit_geom(ctx, 1.0)) > 200 * 1024) {
+        ctx->tile = old;
+        return fail(ctx, GENPK_ERR_UNSUPPORTED, "too many tiles of that shape for this grid");
+    }
+    return GENPK_OK;
+}
+
+int64_t genpk_kernel_launches(const genpk_ctx *ctx)
+{
+    return ctx ? ctx->launches : -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,164 @@
+// internal.h -- declarations shared by the host orchestration (genpk.cpp), the
+// bin tables (tables.cpp) and the CUDA kernels (*.cu).  Not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace genpk {
+
+// ---------------------------------------------------------------------------
+// Grid layout: dims x dims x row floats, row = 2*(dims/2+1) (the in-place r2c
+// layout of gen-pk.cpp:176), x slowest.
+// ---------------------------------------------------------------------------
+struct GridGeom {
+    int dims;        // N
+    int half;        // N/2
+    int hc;          // complex values per row: N/2+1
+    int row;         // floats per row: 2*hc
+    int64_t plane;   // floats per x-plane: row*N
+    int64_t nfloat;  // floats in the grid: plane*N
+};
+
+GridGeom make_grid_geom(int dims);
+
+// ---------------------------------------------------------------------------
+// Deposit
+// ---------------------------------------------------------------------------
+struct DepositGeom {
+    GridGeom grid;
+    int tx, ty, tz;      // tile edge lengths in cells
+    int ntx, nty, ntz;   // tiles per axis (ceil)
+    int ntiles;
+    int halo_per_tile;   // floats of halo scratch per tile
+    float units_hi;      // dims/boxsize split into two floats (hi + lo)
+    float units_lo;
+};
+
+// Scratch the deposit pass needs; owned by the context, grown on demand.
+struct DepositScratch {
+    uint32_t *hist = nullptr;        // [sort_ctas][ntiles]; becomes the scatter offsets
+    size_t hist_cap = 0;             // elements
+    uint32_t *tile_start = nullptr;  // [ntiles + 1]
+    size_t tile_start_cap = 0;
+    uint32_t *totals = nullptr;      // [ntiles]
+    size_t tile_cap = 0;
+    uint4 *sorted = nullptr;         // [cap] packed tile-local particles (x,y,z words, mass bits)
+    size_t sorted_cap = 0;           // particles
+    float *halo = nullptr;           // [ntiles][halo_per_tile]
+    size_t halo_cap = 0;             // floats
+    double *mass_part = nullptr;     // [sort_ctas]
+    int mass_part_cap = 0;
+};
+
+// Device words a deposit pass reports through (all zero-initialised).
+struct DeviceStatus {
+    unsigned long long bad_particles;  // non-finite positions seen (skipped)
+    unsigned long long timeouts;       // bounded waits that gave up
+    double pass_mass;                  // mass deposited by the latest pass
+};
+
+struct DepositArgs {
+    const float *pos;      // device [n][3]
+    const float *masses;   // device [n] or nullptr
+    float mass;            // uniform mass when masses == nullptr
+    int64_t n;
+    float *grid;           // device padded grid
+    double *field_mass;    // device: running mass of this grid
+    bool clean;            // grid content is undefined and must be overwritten
+};
+
+// Tile shapes the deposit kernels are instantiated for.
+struct TileShape {
+    int tx, ty, tz;
+};
+bool deposit_tile_supported(int tx, int ty, int tz);
+TileShape deposit_default_tile(int dims, int64_t n);
+int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms);
+size_t deposit_hist_smem(const DepositGeom &g);
+
+// Called after each kernel launch of a pass with the kernel's short name
+// (used to record timing events); may be null.
+typedef void (*StageHook)(void *user, const char *name);
+
+// Launches the kernels of one deposit pass on `stream`.  Returns cudaSuccess
+// or the first launch error.  *launches is incremented per kernel launched.
+cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScratch &s,
+                         DeviceStatus *dstat, int sort_ctas, cudaStream_t stream,
+                         int64_t *launches, StageHook hook, void *hook_user);
+
+// ---------------------------------------------------------------------------
+// Binning (deconvolution + log-k shells)
+// ---------------------------------------------------------------------------
+struct BinTables {
+    int64_t dims = 0;
+    int nrbins = 0;
+    double binsperunit = 0.0;
+    int64_t kk2max = 0;
+    std::vector<uint32_t> thr;    // [nrbins+1]: smallest |k|^2 whose bin is >= b
+    std::vector<float> iw;        // [dims]: float onedinvwindow(KVAL(i), dims)
+    std::vector<int64_t> count;   // [nrbins] weighted mode counts
+    std::vector<double> keffs;    // [nrbins] mean |k| (already divided by count)
+    std::vector<int32_t> lut;     // [kk2max+1] bin of |k|^2 (-1 for 0)
+};
+
+// Build all tables with the reference's expressions.  Returns false and sets
+// *err on failure (non-monotone bins, bin index out of range).
+bool build_bin_tables(int64_t dims, int nrbins, BinTables *t, std::string *err);
+double ref_onedinvwindow(int64_t k, int64_t n);
+double ref_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
+
+struct BinDevice {
+    uint32_t *thr = nullptr;   // [nrbins+1]
+    float *iw = nullptr;       // [dims]
+    double *count = nullptr;   // [nrbins] as double (exact up to 2^53)
+    double *keffs = nullptr;   // [nrbins]
+};
+
+// One spectrum pair: indexes into the `fields` array of the launch.
+struct BinPair {
+    int a, b;
+    double mass_a, mass_b;
+};
+
+constexpr int kMaxBinFields = 4;
+constexpr int kMaxBinPairs = 10;
+
+struct BinLaunch {
+    const float2 *fields[kMaxBinFields];  // half-complex spectra (in-place layout)
+    int nfields;
+    BinPair pairs[kMaxBinPairs];
+    int npairs;
+};
+
+int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms, int *warps,
+             size_t *smem);
+
+// Runs the binning kernel and the finalize kernel; writes out_power[np][nrbins]
+// on the device.  partial must hold ctas*npairs*nrbins doubles.
+cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                        const BinLaunch &l, double *partial, double *out_power, int ctas,
+                        int warps, size_t smem, cudaStream_t stream, int64_t *launches);
+
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+// Replace the spectrum F in `spec` (in place) by the c2r input H of the
+// density gradient for the auto spectrum: H_m = G_b V_m (c_m / mult_m) F_m with
+// gcoef_dev[b] = G_b = 2 g_b / (M^2 C_b) (device, nrbins floats).
+cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                                       float2 *spec, const float *gcoef_dev, cudaStream_t stream,
+                                       int64_t *launches);
+
+// CIC gather of the real gradient grid: grad_pos[n][3], grad_mass[n] (optional).
+cudaError_t adjoint_gather(const GridGeom &g, float units_hi, float units_lo, const float *grid,
+                           const float *pos, const float *masses, float mass, int64_t n,
+                           float *grad_pos, float *grad_mass, float dl_dmass_norm,
+                           cudaStream_t stream, int64_t *launches);
+
+int device_sm_count();
+
+}  // namespace genpk

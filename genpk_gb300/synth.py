@@ -1,0 +1,138 @@
+"""Seeded synthetic particle sets for tests and benchmarks.
+
+The reference names no public dataset; these generators produce inputs with
+the shapes, sizes and value distributions of the benchmark workloads:
+
+* ``uniform``    i.i.d. uniform float32 positions in [0, box).
+* ``zeldovich``  a regular lattice displaced by the Zel'dovich approximation
+                 from a Gaussian random field with P(k) = A k^-2 exp(-(k/k_c)^2),
+                 k_c = kc_frac * k_Nyquist, scaled so the RMS 3-D displacement
+                 is ``rms`` lattice spacings, wrapped periodically, stored as
+                 float32 in lattice order (x slowest).
+* ``lognormal``  particles Poisson-sampled from a lognormal density
+                 exp(sigma g - sigma^2/2) of a Gaussian field g, jittered
+                 uniformly inside their cell; optional lognormal masses.
+
+numpy implementations run anywhere; ``device="cuda"`` builds the same
+construction with torch on the GPU (used for the large benchmark sets).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def uniform(n: int, box: float, seed: int = 1, device: str = "cpu"):
+    if device != "cpu":
+        import torch
+        g = torch.Generator(device=device).manual_seed(seed)
+        return (torch.rand((n, 3), generator=g, device=device, dtype=torch.float32) * box).clamp_(
+            max=np.nextafter(np.float32(box), np.float32(0)))
+    rng = np.random.default_rng(seed)
+    pos = (rng.random((n, 3)) * box).astype(np.float32)
+    pos[pos >= np.float32(box)] = np.nextafter(np.float32(box), np.float32(0))
+    return pos
+
+
+def _kgrid_np(n):
+    k = np.fft.fftfreq(n) * n
+    kz = np.arange(n // 2 + 1, dtype=np.float64)
+    return k, kz
+
+
+def zeldovich(nside: int, box: float, seed: int = 1, rms: float = 0.3, kc_frac: float = 0.5,
+              amplitude: float = 1.0, device: str = "cpu"):
+    """nside^3 particles, lattice + Zel'dovich displacement (see module doc)."""
+    if device != "cpu":
+        return _zeldovich_torch(nside, box, seed, rms, kc_frac, amplitude, device)
+    rng = np.random.default_rng(seed)
+    n = nside
+    white = rng.standard_normal((n, n, n))
+    wk = np.fft.rfftn(white)
+    k, kz = _kgrid_np(n)
+    kx, ky, kzz = np.meshgrid(k, k, kz, indexing="ij")
+    k2 = kx * kx + ky * ky + kzz * kzz
+    kc = kc_frac * (n / 2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = np.where(k2 > 0, np.sqrt(k2 ** -1.0 * np.exp(-k2 / kc ** 2)), 0.0)
+        dk = wk * amp
+        # psi_k = i k / k^2 delta_k
+        inv = np.where(k2 > 0, 1.0 / k2, 0.0)
+    psi = [np.fft.irfftn(1j * kk * inv * dk, s=(n, n, n)) for kk in (kx, ky, kzz)]
+    cur = np.sqrt(np.mean(psi[0] ** 2 + psi[1] ** 2 + psi[2] ** 2))
+    spacing = box / n
+    scale = amplitude * rms * spacing / cur
+    idx = np.arange(n, dtype=np.float64) * spacing
+    lx, ly, lz = np.meshgrid(idx, idx, idx, indexing="ij")
+    pos = np.stack([lx + scale * psi[0], ly + scale * psi[1], lz + scale * psi[2]], axis=-1)
+    pos = np.mod(pos, box).reshape(-1, 3).astype(np.float32)
+    pos[pos >= np.float32(box)] = 0.0
+    return pos
+
+
+def _zeldovich_torch(nside, box, seed, rms, kc_frac, amplitude, device):
+    import torch
+    n = nside
+    g = torch.Generator(device=device).manual_seed(seed)
+    white = torch.randn((n, n, n), generator=g, device=device, dtype=torch.float32)
+    wk = torch.fft.rfftn(white)
+    del white
+    k = torch.fft.fftfreq(n, device=device, dtype=torch.float32) * n
+    kz = torch.arange(n // 2 + 1, device=device, dtype=torch.float32)
+    kc = kc_frac * (n / 2)
+    spacing = box / n
+    out = torch.empty((n, n, n, 3), device=device, dtype=torch.float32)
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+    amp = torch.where(k2 > 0, torch.rsqrt(k2.clamp(min=1e-30)) * torch.exp(-0.5 * k2 / kc ** 2),
+                      torch.zeros((), device=device))
+    inv = torch.where(k2 > 0, 1.0 / k2.clamp(min=1e-30), torch.zeros((), device=device))
+    dk = wk * (amp * inv)
+    del wk, amp, inv, k2
+    sumsq = 0.0
+    comps = []
+    for axis in range(3):
+        if axis == 0:
+            kk = k[:, None, None]
+        elif axis == 1:
+            kk = k[None, :, None]
+        else:
+            kk = kz[None, None, :]
+        psi = torch.fft.irfftn(1j * kk * dk, s=(n, n, n))
+        sumsq += float((psi.double() ** 2).mean())
+        comps.append(psi)
+    scale = amplitude * rms * spacing / np.sqrt(sumsq)
+    idx = torch.arange(n, device=device, dtype=torch.float64) * spacing
+    lat = [idx[:, None, None], idx[None, :, None], idx[None, None, :]]
+    for axis in range(3):
+        p = (lat[axis] + scale * comps[axis].double()).remainder(box)
+        out[..., axis] = p.float()
+    comps.clear()
+    out[out >= box] = 0.0
+    return out.reshape(-1, 3)
+
+
+def lognormal(n_mean: int, box: float, ngrid: int, sigma: float = 1.5, seed: int = 1,
+              mass_mu=None, mass_sigma=None):
+    """~n_mean particles from a lognormal field on an ngrid^3 mesh (numpy).
+    Returns (pos float32 [n,3], masses float32 [n] or None)."""
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((ngrid,) * 3)
+    gk = np.fft.rfftn(g)
+    k, kz = _kgrid_np(ngrid)
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+    kc = 0.25 * ngrid
+    gk *= np.exp(-0.5 * k2 / kc ** 2)
+    g = np.fft.irfftn(gk, s=(ngrid,) * 3)
+    g /= g.std()
+    rho = np.exp(sigma * g - 0.5 * sigma ** 2)
+    lam = rho * (n_mean / rho.sum())
+    counts = rng.poisson(lam).reshape(-1)
+    cells = np.repeat(np.arange(counts.size), counts)
+    ix, iy, iz = np.unravel_index(cells, (ngrid,) * 3)
+    cell = box / ngrid
+    pos = np.stack([ix, iy, iz], axis=-1) + rng.random((cells.size, 3))
+    pos = (pos * cell).astype(np.float32)
+    pos[pos >= np.float32(box)] = 0.0
+    masses = None
+    if mass_mu is not None:
+        masses = rng.lognormal(mass_mu, mass_sigma, cells.size).astype(np.float32)
+    return pos, masses

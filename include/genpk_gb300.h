@@ -1,0 +1,180 @@
+/*
+ * genpk_gb300.h -- C ABI of the GB300 (sm_103a) power-spectrum hot path.
+ *
+ * This library replaces GenPK's CIC deposit, FFT and binning calls:
+ *
+ *   reference call                                 replaced by
+ *   ---------------------------------------------  -----------------------------
+ *   fftw_malloc + fftw_plan_dft_r2c_3d             genpk_ctx_create
+ *     (gen-pk.cpp:176-193, :263-270, :314-321)
+ *   memset(field, 0, ...) (gen-pk.cpp:208,267)     genpk_zero
+ *   fieldize() (gen-pk.h:93, fieldize.cpp:46)      genpk_deposit
+ *     called from read_fieldize.cpp:90,333 and
+ *     read_fieldize_bigfile.cpp:121
+ *   fftw_execute + powerspectrum()                 genpk_power
+ *     (gen-pk.cpp:233-234, :295-297, :345-348;
+ *      gen-pk.h:119, powerspectrum.c:35)
+ *   invwindow() (gen-pk.h:104, fieldize.cpp:125)   genpk_invwindow
+ *   fftw_free / fftw_destroy_plan                  genpk_ctx_destroy
+ *     (gen-pk.cpp:363-364)
+ *
+ * and adds what the reference does not have: batched multi-field spectra
+ * (genpk_power_multi) and the adjoint of a P(k) loss (genpk_adjoint).
+ *
+ * Conventions
+ *  - Every function returns a genpk_status; nothing aborts, exits or asserts.
+ *    genpk_last_error(ctx) gives a message for the last failure on ctx.
+ *  - Grids live on the GPU.  A context owns `nfields` FP32 grids of
+ *    dims x dims x 2*(dims/2+1) floats: the in-place r2c layout FFTW and cuFFT
+ *    share (gen-pk.cpp:176), x slowest, z fastest.
+ *  - Particle pointers may be host or device memory.  Host buffers are copied
+ *    before genpk_deposit returns, so the caller may free them at once, as
+ *    read_fieldize does.  Device buffers are read in stream order on the
+ *    context's stream and must stay valid until genpk_sync or the next
+ *    genpk_power on that context.
+ *  - Output arrays of genpk_power* and genpk_adjoint are host memory unless a
+ *    function says otherwise.  Results are complete when the call returns.
+ *  - One context per host thread; a context is not thread-safe.
+ */
+#ifndef GENPK_GB300_H
+#define GENPK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct genpk_ctx genpk_ctx;
+
+typedef enum genpk_status {
+    GENPK_OK = 0,
+    GENPK_ERR_INVALID = 1,     /* bad argument (null pointer, field index, dims ...) */
+    GENPK_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    GENPK_ERR_CUFFT = 3,       /* a cuFFT call failed */
+    GENPK_ERR_NOMEM = 4,       /* device or pinned-host allocation failed */
+    GENPK_ERR_BAD_INPUT = 5,   /* non-finite or out-of-range particle data seen on the GPU */
+    GENPK_ERR_STATE = 6,       /* call not valid in the field's current state */
+    GENPK_ERR_UNSUPPORTED = 7, /* size or option this build does not handle */
+    GENPK_ERR_TIMEOUT = 8      /* a bounded device-side wait gave up */
+} genpk_status;
+
+/* genpk_ctx_create flags */
+#define GENPK_FLAG_TIMING 0x1u       /* record per-stage CUDA-event times */
+#define GENPK_FLAG_DETERMINISTIC 0x2u /* reserved: all reductions are already ordered */
+
+/* Create a context for dims^3 grids, nrbins log-k bins and nfields grids.
+ * Builds the bin tables (the reference's bin expression, powerspectrum.c:38,66)
+ * and cuFFT plans, and allocates the grids.  dims >= 2, 1 <= nrbins,
+ * 1 <= nfields <= GENPK_MAX_FIELDS. */
+#define GENPK_MAX_FIELDS 8
+int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genpk_ctx **out);
+
+/* Free every device resource of ctx.  Accepts NULL. */
+void genpk_ctx_destroy(genpk_ctx *ctx);
+
+/* Message for the last error on ctx (never NULL; "" after success). */
+const char *genpk_last_error(const genpk_ctx *ctx);
+
+/* Text for a status code. */
+const char *genpk_status_string(int status);
+
+/* Empty a grid: replaces memset(field,0,...) (gen-pk.cpp:208).  Lazy: the next
+ * deposit writes the grid instead of adding to it. */
+int genpk_zero(genpk_ctx *ctx, int field);
+
+/* CIC-deposit n particles into grid `field` with += semantics, as
+ * fieldize(boxsize, dims, field, n, pos, masses, mass, 1) does
+ * (fieldize.cpp:46-113): pos is float[n][3] in box units, masses float[n] or
+ * NULL for a uniform `mass`.  Periodic wrap.  May be called many times per
+ * field (reader chunks, several files, stars added to gas).  Host-pointer
+ * deposits are staged on the GPU and deposited in as few passes as staging
+ * memory allows; the deposited density is mean-subtracted on the GPU (only the
+ * excluded k=0 mode changes). */
+int genpk_deposit(genpk_ctx *ctx, int field, double boxsize, const float *pos,
+                  const float *masses, double mass, int64_t n);
+
+/* fftw_execute + powerspectrum for one pair of grids (A == B: auto spectrum).
+ * Runs the r2c FFT of each grid still in density form (in place), then the
+ * fused deconvolution + log-k binning.  power[nrbins], count[nrbins],
+ * keffs[nrbins] have the meaning and normalisation of powerspectrum.c:35-111:
+ * power /= mass_a*mass_b*count, keffs /= count, zero where count == 0. */
+int genpk_power(genpk_ctx *ctx, int field_a, int field_b, double mass_a, double mass_b,
+                double *power, int *count, double *keffs);
+
+/* Several spectra in one pass over the modes.  fields[nf] are FFT'd in one
+ * batched plan where they are still densities; pairs[2*np] index into the
+ * context's grids; pair_mass[2*np] are the two normalisation masses of each
+ * pair.  power is [np][nrbins]; count and keffs are [nrbins] (shared by all
+ * pairs, they depend only on the grid).  Replaces the per-type loop of
+ * gen-pk.cpp:204-239 and the cross-spectrum branches :240-356. */
+int genpk_power_multi(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
+                      double *power, int *count, double *keffs);
+
+/* The reference's inverse CIC window, fieldize.cpp:125-133 (host function). */
+double genpk_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
+
+/* Host-only: the weighted mode count and mean |k| of every bin for a dims^3
+ * grid and nrbins bins -- the count[] and keffs[] powerspectrum() returns
+ * (powerspectrum.c:55-108), which depend only on the grid.  Needs no GPU. */
+int genpk_geometry(int64_t dims, int nrbins, int *count, double *keffs);
+
+/* Load a caller-computed half-complex spectrum (dims*dims*(dims/2+1) complex
+ * values as interleaved float64 re, im -- FFTW's in-place r2c output,
+ * gen-pk.cpp:185) into grid `field`, so genpk_power bins it without an FFT.
+ * This is the path behind the reference-signature powerspectrum() drop-in. */
+int genpk_load_spectrum(genpk_ctx *ctx, int field, const double *spectrum);
+
+/* Bin index the library assigns to integer |k|^2 = kk2 on ctx's grid; the
+ * reference's floor(binsperunit*log(sqrt(kk2))) (powerspectrum.c:38,66). */
+int genpk_bin_of(const genpk_ctx *ctx, int64_t kk2);
+
+/* Wait for all work on ctx and report device-side input errors. */
+int genpk_sync(genpk_ctx *ctx);
+
+/* Copy grid `field` (density form) to host as float64 padded grid
+ * (dims*dims*2*(dims/2+1)), the same array fieldize() would have produced.
+ * Intended for tests; flushes pending deposits. */
+int genpk_read_field(genpk_ctx *ctx, int field, double *out);
+
+/* Gradient of a P(k) loss with respect to particle positions and masses
+ * (no reference counterpart).  For the auto spectrum of grid `field` built from
+ * the n particles (pos, masses|NULL, mass) with normalisation mass_norm:
+ * given dl_dp[nrbins] = dL/dP_b, writes grad_pos[n][3] = dL/dpos and, when
+ * masses != NULL, grad_mass[n] = dL/dm (including the dependence of mass_norm
+ * on the masses, d mass_norm / d m_p = 1).  *dl_dmass_norm receives dL/dM.
+ * If the grid still holds this species' spectrum (after genpk_power) it is
+ * reused; otherwise, or with recompute != 0, the density is re-deposited and
+ * transformed again.  pos/masses/grad_* may be host or device pointers (all
+ * of one kind). */
+int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos,
+                  const float *masses, double mass, int64_t n, double mass_norm,
+                  const double *dl_dp, float *grad_pos, float *grad_mass,
+                  double *dl_dmass_norm, int recompute);
+
+/* Per-kernel / per-stage device times (milliseconds, CUDA events on the
+ * context's stream) of all work issued since the last genpk_timing_reset, when
+ * the context was created with GENPK_FLAG_TIMING.  names[i] point at static
+ * strings (e.g. "dep_tile", "fft", "bin").  Waits for that work.  Returns the
+ * number of intervals written (<= cap). */
+int genpk_stage_times(const genpk_ctx *ctx, const char **names, float *ms, int cap);
+
+/* Start a new timing window (see genpk_stage_times). */
+int genpk_timing_reset(genpk_ctx *ctx);
+
+/* Deposit tuning actually in use (tile edge lengths and sort CTA count). */
+int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
+                         int *sort_ctas);
+
+/* Choose the deposit tile (cells per edge; supported: 8^3, 16^3, 16x32x32,
+ * 32^3).  Results do not depend on it beyond FP32 summation order. */
+int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z);
+
+/* Number of kernels the library launched on ctx since creation. */
+int64_t genpk_kernel_launches(const genpk_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GENPK_GB300_H */

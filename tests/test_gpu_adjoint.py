@@ -1,0 +1,190 @@
+"""GPU adjoint (gradient of a P(k) loss w.r.t. positions and masses) against the
+FP64 reference gradient (oracle.reference_gradient) and central finite
+differences of the FP64 oracle forward.
+
+Tolerances: gradients within 1e-4 relative of the FP64 reference gradient,
+norm-wise, and per element within 1e-4 of the largest element.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+G_RTOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def gp(native_lib):
+    import torch
+    assert torch.cuda.is_available()
+    import genpk_gb300
+    return genpk_gb300
+
+
+def loss_grad(p, target, count):
+    ok = count > 0
+    d = np.where(ok, (p - target) / target, 0.0)
+    return float(np.sum(d * d)), np.where(ok, 2.0 * (p - target) / target ** 2, 0.0)
+
+
+def grad_close(g, ref, rtol=G_RTOL):
+    g = np.asarray(g, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    norm = np.linalg.norm(g - ref) / np.linalg.norm(ref)
+    elem = np.abs(g - ref).max() / np.abs(ref).max()
+    assert norm <= rtol and elem <= rtol, (norm, elem)
+    return norm
+
+
+def make_case(kind, dims, box, seed, nrbins, var):
+    from genpk_gb300 import synth
+    if kind == "uniform":
+        pos = synth.uniform(dims ** 3, box, seed=seed)
+    else:
+        pos = synth.zeldovich(dims, box, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    masses = (rng.random(len(pos)) + 0.5).astype(np.float32) if var else None
+    return pos, masses
+
+
+@pytest.mark.parametrize("kind,dims,var", [("uniform", 32, False), ("zeldovich", 32, True),
+                                           ("zeldovich", 64, False), ("uniform", 48, True)])
+def test_adjoint_matches_fp64_reference_gradient(gp, kind, dims, var):
+    box, nrbins, mass = 1000.0, 24, 1.0
+    pos, masses = make_case(kind, dims, box, 3, nrbins, var)
+    tgt_pos, _ = make_case(kind, dims, box, 4, nrbins, False)
+    m = O.total_mass(len(pos), masses, 0.0 if var else mass)
+    target, cnt, _ = O.pk(tgt_pos, box, dims, nrbins, None, 1.0)
+    target = np.where(cnt > 0, target, 1.0)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses, mass)
+        p, c, _ = ctx.power(0, 0, m, m)
+        _, g = loss_grad(p, target, c)
+        gpos, gmass, dldm = ctx.adjoint(0, box, pos, g, m, masses=masses, mass=mass)
+    rpos, rmass, rdldm = O.reference_gradient(pos, box, dims, nrbins, g, masses, mass, m_norm=m)
+    grad_close(gpos, rpos)
+    if var:
+        grad_close(gmass, rmass)
+    assert abs(dldm - rdldm) <= 1e-6 * abs(rdldm) + 1e-300
+
+
+def test_adjoint_recompute_equals_stored_spectrum(gp):
+    dims, box, nrbins = 32, 100.0, 16
+    pos, masses = make_case("zeldovich", dims, box, 9, nrbins, True)
+    m = O.total_mass(len(pos), masses)
+    g = np.linspace(-1.0, 1.0, nrbins) * 1e3
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        ctx.power(0, 0, m, m)
+        a = ctx.adjoint(0, box, pos, g, m, masses=masses)
+        b = ctx.adjoint(0, box, pos, g, m, masses=masses, recompute=True)
+        ctx.zero(0)
+        c = ctx.adjoint(0, box, pos, g, m, masses=masses)  # nothing stored: recomputes
+    for x, y in ((a, b), (a, c)):
+        np.testing.assert_allclose(x[0], y[0], rtol=1e-5, atol=1e-6 * np.abs(a[0]).max())
+        np.testing.assert_allclose(x[1], y[1], rtol=1e-5, atol=1e-6 * np.abs(a[1]).max())
+
+
+def test_adjoint_device_pointers(gp):
+    import torch
+    dims, box, nrbins = 32, 100.0, 16
+    pos, masses = make_case("uniform", dims, box, 5, nrbins, True)
+    m = O.total_mass(len(pos), masses)
+    g = np.ones(nrbins)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        ctx.power(0, 0, m, m)
+        h = ctx.adjoint(0, box, pos, g, m, masses=masses, recompute=True)
+        d = ctx.adjoint(0, box, torch.from_numpy(pos).cuda(), g, m,
+                        masses=torch.from_numpy(masses).cuda(), recompute=True)
+    np.testing.assert_allclose(d[0].cpu().numpy(), h[0], rtol=1e-6, atol=1e-7 * np.abs(h[0]).max())
+    np.testing.assert_allclose(d[1].cpu().numpy(), h[1], rtol=1e-6, atol=1e-7 * np.abs(h[1]).max())
+
+
+def test_adjoint_central_finite_differences_256_particles(gp):
+    """Central differences (step 1e-3 cell) of the FP64 oracle loss on 256
+    random particles against the GPU gradient."""
+    dims, box, nrbins = 32, 3200.0, 16
+    pos, masses = make_case("zeldovich", dims, box, 11, nrbins, True)
+    tgt, _ = make_case("zeldovich", dims, box, 12, nrbins, False)
+    target, cnt, _ = O.pk(tgt, box, dims, nrbins, None, 1.0)
+    target = np.where(cnt > 0, target, 1.0)
+
+    def oracle_loss(p64, m32):
+        mm = O.total_mass(len(p64), m32)
+        pw, c, _ = O.pk(p64.astype(np.float32), box, dims, nrbins, m32, 0.0, m_norm=mm)
+        return loss_grad(pw, target, c)[0]
+
+    m = O.total_mass(len(pos), masses)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        p, c, _ = ctx.power(0, 0, m, m)
+        _, g = loss_grad(p, target, c)
+        gpos, gmass, _ = ctx.adjoint(0, box, pos, g, m, masses=masses)
+    rng = np.random.default_rng(0)
+    idx = rng.choice(len(pos), 256, replace=False)
+    axes = rng.integers(0, 3, 256)
+    h = 1e-3 * box / dims
+    p64 = pos.astype(np.float64)
+    fd = np.empty(256)
+    for q, (i, a) in enumerate(zip(idx, axes)):
+        pp, pm = p64.copy(), p64.copy()
+        pp[i, a] += h
+        pm[i, a] -= h
+        fd[q] = (oracle_loss(pp, masses) - oracle_loss(pm, masses)) / (2 * h)
+    got = gpos[idx, axes].astype(np.float64)
+    scale = np.abs(fd).max()
+    err = np.abs(got - fd)
+    # CIC is piecewise linear: a step that crosses a cell face has an O(h) kink
+    # error, so allow a handful of outliers and bound the rest tightly.
+    assert np.mean(err <= 2e-3 * scale) >= 0.97, np.sort(err / scale)[-10:]
+    assert np.linalg.norm(got - fd) / np.linalg.norm(fd) <= 2e-2
+
+
+def test_autograd_binding(gp):
+    import torch
+    from genpk_gb300 import autograd as ag
+    dims, box, nrbins = 32, 100.0, 16
+    pos, masses = make_case("zeldovich", dims, box, 21, nrbins, True)
+    tgt, _ = make_case("zeldovich", dims, box, 22, nrbins, False)
+    target, cnt, _ = O.pk(tgt, box, dims, nrbins, None, 1.0)
+    target = np.where(cnt > 0, target, 1.0)
+    tp = torch.from_numpy(pos).cuda().requires_grad_(True)
+    tm = torch.from_numpy(masses).cuda().requires_grad_(True)
+    with gp.Context(dims, nrbins) as ctx:
+        p = ag.power_spectrum(tp, tm, ctx, box)
+        loss = ag.relative_loss(p, target, cnt)
+        loss.backward()
+    m = O.total_mass(len(pos), masses)
+    _, g = loss_grad(p.detach().cpu().numpy(), target, cnt)
+    rpos, rmass, _ = O.reference_gradient(pos, box, dims, nrbins, g, masses, 0.0, m_norm=m)
+    grad_close(tp.grad.cpu().numpy(), rpos)
+    grad_close(tm.grad.cpu().numpy(), rmass)
+
+
+def test_adjoint_differentiable_pk_256(gp):
+    """256^3 Zel'dovich particles on a 256^3 grid (L = 50000 kpc/h), 64 bins,
+    loss against the spectrum of a second seed: GPU gradient vs the FP64
+    reference gradient."""
+    from genpk_gb300 import synth
+    dims, box, nrbins = 256, 50000.0, 64
+    pos = synth.zeldovich(dims, box, seed=1)
+    tgt = synth.zeldovich(dims, box, seed=2)
+    rng = np.random.default_rng(7)
+    masses = (1.0 + 0.1 * rng.standard_normal(len(pos))).astype(np.float32)
+    m = O.total_mass(len(pos), masses)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, tgt, None, 1.0)
+        target, cnt, _ = ctx.power(0, 0, O.total_mass(len(tgt), None, 1.0),
+                                   O.total_mass(len(tgt), None, 1.0))
+        target = np.where(cnt > 0, target, 1.0)
+        ctx.zero(0)
+        ctx.deposit(0, box, pos, masses)
+        p, c, _ = ctx.power(0, 0, m, m)
+        _, g = loss_grad(p, target, c)
+        gpos, gmass, _ = ctx.adjoint(0, box, pos, g, m, masses=masses)
+    rpos, rmass, _ = O.reference_gradient(pos, box, dims, nrbins, g, masses, 0.0, m_norm=m)
+    grad_close(gpos, rpos)
+    grad_close(gmass, rmass)

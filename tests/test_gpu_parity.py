@@ -1,0 +1,344 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle and the
+reference's golden fixtures.
+
+Tolerances:
+  * mode counts: bit-exact; keffs: 1e-12 relative (pure geometry, FP64).
+  * P(k): every bin within 1e-5 relative of the FP64 oracle (the stated bar
+    for the FP32 deposit + FP32 FFT path).
+  * deposited grid: |gpu - oracle| <= 2e-6 * max|oracle| per cell (FP32 CIC
+    weights and FP32 accumulation against FP64).
+"""
+import numpy as np
+import pytest
+
+from conftest import cases
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+P_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def gp(native_lib):
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    import genpk_gb300
+    return genpk_gb300
+
+
+def grid_close(gpu, ref, tol=2e-6):
+    scale = max(np.abs(ref).max(), 1e-30)
+    err = np.abs(gpu - ref).max() / scale
+    assert err <= tol, f"grid max rel err {err:.3e}"
+
+
+def bins_close(p_gpu, p_ref, cnt, rtol=P_RTOL):
+    ok = cnt > 0
+    rel = np.abs(p_gpu[ok] - p_ref[ok]) / np.maximum(np.abs(p_ref[ok]), 1e-300)
+    assert rel.max() <= rtol, f"max per-bin rel err {rel.max():.3e} at bin {np.argmax(rel)}"
+    assert np.all(p_gpu[~ok] == 0)
+    return rel.max()
+
+
+# ---------------------------------------------------------------------------
+# The reference's own known answers (test.cpp) through reference-named calls
+# ---------------------------------------------------------------------------
+
+def test_check_fieldize_known_answer(gp):
+    """test.cpp:31-50 through the fieldize() drop-in."""
+    dims = 5
+    field = np.zeros(2 * dims * dims * (dims // 2 + 1))
+    pos = (np.arange(30) / 3.0).astype(np.float32)
+    masses = np.full(30, 10.0, dtype=np.float32)
+    assert gp.fieldize(10, dims, field, pos, masses[:10], 10.0, 1) == 0
+    assert abs(field[0] - 8.61111) <= 8.61111e-5
+    assert field[3] == 0 and field[20] == 0 and field[125] == 0
+    assert abs(field[124] - 1.66666) <= 1.66666e-5
+
+
+def test_check_powerspectrum_known_answer(gp):
+    """test.cpp:59-86 through the powerspectrum() drop-in (FFT by the caller)."""
+    field = np.zeros(2 * 4 * 4 * 3)
+    for i in range(32):
+        field[6 * (i // 4) + i % 4] = 1
+    field[0] = 2
+    f = O.rfft_padded(field.reshape(4, 4, 6))
+    p, c, k = gp.powerspectrum(4, f, f, 10, 64.0, 64.0)
+    assert abs(k[2] - np.sqrt(2)) <= np.sqrt(2) * 1e-5
+    assert (c[0], c[1], c[2]) == (6, 0, 12)
+    assert abs(p[0] - 0.0677526) <= 0.0677526e-5
+    assert p[1] == 0
+    assert abs(p[2] - 0.000565561) <= 0.000565561e-5
+    assert abs(p[9] - 0.0550908) <= 0.0550908e-5
+
+
+def test_check_powerspectrum_known_answer_gpu_fft(gp):
+    """Same field, FFT on the GPU: load it as a density and bin."""
+    field = np.zeros((4, 4, 6))
+    flat = field.reshape(-1)
+    for i in range(32):
+        flat[6 * (i // 4) + i % 4] = 1
+    flat[0] = 2
+    f = O.rfft_padded(field)
+    with gp.Context(4, 10) as ctx:
+        ctx.load_spectrum(0, f)
+        p, c, k = ctx.power(0, 0, 64.0, 64.0)
+    assert (c[0], c[1], c[2]) == (6, 0, 12)
+    assert abs(p[9] - 0.0550908) <= 0.0550908e-5
+
+
+# ---------------------------------------------------------------------------
+# Golden fixtures from the reference build
+# ---------------------------------------------------------------------------
+
+def test_deposit_matches_reference_golden_grids(gp, golden):
+    for name, c in cases(golden["fieldize"]).items():
+        dims, box, n, extra, mass = c["meta"]
+        dims, extra = int(dims), int(extra)
+        pos, masses = c["pos"], c.get("masses")
+        if extra == 1:
+            with gp.Context(dims, 1) as ctx:
+                ctx.deposit(0, box, pos, masses, mass)
+                g = ctx.read_field(0).reshape(-1)
+        else:
+            g = np.zeros_like(c["grid"])
+            gp.fieldize(box, dims, g, pos, masses, mass, extra)
+        grid_close(g, c["grid"])
+
+
+def test_power_matches_reference_golden(gp, golden):
+    for name, c in cases(golden["power"]).items():
+        dims, box, n, mass, nrbins, m = c["meta"]
+        dims, nrbins = int(dims), int(nrbins)
+        with gp.Context(dims, nrbins) as ctx:
+            ctx.deposit(0, box, c["pos"], c.get("masses"), mass)
+            p, cnt, k = ctx.power(0, 0, m, m)
+        assert np.array_equal(cnt, c["count"]), name
+        np.testing.assert_allclose(k, c["keffs"], rtol=1e-12, err_msg=name)
+        bins_close(p, c["power"], cnt)
+
+
+# ---------------------------------------------------------------------------
+# Oracle comparisons at larger sizes
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("kind,dims,nrbins", [("uniform", 64, 64), ("uniform", 128, 64),
+                                              ("zeldovich", 64, 64), ("zeldovich", 128, 128)])
+def test_power_matches_oracle(gp, kind, dims, nrbins):
+    from genpk_gb300 import synth
+    box = 25000.0
+    if kind == "uniform":
+        pos = synth.uniform(dims ** 3, box, seed=dims)
+    else:
+        pos = synth.zeldovich(dims, box, seed=dims)
+    mass = 1.0e-2
+    m = O.total_mass(len(pos), None, mass)
+    pr, cr, kr = O.pk(pos, box, dims, nrbins, None, mass, m_norm=m)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, None, mass)
+        p, c, k = ctx.power(0, 0, m, m)
+    assert np.array_equal(c, cr)
+    assert c.astype(np.int64).sum() == dims ** 3 - 1
+    np.testing.assert_allclose(k, kr, rtol=1e-12)
+    bins_close(p, pr, c)
+
+
+def test_variable_masses_lognormal(gp):
+    from genpk_gb300 import synth
+    dims, box, nrbins = 64, 1000.0, 32
+    pos, masses = synth.lognormal(150000, box, 64, sigma=1.5, seed=4, mass_mu=-5, mass_sigma=0.8)
+    m = O.total_mass(len(pos), masses)
+    pr, cr, _ = O.pk(pos, box, dims, nrbins, masses, 0.0, m_norm=m)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        g = ctx.read_field(0)
+        p, c, _ = ctx.power(0, 0, m, m)
+    grid_close(g, O.deposit(pos, box, dims, masses, 0.0))
+    bins_close(p, pr, c)
+
+
+@pytest.mark.parametrize("dims", [2, 3, 5, 7, 9, 17, 33, 48])
+def test_small_and_odd_grids(gp, dims):
+    rng = np.random.default_rng(dims)
+    box = 7.0
+    pos = (rng.random((3000, 3)) * 9.0 - 1.0).astype(np.float32)  # wraps both ways
+    masses = (rng.random(3000) + 0.1).astype(np.float32)
+    nrbins = max(3, dims)
+    m = O.total_mass(len(pos), masses)
+    ref_grid = O.deposit(pos, box, dims, masses, 0.0)
+    pr, cr, kr = O.pk(pos, box, dims, nrbins, masses, 0.0, m_norm=m)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        grid_close(ctx.read_field(0), ref_grid)
+        p, c, k = ctx.power(0, 0, m, m)
+    assert np.array_equal(c, cr)
+    bins_close(p, pr, c, rtol=2e-5)
+
+
+@pytest.mark.parametrize("tile", [(8, 8, 8), (16, 16, 16), (16, 32, 32), (32, 32, 32)])
+def test_tile_shapes_agree(gp, tile):
+    from genpk_gb300 import synth
+    dims, box = 96, 1000.0
+    pos = synth.uniform(200000, box, seed=7)
+    ref = O.deposit(pos, box, dims, None, 1.0)
+    with gp.Context(dims, 16) as ctx:
+        ctx.set_tile(*tile)
+        ctx.deposit(0, box, pos, None, 1.0)
+        grid_close(ctx.read_field(0), ref)
+
+
+# ---------------------------------------------------------------------------
+# Accumulation semantics, pointer kinds, cross spectra
+# ---------------------------------------------------------------------------
+
+def test_chunked_host_and_device_deposits_accumulate(gp):
+    import torch
+    from genpk_gb300 import synth
+    dims, box = 64, 500.0
+    pos = synth.uniform(300000, box, seed=9)
+    masses = np.linspace(0.5, 1.5, len(pos)).astype(np.float32)
+    ref = O.deposit(pos, box, dims, masses, 0.0)
+    with gp.Context(dims, 8) as ctx:
+        # host chunks like read_fieldize's <= 2^26 loop (read_fieldize.cpp:45-93)
+        for a in range(0, len(pos), 70000):
+            ctx.deposit(0, box, pos[a:a + 70000], masses[a:a + 70000])
+        grid_close(ctx.read_field(0), ref)
+        ctx.zero(0)
+        dpos = torch.from_numpy(pos).cuda()
+        dm = torch.from_numpy(masses).cuda()
+        ctx.deposit(0, box, dpos[:100000], dm[:100000])
+        ctx.deposit(0, box, pos[100000:200000], masses[100000:200000])  # host
+        ctx.deposit(0, box, dpos[200000:], masses[200000:])             # mixed kinds
+        grid_close(ctx.read_field(0), ref)
+
+
+def test_uniform_and_variable_mass_chunks_into_one_grid(gp):
+    """Gas + stars into one grid (gen-pk.cpp:215-230 with -s 1)."""
+    from genpk_gb300 import synth
+    dims, box = 32, 100.0
+    gas = synth.uniform(20000, box, seed=1)
+    stars = synth.uniform(3000, box, seed=2)
+    sm = np.full(3000, 0.37, dtype=np.float32)
+    ref = O.deposit(gas, box, dims, None, 0.19)
+    O.port().fieldize(box, dims, ref, stars, sm, 0.0, 1)
+    with gp.Context(dims, 8) as ctx:
+        ctx.deposit(0, box, gas, None, 0.19)
+        ctx.deposit(0, box, stars, sm)
+        grid_close(ctx.read_field(0), ref)
+
+
+def test_cross_and_multi_spectra(gp):
+    from genpk_gb300 import synth
+    dims, box, nrbins = 64, 1000.0, 24
+    a = synth.zeldovich(64, box, seed=1)
+    b = synth.zeldovich(64, box, seed=1, amplitude=0.7)
+    c = synth.uniform(100000, box, seed=3)
+    cm = np.linspace(0.1, 2.0, len(c)).astype(np.float32)
+    ma, mb, mc = O.total_mass(len(a), None, 1.0), O.total_mass(len(b), None, 0.19), O.total_mass(len(c), cm)
+    fa = O.rfft_padded(O.deposit(a, box, dims, None, 1.0))
+    fb = O.rfft_padded(O.deposit(b, box, dims, None, 0.19))
+    fc = O.rfft_padded(O.deposit(c, box, dims, cm, 0.0))
+    port = O.port()
+    refs = {(0, 0): port.powerspectrum(dims, fa, fa, nrbins, ma, ma),
+            (1, 1): port.powerspectrum(dims, fb, fb, nrbins, mb, mb),
+            (2, 2): port.powerspectrum(dims, fc, fc, nrbins, mc, mc),
+            (0, 1): port.powerspectrum(dims, fa, fb, nrbins, ma, mb),
+            (0, 2): port.powerspectrum(dims, fa, fc, nrbins, ma, mc),
+            (1, 2): port.powerspectrum(dims, fb, fc, nrbins, mb, mc)}
+    mass = {0: ma, 1: mb, 2: mc}
+    with gp.Context(dims, nrbins, nfields=3) as ctx:
+        ctx.deposit(0, box, a, None, 1.0)
+        ctx.deposit(1, box, b, None, 0.19)
+        ctx.deposit(2, box, c, cm)
+        pairs = list(refs)
+        p, cnt, _ = ctx.power_multi(pairs, [(mass[i], mass[j]) for i, j in pairs])
+        for q, pr in enumerate(pairs):
+            ok = cnt > 0
+            ref = refs[pr][0]
+            auto = pr[0] == pr[1]
+            rel = np.abs(p[q][ok] - ref[ok]) / np.abs(ref[ok]).max()
+            # cross spectra can cross zero: compare relative to the bin scale
+            assert rel.max() <= (P_RTOL if auto else 1e-5), (pr, rel.max())
+        # a single cross call after the FFTs are done re-bins without new FFTs
+        p01, _, _ = ctx.power(0, 1, ma, mb)
+        np.testing.assert_allclose(p01, p[pairs.index((0, 1))], rtol=1e-12)
+
+
+def test_compat_bound_fields_route_to_device(gp):
+    """The fieldize/powerspectrum drop-ins on a bound host field."""
+    from genpk_gb300 import native, synth
+    compat = native.load_compat()
+    dims, box, nrbins = 32, 100.0, 16
+    pos = synth.uniform(30000, box, seed=5)
+    host_field = np.zeros(2 * dims * dims * (dims // 2 + 1))
+    with gp.Context(dims, nrbins) as ctx:
+        assert compat.genpk_compat_bind(ctx.h, 0, host_field.ctypes.data) == 0
+        for a in range(0, len(pos), 10000):
+            chunk = np.ascontiguousarray(pos[a:a + 10000])
+            rc = compat.fieldize(box, dims, host_field.ctypes.data_as(native.c_f64p), len(chunk),
+                                 chunk.ctypes.data_as(native.c_f32p), None, 1.0, 1)
+            assert rc == 0
+        assert not host_field.any()  # host array untouched: the grid lives on the GPU
+        m = O.total_mass(len(pos), None, 1.0)
+        p = np.zeros(nrbins)
+        c = np.zeros(nrbins, dtype=np.int32)
+        k = np.zeros(nrbins)
+        fp = host_field.ctypes.data_as(native.c_f64p)
+        rc = compat.powerspectrum(dims, fp, fp, nrbins, p.ctypes.data_as(native.c_f64p),
+                                  c.ctypes.data_as(native.c_i32p), k.ctypes.data_as(native.c_f64p),
+                                  m, m)
+        assert rc == 0
+        assert compat.genpk_compat_unbind(host_field.ctypes.data) == 0
+    pr, cr, _ = O.pk(pos, box, dims, nrbins, None, 1.0, m_norm=m)
+    assert np.array_equal(c, cr)
+    bins_close(p, pr, c)
+
+
+# ---------------------------------------------------------------------------
+# Errors are statuses, never aborts
+# ---------------------------------------------------------------------------
+
+def test_non_finite_particles_are_reported_and_skipped(gp):
+    dims, box = 16, 10.0
+    rng = np.random.default_rng(1)
+    pos = (rng.random((1000, 3)) * box).astype(np.float32)
+    bad = pos.copy()
+    bad[10, 1] = np.nan
+    bad[20, 0] = np.inf
+    with gp.Context(dims, 4) as ctx:
+        ctx.deposit(0, box, bad, None, 1.0)
+        with pytest.raises(gp.GenPKError) as e:
+            ctx.read_field(0)
+        assert e.value.status == 5
+        ctx.zero(0)
+        ctx.deposit(0, box, bad, None, 1.0)
+        with pytest.raises(gp.GenPKError):
+            ctx.sync()
+        g = ctx.read_field(0)  # status was cleared; skipped particles are absent
+    keep = np.ones(1000, bool)
+    keep[[10, 20]] = False
+    grid_close(g, O.deposit(pos[keep], box, dims, None, 1.0))
+
+
+def test_state_and_argument_errors(gp):
+    with gp.Context(8, 4, nfields=2) as ctx:
+        pos = np.zeros((10, 3), np.float32)
+        with pytest.raises(gp.GenPKError) as e:
+            ctx.deposit(5, 1.0, pos)
+        assert e.value.status == 1
+        with pytest.raises(gp.GenPKError):
+            ctx.deposit(0, -1.0, pos)
+        ctx.deposit(0, 1.0, pos, None, 1.0)
+        ctx.power(0, 0, 11.0, 11.0)
+        with pytest.raises(gp.GenPKError) as e:
+            ctx.deposit(0, 1.0, pos, None, 1.0)  # grid holds a spectrum now
+        assert e.value.status == 6
+        with pytest.raises(gp.GenPKError):
+            ctx.read_field(0)
+        ctx.zero(0)
+        ctx.deposit(0, 1.0, pos, None, 1.0)
+        p, c, _ = ctx.power(1, 1, 1.0, 1.0)  # never-deposited grid: all zero
+        assert not p.any()
+        with pytest.raises(gp.GenPKError):
+            ctx.set_tile(7, 7, 7)
