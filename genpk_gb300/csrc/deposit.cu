@@ -1,33 +1,40 @@
 // deposit.cu -- CIC mass assignment (the GPU counterpart of fieldize.cpp:46-113).
 //
-// One deposit pass over n particles runs five kernels on one stream:
+// A deposit pass over n particles is a counting sort into cell tiles followed
+// by one CTA per tile accumulating in shared memory:
 //
-//   K1 k_sort_hist      each CTA owns a contiguous particle range; it computes
-//                       every particle's cell (two-product split, see
-//                       split_cell), counts particles per tile in a shared
-//                       histogram and writes that histogram row to scratch.
-//                       It also sums variable masses (Kahan, FP32 -> FP64).
-//   K2 k_sort_colsum    per tile: total over the CTA rows.
-//   K3 k_sort_scan      one CTA: exclusive scan of the tile totals -> tile_start,
-//                       and the pass mass (FP64) for the mean subtraction.
-//   K4 k_sort_offsets   per tile: turns the histogram rows into each CTA's first
-//                       slot in that tile (a column scan).
-//   K5 k_sort_scatter   re-reads the range and writes each particle, packed as
-//                       tile-local cell + 24-bit fraction per axis (+ mass), to
-//                       its slot: a counting sort into tile order.
-//   K6 k_tile_deposit   one CTA per tile: accumulates its particles' eight CIC
-//                       weights in a (T+1)^3 shared-memory block, stores the
-//                       T^3 interior to the grid minus the pass mean (coalesced
-//                       rows; a plain store when the grid is freshly zeroed,
-//                       read-modify-write otherwise) and the +1 halo faces to
-//                       scratch.
-//   K7 k_halo_merge     adds every tile's halo faces to the neighbouring cells.
+//   k_sort_hist       each CTA owns a contiguous particle range; it computes
+//                     every particle's cell (two-product split, split_cell),
+//                     counts particles per tile in a shared histogram and
+//                     writes the histogram row to scratch; it also sums the
+//                     masses (Kahan, FP32 -> FP64) and takes their maximum.
+//   k_sort_colsum     per tile: total over the CTA rows.
+//   k_sort_scan       one CTA: exclusive scan of the tile totals -> tile_start;
+//                     the pass mass, the fixed-point scale 2^s and the pass
+//                     mean in fixed point.
+//   k_sort_offsets    per tile: histogram rows -> each CTA's first slot.
+//   k_sort_scatter    re-reads the range and writes every particle, packed as
+//                     tile-local cell + 24-bit fraction per axis (+ mass bits),
+//                     to its slot.
+//   (grids with more tiles than a shared histogram holds run both kernels with
+//    global counters instead.)
+//   k_tile_deposit    one CTA per tile: each particle adds its eight CIC
+//                     weights, rounded to integers of 2^-s mass units, to a
+//                     (T+1)^3 block of 64-bit shared accumulators.  Integer
+//                     sums are exact and independent of order, so the deposit
+//                     is bit-reproducible.  Cells strictly inside the tile are
+//                     final: (sum - mean) is converted to FP32 once and stored.
+//                     The tile's low faces and its +1 halo layer go to scratch
+//                     as 64-bit sums.
+//   k_face_gather     per tile: every low-face cell adds the halo sums the
+//                     (up to 7) lower neighbours hold for it, in a fixed order,
+//                     and stores (sum - mean) as FP32.
 //
-// Every grid cell is written by exactly one CTA in K6 and receives halo sums
-// in K7, so no grid memset is needed before the first pass and no global
-// atomics touch the interior.  Mean subtraction keeps the FP32 r2c accurate:
-// each pass removes its own mass / N^3 from every real cell, which changes only
-// the (excluded) k = 0 mode.
+// No global float atomics are involved and no grid memset is needed: every real
+// cell is written exactly once per pass.  Subtracting the pass mean (in fixed
+// point, before the single rounding) keeps the FP32 r2c accurate; it changes
+// only the excluded k = 0 mode.  The mean is rounded to 24 significant bits so
+// that an empty cell holds exactly -mean in FP32 and reads back as exactly 0.
 #include "common.cuh"
 #include "internal.h"
 
@@ -63,12 +70,13 @@ struct SortParams {
 
 constexpr int kSortThreads = 512;
 constexpr int kSortUnroll = 4;
+constexpr uint32_t kNoTile = 0xffffffffu;
 
 // Cell and tile of one particle; false for a particle that must be skipped.
 __device__ __forceinline__ bool particle_cell(const SortParams &p, float x, float y, float z,
-                                              int c[3], float d[3], uint32_t &tile)
+                                              float m, int c[3], float d[3], uint32_t &tile)
 {
-    if (!finite3(x, y, z))
+    if (!finite3(x, y, z) || !isfinite(m))
         return false;
     const float lim = 1.0e9f;
     if (fabsf(x * p.uh) > lim || fabsf(y * p.uh) > lim || fabsf(z * p.uh) > lim)
@@ -82,69 +90,112 @@ __device__ __forceinline__ bool particle_cell(const SortParams &p, float x, floa
     return true;
 }
 
-__global__ void __launch_bounds__(kSortThreads)
-    k_sort_hist(SortParams p, uint32_t *__restrict__ hist, double *__restrict__ mass_part,
-                DeviceStatus *st)
+// Per-CTA mass sum (FP64) and max |mass| (float bits) after the particle loop.
+__device__ __forceinline__ void block_mass(float msum, float mc, float mmax, double *mass_part,
+                                           DeviceStatus *st)
 {
-    extern __shared__ uint32_t sh_hist[];
-    __shared__ double sh_mass[kSortThreads / 32];
-    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
-        sh_hist[i] = 0u;
-    __syncthreads();
-
-    const int64_t b = (int64_t)blockIdx.x * p.chunk;
-    const int64_t e = min(p.n, b + p.chunk);
-    const float *__restrict__ pos = p.pos;
-    float msum = 0.f, mc = 0.f;
-    unsigned bad = 0;
-    for (int64_t i0 = b + threadIdx.x; i0 < e; i0 += (int64_t)kSortUnroll * blockDim.x) {
-        float v[kSortUnroll][3];
-        float m[kSortUnroll];
-#pragma unroll
-        for (int u = 0; u < kSortUnroll; u++) {
-            const int64_t i = i0 + (int64_t)u * blockDim.x;
-            if (i < e) {
-                v[u][0] = __ldg(pos + 3 * i);
-                v[u][1] = __ldg(pos + 3 * i + 1);
-                v[u][2] = __ldg(pos + 3 * i + 2);
-                m[u] = p.masses ? __ldg(p.masses + i) : 0.f;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kSortUnroll; u++) {
-            const int64_t i = i0 + (int64_t)u * blockDim.x;
-            if (i >= e)
-                break;
-            int c[3];
-            float d[3];
-            uint32_t t;
-            if (!particle_cell(p, v[u][0], v[u][1], v[u][2], c, d, t) || !isfinite(m[u])) {
-                bad++;
-                continue;
-            }
-            atomicAdd(&sh_hist[t], 1u);
-            // Kahan-compensated FP32 sum of this thread's masses.
-            const float y = m[u] - mc;
-            const float s = msum + y;
-            mc = (s - msum) - y;
-            msum = s;
-        }
-    }
-    __syncthreads();
-    uint32_t *row = hist + (size_t)blockIdx.x * p.ntiles;
-    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
-        row[i] = sh_hist[i];
-
+    __shared__ double sh_mass[32];
+    __shared__ float sh_max[32];
     double md = warp_sum_d((double)msum - (double)mc);
-    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+    if ((threadIdx.x & 31) == 0) {
         sh_mass[threadIdx.x >> 5] = md;
+        sh_max[threadIdx.x >> 5] = mmax;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+        float mx = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
             s += sh_mass[w];
+            mx = fmaxf(mx, sh_max[w]);
+        }
         mass_part[blockIdx.x] = s;
+        if (mx > 0.f)
+            atomicMax(&st->max_mass_bits, __float_as_uint(mx));
     }
+}
+
+// Each warp walks its CTA's range in blocks of 32*kSortUnroll consecutive
+// particles (lane l takes base + l + 32u, so every load is coalesced).  The trip
+// count is warp-uniform, so warp-collective intrinsics are safe in `f`.
+template <typename F>
+__device__ __forceinline__ void for_each_warp_batch(const SortParams &p, F &&f)
+{
+    const int64_t b = (int64_t)blockIdx.x * p.chunk;
+    const int64_t e = min(p.n, b + p.chunk);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int64_t base = b + (int64_t)warp * 32 * kSortUnroll; base < e;
+         base += (int64_t)nwarps * 32 * kSortUnroll) {
+        float v[kSortUnroll][3], m[kSortUnroll];
+        bool in[kSortUnroll];
+#pragma unroll
+        for (int u = 0; u < kSortUnroll; u++) {
+            const int64_t i = base + 32 * u + lane;
+            in[u] = i < e;
+            if (in[u]) {
+                v[u][0] = __ldg(p.pos + 3 * i);
+                v[u][1] = __ldg(p.pos + 3 * i + 1);
+                v[u][2] = __ldg(p.pos + 3 * i + 2);
+                m[u] = p.masses ? __ldg(p.masses + i) : 0.f;
+            } else {
+                v[u][0] = v[u][1] = v[u][2] = m[u] = 0.f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kSortUnroll; u++)
+            f(in[u], v[u], m[u]);
+    }
+}
+
+// Tile counts of one CTA's range: a shared histogram row (GLOBAL = false) or
+// straight into global totals (GLOBAL = true, for grids with many tiles).
+// Lanes of a warp that fall in the same tile are merged first
+// (__match_any_sync), so spatially ordered input costs one atomic per warp.
+template <bool GLOBAL>
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_hist(SortParams p, uint32_t *__restrict__ out, double *__restrict__ mass_part,
+                DeviceStatus *st)
+{
+    extern __shared__ uint32_t sh_hist[];
+    if (!GLOBAL) {
+        for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
+            sh_hist[i] = 0u;
+        __syncthreads();
+    }
+    uint32_t *counts = GLOBAL ? out : sh_hist;
+    const int lane = threadIdx.x & 31;
+    float msum = 0.f, mc = 0.f, mmax = 0.f;
+    unsigned bad = 0;
+    for_each_warp_batch(p, [&](bool in, const float *v, float m) {
+        uint32_t t = kNoTile;
+        if (in) {
+            int c[3];
+            float d[3];
+            if (particle_cell(p, v[0], v[1], v[2], m, c, d, t)) {
+                const float y = m - mc;  // Kahan-compensated FP32 sum of masses
+                const float s = msum + y;
+                mc = (s - msum) - y;
+                msum = s;
+                mmax = fmaxf(mmax, fabsf(m));
+            } else {
+                t = kNoTile;
+                bad++;
+            }
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, t);
+        if (t != kNoTile && lane == __ffs(peers) - 1)
+            atomicAdd(&counts[t], (uint32_t)__popc(peers));
+    });
+    __syncthreads();
+    if (!GLOBAL) {
+        uint32_t *row = out + (size_t)blockIdx.x * p.ntiles;
+        for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
+            row[i] = sh_hist[i];
+    }
+    block_mass(msum, mc, mmax, mass_part, st);
     if (bad)
         atomicAdd(&st->bad_particles, (unsigned long long)bad);
 }
@@ -163,12 +214,13 @@ __global__ void k_sort_colsum(const uint32_t *__restrict__ hist, int nsort, int 
 
 constexpr int kScanThreads = 1024;
 
-// Exclusive scan of tile totals (one CTA, chunks of kScanThreads) and the pass
-// mass.  uniform_mass >= 0 means every particle weighs uniform_mass.
+// Exclusive scan of tile totals (one CTA) and the per-pass constants.
+// uniform_mass >= 0 means every particle weighs uniform_mass.
 __global__ void __launch_bounds__(kScanThreads)
     k_sort_scan(const uint32_t *__restrict__ totals, int ntiles, uint32_t *__restrict__ tile_start,
-                const double *__restrict__ mass_part, int nsort, double uniform_mass,
-                double *field_mass, DeviceStatus *st)
+                uint32_t *__restrict__ cursor, const double *__restrict__ mass_part, int nsort,
+                double uniform_mass, double inv_cells, double *field_mass, double *field_sub,
+                DeviceStatus *st)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     __shared__ uint32_t carry;
@@ -198,12 +250,15 @@ __global__ void __launch_bounds__(kScanThreads)
                 if (lane >= o)
                     w += y;
             }
-            warp_tot[lane] = w;  // inclusive over warps
+            warp_tot[lane] = w;
         }
         __syncthreads();
         const uint32_t before = (wid ? warp_tot[wid - 1] : 0u) + carry;
-        if (t < ntiles)
+        if (t < ntiles) {
             tile_start[t] = before + x - v;
+            if (cursor)
+                cursor[t] = before + x - v;
+        }
         __syncthreads();
         if (threadIdx.x == kScanThreads - 1)
             carry = before + x;
@@ -212,7 +267,6 @@ __global__ void __launch_bounds__(kScanThreads)
     if (threadIdx.x == 0)
         tile_start[ntiles] = carry;
 
-    // Pass mass.
     double m = 0.0;
     if (uniform_mass < 0.0) {
         for (int c = threadIdx.x; c < nsort; c += blockDim.x)
@@ -231,8 +285,30 @@ __global__ void __launch_bounds__(kScanThreads)
         m = (double)carry * uniform_mass;
     }
     if (threadIdx.x == 0) {
+        // Scale: the largest |mass| maps into [2^31, 2^32) units, which leaves
+        // room for 2^31 full-mass particles in one cell of a 64-bit sum.
+        const float mref = uniform_mass >= 0.0 ? (float)fabs(uniform_mass)
+                                               : __uint_as_float(st->max_mass_bits);
+        int s = 0;
+        if (mref > 0.f && isfinite(mref))
+            s = 31 - ilogbf(mref);
+        s = max(-100, min(100, s));
+        const double mf = m * inv_cells * ldexp(1.0, s);
+        // Round the mean to 24 significant bits: exactly representable in FP32
+        // after the final 2^-s scaling.
+        long long mean_fixed;
+        const double amf = fabs(mf);
+        if (amf >= 16777216.0) {
+            const double q = ldexp(1.0, ilogb(amf) - 23);
+            mean_fixed = (long long)(rint(mf / q) * q);
+        } else {
+            mean_fixed = llrint(mf);
+        }
         st->pass_mass = m;
+        st->fx_shift = s;
+        st->mean_fixed = mean_fixed;
         *field_mass += m;
+        *field_sub += ldexp((double)mean_fixed, -s);
     }
 }
 
@@ -251,69 +327,77 @@ __global__ void k_sort_offsets(uint32_t *__restrict__ hist, int nsort, int ntile
     }
 }
 
-// Packed particle: per axis (tile-local cell << 24) | 24-bit fraction; w = mass bits.
-template <bool VARMASS>
-__global__ void __launch_bounds__(kSortThreads)
-    k_sort_scatter(SortParams p, const uint32_t *__restrict__ offs, uint4 *__restrict__ sorted)
+__device__ __forceinline__ uint4 pack_particle(const int c[3], const float d[3], float m,
+                                               uint32_t mx, uint32_t my, uint32_t mz)
 {
-    extern __shared__ uint32_t sh_cur[];
-    const uint32_t *row = offs + (size_t)blockIdx.x * p.ntiles;
-    for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
-        sh_cur[i] = row[i];
-    __syncthreads();
-    const int64_t b = (int64_t)blockIdx.x * p.chunk;
-    const int64_t e = min(p.n, b + p.chunk);
-    const float *__restrict__ pos = p.pos;
-    const uint32_t mx = (1u << p.lx) - 1u, my = (1u << p.ly) - 1u, mz = (1u << p.lz) - 1u;
-    for (int64_t i0 = b + threadIdx.x; i0 < e; i0 += (int64_t)kSortUnroll * blockDim.x) {
-        float v[kSortUnroll][3];
-        float m[kSortUnroll];
-#pragma unroll
-        for (int u = 0; u < kSortUnroll; u++) {
-            const int64_t i = i0 + (int64_t)u * blockDim.x;
-            if (i < e) {
-                v[u][0] = __ldg(pos + 3 * i);
-                v[u][1] = __ldg(pos + 3 * i + 1);
-                v[u][2] = __ldg(pos + 3 * i + 2);
-                m[u] = VARMASS ? __ldg(p.masses + i) : 0.f;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kSortUnroll; u++) {
-            const int64_t i = i0 + (int64_t)u * blockDim.x;
-            if (i >= e)
-                break;
-            int c[3];
-            float d[3];
-            uint32_t t;
-            if (!particle_cell(p, v[u][0], v[u][1], v[u][2], c, d, t) || !isfinite(m[u]))
-                continue;
-            const uint32_t slot = atomicAdd(&sh_cur[t], 1u);
-            uint4 w;
-            w.x = (((uint32_t)c[0] & mx) << 24) | frac_to_q24(d[0]);
-            w.y = (((uint32_t)c[1] & my) << 24) | frac_to_q24(d[1]);
-            w.z = (((uint32_t)c[2] & mz) << 24) | frac_to_q24(d[2]);
-            w.w = VARMASS ? __float_as_uint(m[u]) : 0u;
-            sorted[slot] = w;
-        }
-    }
+    uint4 w;
+    w.x = (((uint32_t)c[0] & mx) << 24) | frac_to_q24(d[0]);
+    w.y = (((uint32_t)c[1] & my) << 24) | frac_to_q24(d[1]);
+    w.z = (((uint32_t)c[2] & mz) << 24) | frac_to_q24(d[2]);
+    w.w = __float_as_uint(m);
+    return w;
 }
 
-// Halo face layout of one tile (SX = TX+1 etc.; e = element index):
-//   X face, local x = ext_x:        e = y*SZ + z                  y<=ext_y, z<=ext_z
-//   Y face, local y = ext_y:        e = SY*SZ + x*SZ + z          x<ext_x,  z<=ext_z
-//   Z face, local z = ext_z:        e = SY*SZ + TX*SZ + x*TY + y  x<ext_x,  y<ext_y
-template <int TX, int TY, int TZ>
-struct HaloLayout {
-    static constexpr int SX = TX + 1, SY = TY + 1, SZ = TZ + 1;
-    static constexpr int NX = SY * SZ;
-    static constexpr int NY = TX * SZ;
-    static constexpr int NZ = TX * TY;
-    static constexpr int N = NX + NY + NZ;
+// Writes every particle of the CTA's range to its slot in tile order.  Shared
+// cursors start at this CTA's offsets (GLOBAL = false) or global cursors are
+// used directly (GLOBAL = true).  Lanes in the same tile take consecutive slots
+// from one atomic.  Packed particle: per axis (tile-local cell << 24) | 24-bit
+// fraction; w = mass bits.
+template <bool GLOBAL>
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_scatter(SortParams p, uint32_t *__restrict__ offs, uint4 *__restrict__ sorted)
+{
+    extern __shared__ uint32_t sh_cur[];
+    if (!GLOBAL) {
+        const uint32_t *row = offs + (size_t)blockIdx.x * p.ntiles;
+        for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
+            sh_cur[i] = row[i];
+        __syncthreads();
+    }
+    uint32_t *cur = GLOBAL ? offs : sh_cur;
+    const uint32_t mx = (1u << p.lx) - 1u, my = (1u << p.ly) - 1u, mz = (1u << p.lz) - 1u;
+    const int lane = threadIdx.x & 31;
+    for_each_warp_batch(p, [&](bool in, const float *v, float m) {
+        uint32_t t = kNoTile;
+        int c[3] = {0, 0, 0};
+        float d[3] = {0.f, 0.f, 0.f};
+        if (in && !particle_cell(p, v[0], v[1], v[2], m, c, d, t))
+            t = kNoTile;
+        const unsigned peers = __match_any_sync(0xffffffffu, t);
+        const int leader = __ffs(peers) - 1;
+        uint32_t slot0 = 0;
+        if (t != kNoTile && lane == leader)
+            slot0 = atomicAdd(&cur[t], (uint32_t)__popc(peers));
+        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+        if (t != kNoTile)
+            sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = pack_particle(c, d, m, mx, my, mz);
+    });
+}
 
-    // Local (x, y, z) of halo element e; false where the element is unused.
-    __device__ __forceinline__ static bool decode(int e, int ex, int ey, int ez, int &x, int &y,
-                                                  int &z)
+// Halo layer of one tile (the cells at local x = ext_x, y = ext_y or z = ext_z),
+// stored as 64-bit sums.  S* = T* + 1.
+//   X face (x = ext_x):              e = y*SZ + z                   y<=ext_y, z<=ext_z
+//   Y face (y = ext_y, x < ext_x):   e = NX + x*SZ + z              z<=ext_z
+//   Z face (z = ext_z, x, y inside): e = NX + NY + x*TY + y
+// Low faces of one tile (local x = 0, y = 0 or z = 0), 64-bit sums:
+//   A (x = 0):                       e = y*TZ + z
+//   B (y = 0, x >= 1):               e = TY*TZ + x*TZ + z
+//   C (z = 0, x >= 1, y >= 1):       e = TY*TZ + TX*TZ + x*TY + y
+template <int TX, int TY, int TZ>
+struct TileLayout {
+    static constexpr int SX = TX + 1, SY = TY + 1, SZ = TZ + 1;
+    static constexpr int NACC = SX * SY * SZ;
+    static constexpr int NX = SY * SZ, NY = TX * SZ, NZ = TX * TY;
+    static constexpr int NHALO = NX + NY + NZ;
+    static constexpr int NFACE = TY * TZ + TX * TZ + TX * TY;
+
+    __device__ __forceinline__ static int acc_index(int x, int y, int z)
+    {
+        return (x * SY + y) * SZ + z;
+    }
+
+    __device__ __forceinline__ static bool halo_decode(int e, int ex, int ey, int ez, int &x,
+                                                       int &y, int &z)
     {
         if (e < NX) {
             x = ex;
@@ -334,114 +418,216 @@ struct HaloLayout {
         z = ez;
         return x < ex && y < ey;
     }
+
+    // Inverse of halo_decode for a cell on the halo layer.
+    __device__ __forceinline__ static int halo_encode(int x, int y, int z, int ex, int ey)
+    {
+        if (x == ex)
+            return y * SZ + z;
+        if (y == ey)
+            return NX + x * SZ + z;
+        return NX + NY + x * TY + y;
+    }
+
+    __device__ __forceinline__ static bool face_decode(int e, int ex, int ey, int ez, int &x,
+                                                       int &y, int &z)
+    {
+        if (e < TY * TZ) {
+            x = 0;
+            y = e / TZ;
+            z = e - y * TZ;
+            return y < ey && z < ez;
+        }
+        e -= TY * TZ;
+        if (e < TX * TZ) {
+            x = e / TZ;
+            z = e - x * TZ;
+            y = 0;
+            return x >= 1 && x < ex && z < ez;
+        }
+        e -= TX * TZ;
+        x = e / TY;
+        y = e - x * TY;
+        z = 0;
+        return x >= 1 && x < ex && y >= 1 && y < ey;
+    }
 };
 
 struct TileParams {
     int dims;
     int64_t plane;
     int row;
-    int nty, ntz;
-    float mass;          // uniform mass
-    double inv_cells;    // 1 / N^3
+    int ntx, nty, ntz;
+    float mass;  // uniform mass when the particles carry none
 };
 
 constexpr int kTileThreads = 512;
 
+__device__ __forceinline__ float fixed_to_float(long long v, float inv_scale)
+{
+    // One rounding (int64 -> float), then an exact power-of-two scaling.
+    return __ll2float_rn(v) * inv_scale;
+}
+
+// Adds this thread's share of sum (-1)^(x+y+z) * cell to the pass total: a
+// warp sum then one 64-bit atomic per warp.  Integer arithmetic modulo 2^64 is
+// exact, so the (small) final value is exact whatever the order.
+__device__ __forceinline__ void add_alternating(long long v, DeviceStatus *st)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0)
+        atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
+}
+
+__device__ __forceinline__ void tile_coords(const TileParams &p, int t, int &tx, int &ty, int &tz)
+{
+    tz = t % p.ntz;
+    ty = (t / p.ntz) % p.nty;
+    tx = t / (p.ntz * p.nty);
+}
+
 template <int TX, int TY, int TZ, bool VARMASS, bool CLEAN>
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_deposit(TileParams p, const uint4 *__restrict__ sorted,
-                   const uint32_t *__restrict__ tile_start, const DeviceStatus *__restrict__ st,
-                   float *__restrict__ grid, float *__restrict__ halo)
+                   const uint32_t *__restrict__ tile_start, DeviceStatus *__restrict__ st,
+                   float *__restrict__ grid, long long *__restrict__ faces,
+                   long long *__restrict__ halo)
 {
-    using HL = HaloLayout<TX, TY, TZ>;
-    constexpr int SX = HL::SX, SY = HL::SY, SZ = HL::SZ;
-    constexpr int NACC = SX * SY * SZ;
-    extern __shared__ float acc[];
-
+    using L = TileLayout<TX, TY, TZ>;
+    extern __shared__ unsigned long long acc[];
     const int t = blockIdx.x;
-    const int tz = t % p.ntz;
-    const int ty = (t / p.ntz) % p.nty;
-    const int tx = t / (p.ntz * p.nty);
+    int tx, ty, tz;
+    tile_coords(p, t, tx, ty, tz);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
     const int ex = min(TX, p.dims - x0), ey = min(TY, p.dims - y0), ez = min(TZ, p.dims - z0);
-
-    for (int i = threadIdx.x; i < NACC; i += blockDim.x)
-        acc[i] = 0.f;
+    for (int i = threadIdx.x; i < L::NACC; i += blockDim.x)
+        acc[i] = 0ull;
     __syncthreads();
 
+    const int s = st->fx_shift;
+    const float scale = ldexpf(1.f, s), inv_scale = ldexpf(1.f, -s);
     const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
     for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         const uint4 w = sorted[i];
         const float dx = q24_to_frac(w.x), dy = q24_to_frac(w.y), dz = q24_to_frac(w.z);
-        const float m = VARMASS ? __uint_as_float(w.w) : p.mass;
-        const int base = ((int)(w.x >> 24) * SY + (int)(w.y >> 24)) * SZ + (int)(w.z >> 24);
+        const float m = (VARMASS ? __uint_as_float(w.w) : p.mass) * scale;
+        const int base = L::acc_index((int)(w.x >> 24), (int)(w.y >> 24), (int)(w.z >> 24));
         const float tx_ = 1.f - dx, ty_ = 1.f - dy, tz_ = 1.f - dz;
         // Weight order follows fieldize.cpp:77-84: ((m*wx)*wy)*wz.
         const float mtx = m * tx_, mdx = m * dx;
         const float a00 = mtx * ty_, a10 = mdx * ty_, a01 = mtx * dy, a11 = mdx * dy;
-        atomicAdd(&acc[base], a00 * tz_);
-        atomicAdd(&acc[base + SY * SZ], a10 * tz_);
-        atomicAdd(&acc[base + SZ], a01 * tz_);
-        atomicAdd(&acc[base + SY * SZ + SZ], a11 * tz_);
-        atomicAdd(&acc[base + 1], a00 * dz);
-        atomicAdd(&acc[base + SY * SZ + 1], a10 * dz);
-        atomicAdd(&acc[base + SZ + 1], a01 * dz);
-        atomicAdd(&acc[base + SY * SZ + SZ + 1], a11 * dz);
+        constexpr int DX = L::SY * L::SZ, DY = L::SZ;
+        atomicAdd(&acc[base], (unsigned long long)__float2ll_rn(a00 * tz_));
+        atomicAdd(&acc[base + DX], (unsigned long long)__float2ll_rn(a10 * tz_));
+        atomicAdd(&acc[base + DY], (unsigned long long)__float2ll_rn(a01 * tz_));
+        atomicAdd(&acc[base + DX + DY], (unsigned long long)__float2ll_rn(a11 * tz_));
+        atomicAdd(&acc[base + 1], (unsigned long long)__float2ll_rn(a00 * dz));
+        atomicAdd(&acc[base + DX + 1], (unsigned long long)__float2ll_rn(a10 * dz));
+        atomicAdd(&acc[base + DY + 1], (unsigned long long)__float2ll_rn(a01 * dz));
+        atomicAdd(&acc[base + DX + DY + 1], (unsigned long long)__float2ll_rn(a11 * dz));
     }
     __syncthreads();
 
-    // Interior: every real cell of the grid belongs to exactly one tile.
-    const float mean = (float)(st->pass_mass * p.inv_cells);
+    // Cells strictly inside the tile (no low face): final value.
+    const long long mean = st->mean_fixed;
+    long long alt = 0;
     for (int i = threadIdx.x; i < TX * TY * TZ; i += blockDim.x) {
         const int x = i / (TY * TZ);
         const int y = (i / TZ) % TY;
         const int z = i % TZ;
-        if (x < ex && y < ey && z < ez) {
-            const float v = acc[(x * SY + y) * SZ + z] - mean;
+        if (x >= 1 && y >= 1 && z >= 1 && x < ex && y < ey && z < ez) {
+            const long long sum = (long long)acc[L::acc_index(x, y, z)];
+            const float v = fixed_to_float(sum - mean, inv_scale);
             float *dst = grid + cell_index(p.plane, p.row, x0 + x, y0 + y, z0 + z);
             if (CLEAN)
                 *dst = v;
             else
                 *dst += v;
+            alt += ((x0 + x + y0 + y + z0 + z) & 1) ? -sum : sum;
         }
     }
-    // Halo faces to scratch (zeros where unused).
-    float *h = halo + (size_t)t * HL::N;
-    for (int e = threadIdx.x; e < HL::N; e += blockDim.x) {
+    add_alternating(alt, st);
+    long long *f = faces + (size_t)t * L::NFACE;
+    for (int e = threadIdx.x; e < L::NFACE; e += blockDim.x) {
         int x, y, z;
-        const bool ok = HL::decode(e, ex, ey, ez, x, y, z);
-        h[e] = ok ? acc[(x * SY + y) * SZ + z] : 0.f;
+        if (L::face_decode(e, ex, ey, ez, x, y, z))
+            f[e] = (long long)acc[L::acc_index(x, y, z)];
+    }
+    long long *h = halo + (size_t)t * L::NHALO;
+    for (int e = threadIdx.x; e < L::NHALO; e += blockDim.x) {
+        int x, y, z;
+        if (L::halo_decode(e, ex, ey, ez, x, y, z))
+            h[e] = (long long)acc[L::acc_index(x, y, z)];
     }
 }
 
-template <int TX, int TY, int TZ>
-__global__ void __launch_bounds__(256)
-    k_halo_merge(TileParams p, const float *__restrict__ halo, float *__restrict__ grid)
+// Extent of tile index ti along an axis of `dims` cells with tiles of T.
+__device__ __forceinline__ int tile_ext(int ti, int T, int dims)
 {
-    using HL = HaloLayout<TX, TY, TZ>;
+    return min(T, dims - ti * T);
+}
+
+template <int TX, int TY, int TZ, bool CLEAN>
+__global__ void __launch_bounds__(256)
+    k_face_gather(TileParams p, const long long *__restrict__ faces,
+                  const long long *__restrict__ halo, DeviceStatus *__restrict__ st,
+                  float *__restrict__ grid)
+{
+    using L = TileLayout<TX, TY, TZ>;
     const int t = blockIdx.x;
-    const int tz = t % p.ntz;
-    const int ty = (t / p.ntz) % p.nty;
-    const int tx = t / (p.ntz * p.nty);
+    int tx, ty, tz;
+    tile_coords(p, t, tx, ty, tz);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
     const int ex = min(TX, p.dims - x0), ey = min(TY, p.dims - y0), ez = min(TZ, p.dims - z0);
-    const float *h = halo + (size_t)t * HL::N;
-    for (int e = threadIdx.x; e < HL::N; e += blockDim.x) {
-        const float v = h[e];
-        if (v == 0.f)
+    // Lower neighbour along each axis (periodic) and its extent.
+    const int txm = tx ? tx - 1 : p.ntx - 1;
+    const int tym = ty ? ty - 1 : p.nty - 1;
+    const int tzm = tz ? tz - 1 : p.ntz - 1;
+    const int exm = tile_ext(txm, TX, p.dims), eym = tile_ext(tym, TY, p.dims),
+              ezm = tile_ext(tzm, TZ, p.dims);
+    const float inv_scale = ldexpf(1.f, -st->fx_shift);
+    const long long mean = st->mean_fixed;
+    const long long *f = faces + (size_t)t * L::NFACE;
+    long long alt = 0;
+    for (int e = threadIdx.x; e < L::NFACE; e += blockDim.x) {
+        int a, b, c;
+        if (!L::face_decode(e, ex, ey, ez, a, b, c))
             continue;
-        int x, y, z;
-        if (!HL::decode(e, ex, ey, ez, x, y, z))
-            continue;
-        int gx = x0 + x, gy = y0 + y, gz = z0 + z;
-        if (gx >= p.dims)
-            gx -= p.dims;
-        if (gy >= p.dims)
-            gy -= p.dims;
-        if (gz >= p.dims)
-            gz -= p.dims;
-        atomicAdd(grid + cell_index(p.plane, p.row, gx, gy, gz), v);
+        long long sum = f[e];
+        const int zmask = (a == 0 ? 1 : 0) | (b == 0 ? 2 : 0) | (c == 0 ? 4 : 0);
+        // Every non-empty subset of the axes on which the cell sits on the low
+        // face names one lower neighbour whose halo layer holds a share of it.
+#pragma unroll
+        for (int mask = 1; mask < 8; mask++) {
+            if (mask & ~zmask)
+                continue;
+            const int sx = (mask & 1) ? txm : tx, sy = (mask & 2) ? tym : ty,
+                      sz = (mask & 4) ? tzm : tz;
+            const int sex = (mask & 1) ? exm : ex, sey = (mask & 2) ? eym : ey;
+            const int xs = (mask & 1) ? exm : a, ys = (mask & 2) ? eym : b,
+                      zs = (mask & 4) ? ezm : c;
+            const int src = (sx * p.nty + sy) * p.ntz + sz;
+            sum += halo[(size_t)src * L::NHALO + L::halo_encode(xs, ys, zs, sex, sey)];
+        }
+        const float v = fixed_to_float(sum - mean, inv_scale);
+        float *dst = grid + cell_index(p.plane, p.row, x0 + a, y0 + b, z0 + c);
+        if (CLEAN)
+            *dst = v;
+        else
+            *dst += v;
+        alt += ((x0 + a + y0 + b + z0 + c) & 1) ? -sum : sum;
     }
+    add_alternating(alt, st);
+}
+
+// The corner mode k = (N/2, N/2, N/2) of an even grid is sum (-1)^(x+y+z) rho(x):
+// this pass's exact share, in mass units, joins the grid's running value.  (The
+// subtracted mean contributes nothing: the signs balance on an even grid.)
+__global__ void k_pass_finish(const DeviceStatus *__restrict__ st, double *field_corner)
+{
+    *field_corner += ldexp((double)st->alt_sum, -st->fx_shift);
 }
 
 int ilog2(int v)
@@ -453,20 +639,20 @@ int ilog2(int v)
 }
 
 template <int TX, int TY, int TZ>
-cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a,
-                                DepositScratch &s, DeviceStatus *dstat, cudaStream_t stream,
-                                int64_t *launches, StageHook hook, void *hook_user)
+cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, DepositScratch &s,
+                                DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
+                                StageHook hook, void *hook_user)
 {
+    using L = TileLayout<TX, TY, TZ>;
     TileParams tp;
     tp.dims = g.grid.dims;
     tp.plane = g.grid.plane;
     tp.row = g.grid.row;
+    tp.ntx = g.ntx;
     tp.nty = g.nty;
     tp.ntz = g.ntz;
     tp.mass = a.mass;
-    const double n = (double)g.grid.dims;
-    tp.inv_cells = 1.0 / (n * n * n);
-    const size_t smem = sizeof(float) * (TX + 1) * (TY + 1) * (TZ + 1);
+    const size_t smem = sizeof(unsigned long long) * L::NACC;
     const bool var = a.masses != nullptr;
     cudaError_t err;
 #define GENPK_TILE_LAUNCH(V, C)                                                                \
@@ -477,7 +663,7 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a,
         if (err != cudaSuccess)                                                                \
             return err;                                                                        \
         kern<<<g.ntiles, kTileThreads, smem, stream>>>(tp, s.sorted, s.tile_start, dstat,      \
-                                                      a.grid, s.halo);                         \
+                                                      a.grid, s.faces, s.halo);                \
     } while (0)
     if (var && a.clean)
         GENPK_TILE_LAUNCH(true, true);
@@ -493,10 +679,19 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a,
         hook(hook_user, "dep_tile");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    k_halo_merge<TX, TY, TZ><<<g.ntiles, 256, 0, stream>>>(tp, s.halo, a.grid);
+    if (a.clean)
+        k_face_gather<TX, TY, TZ, true><<<g.ntiles, 256, 0, stream>>>(tp, s.faces, s.halo, dstat,
+                                                                      a.grid);
+    else
+        k_face_gather<TX, TY, TZ, false><<<g.ntiles, 256, 0, stream>>>(tp, s.faces, s.halo,
+                                                                       dstat, a.grid);
     (*launches)++;
     if (hook)
-        hook(hook_user, "dep_halo");
+        hook(hook_user, "dep_faces");
+    if ((err = cudaGetLastError()) != cudaSuccess)
+        return err;
+    k_pass_finish<<<1, 1, 0, stream>>>(dstat, a.field_corner);
+    (*launches)++;
     return cudaGetLastError();
 }
 
@@ -505,12 +700,7 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a,
 bool deposit_tile_supported(int tx, int ty, int tz)
 {
     return (tx == 8 && ty == 8 && tz == 8) || (tx == 16 && ty == 16 && tz == 16) ||
-           (tx == 16 && ty == 32 && tz == 32) || (tx == 32 && ty == 32 && tz == 32);
-}
-
-int halo_floats(int tx, int ty, int tz)
-{
-    return (ty + 1) * (tz + 1) + tx * (tz + 1) + tx * ty;
+           (tx == 16 && ty == 16 && tz == 32);
 }
 
 TileShape deposit_default_tile(int dims, int64_t n)
@@ -518,9 +708,14 @@ TileShape deposit_default_tile(int dims, int64_t n)
     (void)n;
     if (dims <= 64)
         return {8, 8, 8};
-    if (dims <= 512)
-        return {16, 16, 16};
-    return {32, 32, 32};
+    return {16, 16, 16};
+}
+
+void deposit_scratch_sizes(const DepositGeom &g, size_t *face_elems, size_t *halo_elems)
+{
+    const int tx = g.tx, ty = g.ty, tz = g.tz;
+    *face_elems = (size_t)g.ntiles * (size_t)(ty * tz + tx * tz + tx * ty);
+    *halo_elems = (size_t)g.ntiles * (size_t)((ty + 1) * (tz + 1) + tx * (tz + 1) + tx * ty);
 }
 
 size_t deposit_hist_smem(const DepositGeom &g)
@@ -528,11 +723,19 @@ size_t deposit_hist_smem(const DepositGeom &g)
     return sizeof(uint32_t) * (size_t)g.ntiles;
 }
 
+bool deposit_shared_hist(const DepositGeom &g)
+{
+    return deposit_hist_smem(g) <= 160 * 1024;
+}
+
 int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms)
 {
-    const size_t smem = deposit_hist_smem(g) + 1024;
-    int per_sm = (int)std::min<size_t>(4, (200 * 1024) / std::max<size_t>(smem, 1));
-    per_sm = std::max(per_sm, 1);
+    int per_sm = 4;
+    if (deposit_shared_hist(g)) {
+        const size_t smem = deposit_hist_smem(g) + 1024;
+        per_sm = (int)std::min<size_t>(4, (200 * 1024) / std::max<size_t>(smem, 1));
+        per_sm = std::max(per_sm, 1);
+    }
     const int64_t want = (n + 4095) / 4096;
     return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms * per_sm, want));
 }
@@ -562,54 +765,59 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     sp.nty = g.nty;
     sp.ntz = g.ntz;
     sp.ntiles = g.ntiles;
-    const size_t hsmem = deposit_hist_smem(g);
+    const bool shared_hist = deposit_shared_hist(g);
+    const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
     cudaError_t err;
-    if ((err = cudaFuncSetAttribute(k_sort_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)hsmem)) != cudaSuccess)
+    if ((err = cudaMemsetAsync(&dstat->max_mass_bits, 0, sizeof(unsigned), stream)) !=
+        cudaSuccess)
         return err;
-    k_sort_hist<<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.mass_part, dstat);
-    mark("dep_hist");
-    if ((err = cudaGetLastError()) != cudaSuccess)
+    if ((err = cudaMemsetAsync(&dstat->alt_sum, 0, sizeof(long long), stream)) != cudaSuccess)
         return err;
     const int tb = 256, tgrid = (g.ntiles + tb - 1) / tb;
-    k_sort_colsum<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.totals);
-    mark("dep_colsum");
-    k_sort_scan<<<1, kScanThreads, 0, stream>>>(s.totals, g.ntiles, s.tile_start, s.mass_part,
-                                                sort_ctas,
-                                                a.masses ? -1.0 : (double)a.mass, a.field_mass,
-                                                dstat);
-    mark("dep_scan");
-    k_sort_offsets<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.tile_start);
-    mark("dep_offsets");
-    if ((err = cudaGetLastError()) != cudaSuccess)
-        return err;
-    if (a.masses) {
-        if ((err = cudaFuncSetAttribute(k_sort_scatter<true>,
+    const size_t hsmem = deposit_hist_smem(g);
+    if (shared_hist) {
+        if ((err = cudaFuncSetAttribute(k_sort_hist<false>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hsmem)) != cudaSuccess)
             return err;
-        k_sort_scatter<true><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted);
+        k_sort_hist<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.mass_part,
+                                                                       dstat);
+        mark("dep_hist");
+        k_sort_colsum<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.totals);
+        mark("dep_colsum");
     } else {
+        if ((err = cudaMemsetAsync(s.totals, 0, sizeof(uint32_t) * g.ntiles, stream)) !=
+            cudaSuccess)
+            return err;
+        k_sort_hist<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.totals, s.mass_part,
+                                                                  dstat);
+        mark("dep_hist");
+    }
+    if ((err = cudaGetLastError()) != cudaSuccess)
+        return err;
+    k_sort_scan<<<1, kScanThreads, 0, stream>>>(
+        s.totals, g.ntiles, s.tile_start, shared_hist ? nullptr : s.cursor, s.mass_part,
+        sort_ctas, a.masses ? -1.0 : (double)a.mass, 1.0 / n3, a.field_mass, a.field_sub, dstat);
+    mark("dep_scan");
+    if (shared_hist) {
+        k_sort_offsets<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.tile_start);
+        mark("dep_offsets");
         if ((err = cudaFuncSetAttribute(k_sort_scatter<false>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hsmem)) != cudaSuccess)
             return err;
         k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted);
+    } else {
+        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.cursor, s.sorted);
     }
     mark("dep_scatter");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
     if (g.tx == 8)
-        return launch_tile_kernels<8, 8, 8>(g, a, s, dstat, stream, launches, hook,
-                                                hook_user);
-    if (g.tx == 16 && g.ty == 16)
-        return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook,
-                                                hook_user);
-    if (g.tx == 16)
-        return launch_tile_kernels<16, 32, 32>(g, a, s, dstat, stream, launches, hook,
-                                                hook_user);
-    return launch_tile_kernels<32, 32, 32>(g, a, s, dstat, stream, launches, hook,
-                                                hook_user);
+        return launch_tile_kernels<8, 8, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
+    if (g.tz == 16)
+        return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook, hook_user);
+    return launch_tile_kernels<16, 16, 32>(g, a, s, dstat, stream, launches, hook, hook_user);
 }
 
 }  // namespace genpk

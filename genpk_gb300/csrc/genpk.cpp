@@ -52,7 +52,9 @@ struct genpk_ctx {
 
     float *grids = nullptr;  // nfields contiguous grids of gg.nfloat floats
     std::vector<int> state;
-    double *d_field_mass = nullptr;  // [nfields]
+    // [3*nfields]: deposited mass, subtracted mean, exact (N/2,N/2,N/2) mode
+    double *d_field_mass = nullptr;
+    std::vector<bool> corner_valid;  // the corner value belongs to the grid's spectrum
     DeviceStatus *d_status = nullptr;
 
     BinTables tables;
@@ -243,14 +245,19 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         return fail(ctx, GENPK_ERR_UNSUPPORTED, "more than 2^32-1 particles in one pass");
     const DepositGeom g = deposit_geom(ctx, boxsize);
     const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
-    if (deposit_hist_smem(g) > 200 * 1024)
-        return fail(ctx, GENPK_ERR_UNSUPPORTED, "too many deposit tiles for the shared histogram");
     DepositScratch &s = ctx->dscr;
-    GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
+    if (deposit_shared_hist(g)) {
+        GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
+    } else {
+        GENPK_TRY(grow(ctx, &s.cursor, &s.cursor_cap, (size_t)g.ntiles));
+    }
     GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
     GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
     GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
-    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, (size_t)g.ntiles * g.halo_per_tile));
+    size_t nface = 0, nhalo = 0;
+    deposit_scratch_sizes(g, &nface, &nhalo);
+    GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface));
+    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo));
     size_t mp = (size_t)s.mass_part_cap;
     GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
     s.mass_part_cap = (int)mp;
@@ -262,6 +269,8 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     a.n = n;
     a.grid = grid_of(ctx, f);
     a.field_mass = ctx->d_field_mass + f;
+    a.field_sub = ctx->d_field_mass + ctx->nfields + f;
+    a.field_corner = ctx->d_field_mass + 2 * ctx->nfields + f;
     a.clean = ctx->state[(size_t)f] == F_CLEAN;
     timing_touch(ctx);
     GENPK_CUDA(deposit_pass(g, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
@@ -417,8 +426,10 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need)
         GENPK_TRY(make_r2c(ctx, batch, &h));
         float *base = grid_of(ctx, todo[i]);
         GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
-        for (size_t k = i; k < j; k++)
+        for (size_t k = i; k < j; k++) {
             ctx->state[(size_t)todo[k]] = F_SPECTRUM;
+            ctx->corner_valid[(size_t)todo[k]] = true;
+        }
         i = j;
     }
     stage_event(ctx, "fft");
@@ -463,6 +474,10 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
                     } else {
                         slot[e] = l.nfields + added;
                         l.fields[slot[e]] = fp;
+                        const int fi = pairs[2 * q + e];
+                        l.corner[slot[e]] = ctx->corner_valid[(size_t)fi]
+                                                ? ctx->d_field_mass + 2 * ctx->nfields + fi
+                                                : nullptr;
                         added++;
                     }
                 }
@@ -563,6 +578,8 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->dscr.totals);
     cudaFree(ctx->dscr.sorted);
     cudaFree(ctx->dscr.halo);
+    cudaFree(ctx->dscr.faces);
+    cudaFree(ctx->dscr.cursor);
     cudaFree(ctx->dscr.mass_part);
     cudaFree(ctx->stage_pos);
     cudaFree(ctx->stage_mass);
@@ -616,8 +633,8 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     for (auto &e : ctx->ev)
         CREATE_CUDA(cudaEventCreate(&e));
     CREATE_CUDA(cudaMalloc(&ctx->grids, sizeof(float) * (size_t)ctx->gg.nfloat * nfields));
-    CREATE_CUDA(cudaMalloc(&ctx->d_field_mass, sizeof(double) * nfields));
-    CREATE_CUDA(cudaMemset(ctx->d_field_mass, 0, sizeof(double) * nfields));
+    CREATE_CUDA(cudaMalloc(&ctx->d_field_mass, sizeof(double) * 3 * nfields));
+    CREATE_CUDA(cudaMemset(ctx->d_field_mass, 0, sizeof(double) * 3 * nfields));
     CREATE_CUDA(cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)));
     CREATE_CUDA(cudaMemset(ctx->d_status, 0, sizeof(DeviceStatus)));
     CREATE_CUDA(cudaMalloc(&ctx->bdev.thr, sizeof(uint32_t) * (nrbins + 1)));
@@ -638,6 +655,7 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     ctx->auto_power.assign((size_t)nfields, {});
     ctx->auto_mass.assign((size_t)nfields, 0.0);
     ctx->auto_valid.assign((size_t)nfields, false);
+    ctx->corner_valid.assign((size_t)nfields, false);
     ctx->tile = deposit_default_tile((int)dims, 0);
     (void)rc;
     *out = ctx;
@@ -653,6 +671,10 @@ int genpk_zero(genpk_ctx *ctx, int field)
     ctx->state[(size_t)field] = F_CLEAN;
     ctx->auto_valid[(size_t)field] = false;
     GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
+    GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + ctx->nfields + field, 0, sizeof(double),
+                               ctx->stream));
+    GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + 2 * ctx->nfields + field, 0, sizeof(double),
+                               ctx->stream));
     return GENPK_OK;
 }
 
@@ -763,6 +785,7 @@ int genpk_load_spectrum(genpk_ctx *ctx, int field, const double *spectrum)
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->state[(size_t)field] = F_SPECTRUM;
     ctx->auto_valid[(size_t)field] = false;
+    ctx->corner_valid[(size_t)field] = false;
     return GENPK_OK;
 }
 
@@ -798,14 +821,12 @@ int genpk_read_field(genpk_ctx *ctx, int field, double *out)
     if (st != F_DENSITY)
         return fail(ctx, GENPK_ERR_STATE, "genpk_read_field: field is not a density");
     std::vector<float> tmp(nf);
-    double mass = 0.0;
+    double mean = 0.0;  // the exact sum of the (fixed-point) means subtracted by the passes
     GENPK_CUDA(cudaMemcpyAsync(tmp.data(), grid_of(ctx, field), sizeof(float) * nf,
                                cudaMemcpyDeviceToHost, ctx->stream));
-    GENPK_CUDA(cudaMemcpyAsync(&mass, ctx->d_field_mass + field, sizeof(double),
+    GENPK_CUDA(cudaMemcpyAsync(&mean, ctx->d_field_mass + ctx->nfields + field, sizeof(double),
                                cudaMemcpyDeviceToHost, ctx->stream));
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-    const double n = (double)ctx->dims;
-    const double mean = mass / (n * n * n);
     const int row = ctx->gg.row, dims = (int)ctx->dims;
     for (size_t i = 0; i < nf; i++) {
         const int z = (int)(i % (size_t)row);
@@ -854,6 +875,10 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     if (recompute || !have) {
         ctx->state[(size_t)field] = F_CLEAN;
         GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + ctx->nfields + field, 0, sizeof(double),
+                                   ctx->stream));
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + 2 * ctx->nfields + field, 0,
+                                   sizeof(double), ctx->stream));
         GENPK_TRY(run_deposit(ctx, field, boxsize, dpos, dmass, (float)mass, n));
         GENPK_TRY(genpk_power(ctx, field, field, mass_norm, mass_norm, pw.data(), nullptr, nullptr));
     } else {
@@ -950,10 +975,7 @@ int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z)
     GENPK_TRY(flush_pending(ctx));
     const TileShape old = ctx->tile;
     ctx->tile = TileShape{tile_x, tile_y, tile_z};
-    if (deposit_hist_smem(deposit_geom(ctx, 1.0)) > 200 * 1024) {
-        ctx->tile = old;
-        return fail(ctx, GENPK_ERR_UNSUPPORTED, "too many tiles of that shape for this grid");
-    }
+    (void)old;
     return GENPK_OK;
 }
 

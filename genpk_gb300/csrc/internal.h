@@ -46,19 +46,27 @@ struct DepositScratch {
     size_t tile_start_cap = 0;
     uint32_t *totals = nullptr;      // [ntiles]
     size_t tile_cap = 0;
+    uint32_t *cursor = nullptr;      // [ntiles] scatter cursors (global-counter mode)
+    size_t cursor_cap = 0;
     uint4 *sorted = nullptr;         // [cap] packed tile-local particles (x,y,z words, mass bits)
     size_t sorted_cap = 0;           // particles
-    float *halo = nullptr;           // [ntiles][halo_per_tile]
-    size_t halo_cap = 0;             // floats
+    long long *faces = nullptr;      // [ntiles][face cells] 64-bit low-face sums
+    size_t faces_cap = 0;
+    long long *halo = nullptr;       // [ntiles][halo cells] 64-bit halo-layer sums
+    size_t halo_cap = 0;
     double *mass_part = nullptr;     // [sort_ctas]
     int mass_part_cap = 0;
 };
 
-// Device words a deposit pass reports through (all zero-initialised).
+// Device words a deposit pass reports through (zero-initialised).
 struct DeviceStatus {
-    unsigned long long bad_particles;  // non-finite positions seen (skipped)
+    unsigned long long bad_particles;  // non-finite positions/masses seen (skipped)
     unsigned long long timeouts;       // bounded waits that gave up
     double pass_mass;                  // mass deposited by the latest pass
+    long long mean_fixed;              // pass mean in 2^-fx_shift mass units
+    long long alt_sum;                 // sum over cells of (-1)^(x+y+z) * cell, fixed point
+    int fx_shift;                      // weights are accumulated as round(w * 2^fx_shift)
+    unsigned max_mass_bits;            // max |mass| of the pass, as float bits
 };
 
 struct DepositArgs {
@@ -68,6 +76,8 @@ struct DepositArgs {
     int64_t n;
     float *grid;           // device padded grid
     double *field_mass;    // device: running mass of this grid
+    double *field_sub;     // device: running sum of the means subtracted from it
+    double *field_corner;  // device: exact DFT value at k = (N/2, N/2, N/2), even N
     bool clean;            // grid content is undefined and must be overwritten
 };
 
@@ -79,6 +89,11 @@ bool deposit_tile_supported(int tx, int ty, int tz);
 TileShape deposit_default_tile(int dims, int64_t n);
 int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms);
 size_t deposit_hist_smem(const DepositGeom &g);
+// True when the per-CTA tile histogram fits in shared memory (else the pass
+// uses global counters).
+bool deposit_shared_hist(const DepositGeom &g);
+// 64-bit elements of face and halo scratch one pass needs.
+void deposit_scratch_sizes(const DepositGeom &g, size_t *face_elems, size_t *halo_elems);
 
 // Called after each kernel launch of a pass with the kernel's short name
 // (used to record timing events); may be null.
@@ -129,6 +144,9 @@ constexpr int kMaxBinPairs = 10;
 
 struct BinLaunch {
     const float2 *fields[kMaxBinFields];  // half-complex spectra (in-place layout)
+    // Exact value of the (N/2, N/2, N/2) mode per field (device double), or null
+    // to use the transform's own value.
+    const double *corner[kMaxBinFields];
     int nfields;
     BinPair pairs[kMaxBinPairs];
     int npairs;

@@ -29,6 +29,8 @@ namespace {
 
 struct BinParams {
     const float2 *f[kMaxBinFields];
+    const double *corner[kMaxBinFields];  // exact (N/2,N/2,N/2) value per field, or null
+    int64_t corner_row;                   // row index i*N+j of that mode, -1 if none
     int pa[kMaxBinPairs], pb[kMaxBinPairs];
     int np;          // pairs actually reported (<= NP of the instantiation)
     int dims, hc, half;
@@ -166,6 +168,15 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                 for (int f = 0; f < NF; f++)
                     fv[f] = buf[f * kBinBuf + q];
+                if (r == p.corner_row && kz == p.half) {
+                    // The last log-k bin holds this single mode; its exact value
+                    // (an alternating sum computed by the deposit) replaces the
+                    // FP32 transform's, whose rounding noise it cannot average.
+#pragma unroll
+                    for (int f = 0; f < NF; f++)
+                        if (p.corner[f])
+                            fv[f] = make_float2((float)*p.corner[f], 0.f);
+                }
 #pragma unroll
                 for (int s = 0; s < NP; s++) {
                     const float2 a = pick<NF>(fv, p.pa[s]), c = pick<NF>(fv, p.pb[s]);
@@ -280,8 +291,11 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
 {
     const Shape s = pick_shape(l.nfields, l.npairs);
     BinParams p;
-    for (int f = 0; f < kMaxBinFields; f++)
+    for (int f = 0; f < kMaxBinFields; f++) {
         p.f[f] = l.fields[f < l.nfields ? f : 0];
+        p.corner[f] = l.corner[f < l.nfields ? f : 0];
+    }
+    p.corner_row = (g.dims % 2 == 0) ? (int64_t)g.half * g.dims + g.half : -1;
     for (int q = 0; q < kMaxBinPairs; q++) {
         const int src = q < l.npairs ? q : 0;
         p.pa[q] = l.pairs[src].a;

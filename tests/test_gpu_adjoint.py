@@ -67,7 +67,7 @@ def test_adjoint_matches_fp64_reference_gradient(gp, kind, dims, var):
     grad_close(gpos, rpos)
     if var:
         grad_close(gmass, rmass)
-    assert abs(dldm - rdldm) <= 1e-6 * abs(rdldm) + 1e-300
+    assert abs(dldm - rdldm) <= G_RTOL * abs(rdldm) + 1e-300
 
 
 def test_adjoint_recompute_equals_stored_spectrum(gp):
@@ -99,8 +99,9 @@ def test_adjoint_device_pointers(gp):
         h = ctx.adjoint(0, box, pos, g, m, masses=masses, recompute=True)
         d = ctx.adjoint(0, box, torch.from_numpy(pos).cuda(), g, m,
                         masses=torch.from_numpy(masses).cuda(), recompute=True)
-    np.testing.assert_allclose(d[0].cpu().numpy(), h[0], rtol=1e-6, atol=1e-7 * np.abs(h[0]).max())
-    np.testing.assert_allclose(d[1].cpu().numpy(), h[1], rtol=1e-6, atol=1e-7 * np.abs(h[1]).max())
+    # the deposit is bit-reproducible, so host and device inputs give identical gradients
+    assert np.array_equal(d[0].cpu().numpy(), h[0])
+    assert np.array_equal(d[1].cpu().numpy(), h[1])
 
 
 def test_adjoint_central_finite_differences_256_particles(gp):

@@ -176,16 +176,62 @@ def test_small_and_odd_grids(gp, dims):
     bins_close(p, pr, c, rtol=2e-5)
 
 
-@pytest.mark.parametrize("tile", [(8, 8, 8), (16, 16, 16), (16, 32, 32), (32, 32, 32)])
-def test_tile_shapes_agree(gp, tile):
+def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
+    """64-bit fixed-point accumulation: the grid does not depend on summation
+    order, tile shape or where the particles came from."""
+    import torch
     from genpk_gb300 import synth
     dims, box = 96, 1000.0
     pos = synth.uniform(200000, box, seed=7)
+    masses = np.linspace(0.2, 3.0, len(pos)).astype(np.float32)
+    ref = O.deposit(pos, box, dims, masses, 0.0)
+    grids = []
+    for tile in [(8, 8, 8), (16, 16, 16), (16, 16, 32)]:
+        with gp.Context(dims, 16) as ctx:
+            ctx.set_tile(*tile)
+            ctx.deposit(0, box, pos, masses)
+            grids.append(ctx.read_field(0))
+            ctx.zero(0)
+            ctx.deposit(0, box, torch.from_numpy(pos).cuda(), torch.from_numpy(masses).cuda())
+            grids.append(ctx.read_field(0))
+    grid_close(grids[0], ref)
+    for g in grids[1:]:
+        assert np.array_equal(g, grids[0])
+
+
+def test_global_counter_sort_mode(gp):
+    """More tiles than a shared histogram holds (8^3 tiles on 288^3: 46656
+    tiles) switches the sort to warp-aggregated global counters."""
+    from genpk_gb300 import synth
+    dims, box, nrbins = 288, 1000.0, 32
+    pos = synth.uniform(400000, box, seed=8)
     ref = O.deposit(pos, box, dims, None, 1.0)
-    with gp.Context(dims, 16) as ctx:
-        ctx.set_tile(*tile)
+    m = O.total_mass(len(pos), None, 1.0)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.set_tile(8, 8, 8)
         ctx.deposit(0, box, pos, None, 1.0)
-        grid_close(ctx.read_field(0), ref)
+        g8 = ctx.read_field(0)
+        ctx.zero(0)
+        ctx.set_tile(16, 16, 16)
+        ctx.deposit(0, box, pos, None, 1.0)
+        g16 = ctx.read_field(0)
+        p, c, _ = ctx.power(0, 0, m, m)
+    grid_close(g8, ref)
+    assert np.array_equal(g8, g16)
+    pr, cr, _ = O.pk(pos, box, dims, nrbins, None, 1.0, m_norm=m)
+    bins_close(p, pr, c)
+
+
+def test_dense_cells_accumulate_exactly(gp):
+    """Thousands of particles per cell: 64-bit integer sums lose nothing."""
+    rng = np.random.default_rng(3)
+    dims, box = 4, 4.0
+    pos = (rng.random((200000, 3)) * box).astype(np.float32)
+    ref = O.deposit(pos, box, dims, None, 1.0)
+    with gp.Context(dims, 4) as ctx:
+        ctx.deposit(0, box, pos, None, 1.0)
+        g = ctx.read_field(0)
+    grid_close(g, ref, tol=1e-7)
 
 
 # ---------------------------------------------------------------------------
