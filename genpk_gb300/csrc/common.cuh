@@ -38,6 +38,58 @@ __device__ __forceinline__ void split_cell(float p, float uh, float ul, int dims
     frac = d;
 }
 
+// Unevaluated sum hi + lo of two floats (double-float arithmetic, Dekker/Knuth).
+struct f2sum {
+    float hi, lo;
+};
+
+__device__ __forceinline__ f2sum two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ f2sum renorm(float hi, float lo)
+{
+    const float s = __fadd_rn(hi, lo);
+    return {s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+
+__device__ __forceinline__ f2sum f2_add(f2sum a, float b)
+{
+    const f2sum s = two_sum(a.hi, b);
+    return renorm(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ f2sum f2_mul(f2sum a, f2sum b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return renorm(p, e);
+}
+
+// 1 - 2d for one axis of a particle, d = x - floor(x), x = p*units, as a float
+// pair good to ~2^-44.  The carry decisions repeat split_cell's exactly, so the
+// value belongs to the same cell split_cell returns.
+__device__ __forceinline__ f2sum one_minus_2frac(float p, float uh, float ul)
+{
+    const float xh = __fmul_rn(p, uh);
+    const float xe = fmaf(p, uh, -xh);
+    const float xl = fmaf(p, ul, xe);
+    const float f = floorf(xh);
+    f2sum d = two_sum(__fsub_rn(xh, f), xl);
+    if (d.hi < 0.f)
+        d = f2_add(d, 1.f);
+    if (d.hi >= 1.f)
+        d = f2_add(d, -1.f);
+    const f2sum u = two_sum(1.f, -2.f * d.hi);
+    return renorm(u.hi, __fsub_rn(u.lo, 2.f * d.lo));
+}
+
 // 24-bit fixed point of a fraction in [0,1); exact in FP32 on the way back.
 __device__ __forceinline__ uint32_t frac_to_q24(float d)
 {

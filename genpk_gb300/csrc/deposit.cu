@@ -66,6 +66,8 @@ struct SortParams {
     int lx, ly, lz;  // log2 of the tile edges
     int nty, ntz;
     int ntiles;
+    float umass;     // uniform mass when masses == nullptr
+    int corner;      // accumulate the exact (N/2,N/2,N/2) mode (even grids)
 };
 
 constexpr int kSortThreads = 512;
@@ -338,14 +340,35 @@ __device__ __forceinline__ uint4 pack_particle(const int c[3], const float d[3],
     return w;
 }
 
+// Adds this thread's share of the corner-mode sum to the pass total: a warp
+// sum then one 64-bit atomic per warp.  Integer arithmetic modulo 2^64 is
+// exact, so the (small) final value is exact whatever the order.
+__device__ __forceinline__ void add_alternating(long long v, DeviceStatus *st)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0)
+        atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
+}
+
 // Writes every particle of the CTA's range to its slot in tile order.  Shared
 // cursors start at this CTA's offsets (GLOBAL = false) or global cursors are
 // used directly (GLOBAL = true).  Lanes in the same tile take consecutive slots
 // from one atomic.  Packed particle: per axis (tile-local cell << 24) | 24-bit
 // fraction; w = mass bits.
+//
+// On even grids it also sums the corner mode k = (N/2, N/2, N/2) of the CIC
+// density exactly: that DFT coefficient is sum over particles of
+// m (-1)^(x+y+z) prod_a (1 - 2 d_a) with (x, y, z) the particle's cell and d_a
+// its fractions.  Each term is formed from the full two-product position in
+// float-pair arithmetic, rounded to an integer of 2^-s mass units and summed in
+// 64-bit integers (exact, order-independent).  The last log-k bin holds only
+// this mode, so its value must not carry the FP32 grid's rounding noise.
 template <bool GLOBAL>
 __global__ void __launch_bounds__(kSortThreads)
-    k_sort_scatter(SortParams p, uint32_t *__restrict__ offs, uint4 *__restrict__ sorted)
+    k_sort_scatter(SortParams p, uint32_t *__restrict__ offs, uint4 *__restrict__ sorted,
+                   DeviceStatus *st)
 {
     extern __shared__ uint32_t sh_cur[];
     if (!GLOBAL) {
@@ -357,6 +380,8 @@ __global__ void __launch_bounds__(kSortThreads)
     uint32_t *cur = GLOBAL ? offs : sh_cur;
     const uint32_t mx = (1u << p.lx) - 1u, my = (1u << p.ly) - 1u, mz = (1u << p.lz) - 1u;
     const int lane = threadIdx.x & 31;
+    const float mscale = ldexpf(1.f, st->fx_shift);
+    long long alt = 0;
     for_each_warp_batch(p, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
         int c[3] = {0, 0, 0};
@@ -369,9 +394,20 @@ __global__ void __launch_bounds__(kSortThreads)
         if (t != kNoTile && lane == leader)
             slot0 = atomicAdd(&cur[t], (uint32_t)__popc(peers));
         slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-        if (t != kNoTile)
+        if (t != kNoTile) {
             sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = pack_particle(c, d, m, mx, my, mz);
+            if (p.corner) {
+                const float mm = (p.masses ? m : p.umass) * mscale;
+                f2sum u = f2_mul(one_minus_2frac(v[0], p.uh, p.ul), one_minus_2frac(v[1], p.uh, p.ul));
+                u = f2_mul(u, one_minus_2frac(v[2], p.uh, p.ul));
+                u = f2_mul(u, f2sum{mm, 0.f});
+                const long long w = __float2ll_rn(u.hi) + __float2ll_rn(u.lo);
+                alt += ((c[0] + c[1] + c[2]) & 1) ? -w : w;
+            }
+        }
     });
+    if (p.corner)
+        add_alternating(alt, st);
 }
 
 // Halo layer of one tile (the cells at local x = ext_x, y = ext_y or z = ext_z),
@@ -469,18 +505,6 @@ __device__ __forceinline__ float fixed_to_float(long long v, float inv_scale)
     return __ll2float_rn(v) * inv_scale;
 }
 
-// Adds this thread's share of sum (-1)^(x+y+z) * cell to the pass total: a
-// warp sum then one 64-bit atomic per warp.  Integer arithmetic modulo 2^64 is
-// exact, so the (small) final value is exact whatever the order.
-__device__ __forceinline__ void add_alternating(long long v, DeviceStatus *st)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0)
-        atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
-}
-
 __device__ __forceinline__ void tile_coords(const TileParams &p, int t, int &tx, int &ty, int &tz)
 {
     tz = t % p.ntz;
@@ -532,7 +556,6 @@ __global__ void __launch_bounds__(kTileThreads)
 
     // Cells strictly inside the tile (no low face): final value.
     const long long mean = st->mean_fixed;
-    long long alt = 0;
     for (int i = threadIdx.x; i < TX * TY * TZ; i += blockDim.x) {
         const int x = i / (TY * TZ);
         const int y = (i / TZ) % TY;
@@ -545,10 +568,8 @@ __global__ void __launch_bounds__(kTileThreads)
                 *dst = v;
             else
                 *dst += v;
-            alt += ((x0 + x + y0 + y + z0 + z) & 1) ? -sum : sum;
         }
     }
-    add_alternating(alt, st);
     long long *f = faces + (size_t)t * L::NFACE;
     for (int e = threadIdx.x; e < L::NFACE; e += blockDim.x) {
         int x, y, z;
@@ -590,7 +611,6 @@ __global__ void __launch_bounds__(256)
     const float inv_scale = ldexpf(1.f, -st->fx_shift);
     const long long mean = st->mean_fixed;
     const long long *f = faces + (size_t)t * L::NFACE;
-    long long alt = 0;
     for (int e = threadIdx.x; e < L::NFACE; e += blockDim.x) {
         int a, b, c;
         if (!L::face_decode(e, ex, ey, ez, a, b, c))
@@ -617,9 +637,7 @@ __global__ void __launch_bounds__(256)
             *dst = v;
         else
             *dst += v;
-        alt += ((x0 + a + y0 + b + z0 + c) & 1) ? -sum : sum;
     }
-    add_alternating(alt, st);
 }
 
 // The corner mode k = (N/2, N/2, N/2) of an even grid is sum (-1)^(x+y+z) rho(x):
@@ -765,6 +783,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     sp.nty = g.nty;
     sp.ntz = g.ntz;
     sp.ntiles = g.ntiles;
+    sp.umass = a.mass;
+    sp.corner = (g.grid.dims % 2 == 0) ? 1 : 0;
     const bool shared_hist = deposit_shared_hist(g);
     const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
     cudaError_t err;
@@ -806,9 +826,10 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hsmem)) != cudaSuccess)
             return err;
-        k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted);
+        k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted,
+                                                                         dstat);
     } else {
-        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.cursor, s.sorted);
+        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.cursor, s.sorted, dstat);
     }
     mark("dep_scatter");
     if ((err = cudaGetLastError()) != cudaSuccess)
