@@ -20,6 +20,7 @@ import numpy as np
 from . import native
 
 GENPK_FLAG_TIMING = 0x1
+ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW = 0, 1, 2
 
 
 class GenPKError(RuntimeError):
@@ -198,6 +199,14 @@ class Context:
         v = [ctypes.c_int() for _ in range(4)]
         self._chk(self.lib.genpk_deposit_config(self.h, *[ctypes.byref(x) for x in v]))
         return {"tile": (v[0].value, v[1].value, v[2].value), "sort_ctas": v[3].value}
+
+    def set_engine(self, engine: int):
+        """Deposit engine: ENGINE_AUTO, ENGINE_SORTED (exact) or ENGINE_WINDOW."""
+        self._chk(self.lib.genpk_set_deposit_engine(self.h, int(engine)))
+
+    @property
+    def last_engine(self) -> int:
+        return int(self.lib.genpk_last_deposit_engine(self.h))
 
     def set_tile(self, tx: int, ty: int, tz: int):
         self._chk(self.lib.genpk_set_deposit_tile(self.h, tx, ty, tz))

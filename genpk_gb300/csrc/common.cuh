@@ -31,11 +31,42 @@ __device__ __forceinline__ void split_cell(float p, float uh, float ul, int dims
         d = __fsub_rn(d, 1.f);
         fi += 1;
     }
-    fi %= dims;
-    if (fi < 0)
-        fi += dims;
+    if ((unsigned)fi >= (unsigned)dims) {  // outside [0, dims): periodic wrap
+        fi %= dims;
+        if (fi < 0)
+            fi += dims;
+    }
     cell = fi;
     frac = d;
+}
+
+// Nearest float to a 64-bit integer (ties to even), with integer instructions
+// only: the hardware int64 -> float conversion runs on the FP64 pipe, which
+// GB300 has little of.
+__device__ __forceinline__ float i64_to_f32_rn(long long v)
+{
+    const unsigned neg = (unsigned)((unsigned long long)v >> 63);
+    unsigned long long a = neg ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    if (a == 0ull)
+        return 0.f;
+    int e = 63 - __clzll((long long)a);  // position of the leading one
+    unsigned m;
+    if (e <= 23) {
+        m = (unsigned)a << (23 - e);
+    } else {
+        const int sh = e - 23;
+        unsigned long long q = a >> sh;
+        const unsigned long long rem = a & ((1ull << sh) - 1ull);
+        const unsigned long long half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull)))
+            q++;
+        if (q == (1ull << 24)) {
+            q >>= 1;
+            e++;
+        }
+        m = (unsigned)q;
+    }
+    return __uint_as_float((neg << 31) | ((unsigned)(e + 127) << 23) | (m & 0x7fffffu));
 }
 
 // Unevaluated sum hi + lo of two floats (double-float arithmetic, Dekker/Knuth).
@@ -61,6 +92,12 @@ __device__ __forceinline__ f2sum f2_add(f2sum a, float b)
 {
     const f2sum s = two_sum(a.hi, b);
     return renorm(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ f2sum f2_add2(f2sum a, f2sum b)
+{
+    const f2sum s = two_sum(a.hi, b.hi);
+    return renorm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
 __device__ __forceinline__ f2sum f2_mul(f2sum a, f2sum b)

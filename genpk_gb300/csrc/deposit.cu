@@ -287,13 +287,14 @@ __global__ void __launch_bounds__(kScanThreads)
         m = (double)carry * uniform_mass;
     }
     if (threadIdx.x == 0) {
-        // Scale: the largest |mass| maps into [2^31, 2^32) units, which leaves
-        // room for 2^31 full-mass particles in one cell of a 64-bit sum.
+        // Scale: the largest |mass| maps into [2^27, 2^28) units of 2^-s, so one
+        // CIC weight is below 2^28 (the 32-bit shared accumulators carry at most
+        // once per 2^4 adds) and 64-bit cell sums hold 2^35 full-mass particles.
         const float mref = uniform_mass >= 0.0 ? (float)fabs(uniform_mass)
                                                : __uint_as_float(st->max_mass_bits);
         int s = 0;
         if (mref > 0.f && isfinite(mref))
-            s = 31 - ilogbf(mref);
+            s = 27 - ilogbf(mref);
         s = max(-100, min(100, s));
         const double mf = m * inv_cells * ldexp(1.0, s);
         // Round the mean to 24 significant bits: exactly representable in FP32
@@ -340,18 +341,6 @@ __device__ __forceinline__ uint4 pack_particle(const int c[3], const float d[3],
     return w;
 }
 
-// Adds this thread's share of the corner-mode sum to the pass total: a warp
-// sum then one 64-bit atomic per warp.  Integer arithmetic modulo 2^64 is
-// exact, so the (small) final value is exact whatever the order.
-__device__ __forceinline__ void add_alternating(long long v, DeviceStatus *st)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0)
-        atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
-}
-
 // Writes every particle of the CTA's range to its slot in tile order.  Shared
 // cursors start at this CTA's offsets (GLOBAL = false) or global cursors are
 // used directly (GLOBAL = true).  Lanes in the same tile take consecutive slots
@@ -362,8 +351,9 @@ __device__ __forceinline__ void add_alternating(long long v, DeviceStatus *st)
 // density exactly: that DFT coefficient is sum over particles of
 // m (-1)^(x+y+z) prod_a (1 - 2 d_a) with (x, y, z) the particle's cell and d_a
 // its fractions.  Each term is formed from the full two-product position in
-// float-pair arithmetic, rounded to an integer of 2^-s mass units and summed in
-// 64-bit integers (exact, order-independent).  The last log-k bin holds only
+// float-pair arithmetic and summed per thread in float pairs; each warp's total
+// is rounded to an integer of 2^-(s+4) mass units and summed in 64-bit integers
+// (deterministic: fixed per-thread order, integer sums across warps).  The last log-k bin holds only
 // this mode, so its value must not carry the FP32 grid's rounding noise.
 template <bool GLOBAL>
 __global__ void __launch_bounds__(kSortThreads)
@@ -380,8 +370,10 @@ __global__ void __launch_bounds__(kSortThreads)
     uint32_t *cur = GLOBAL ? offs : sh_cur;
     const uint32_t mx = (1u << p.lx) - 1u, my = (1u << p.ly) - 1u, mz = (1u << p.lz) - 1u;
     const int lane = threadIdx.x & 31;
-    const float mscale = ldexpf(1.f, st->fx_shift);
-    long long alt = 0;
+    // Corner terms in 2^-(s+4) mass units (|term| < 2^32), summed per thread as
+    // a float pair and converted to an integer once per warp.
+    const float mscale = ldexpf(1.f, st->fx_shift + 4);
+    f2sum alt = {0.f, 0.f};
     for_each_warp_batch(p, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
         int c[3] = {0, 0, 0};
@@ -401,13 +393,25 @@ __global__ void __launch_bounds__(kSortThreads)
                 f2sum u = f2_mul(one_minus_2frac(v[0], p.uh, p.ul), one_minus_2frac(v[1], p.uh, p.ul));
                 u = f2_mul(u, one_minus_2frac(v[2], p.uh, p.ul));
                 u = f2_mul(u, f2sum{mm, 0.f});
-                const long long w = __float2ll_rn(u.hi) + __float2ll_rn(u.lo);
-                alt += ((c[0] + c[1] + c[2]) & 1) ? -w : w;
+                if ((c[0] + c[1] + c[2]) & 1)
+                    u = f2sum{-u.hi, -u.lo};
+                alt = f2_add2(alt, u);
             }
         }
     });
-    if (p.corner)
-        add_alternating(alt, st);
+    if (p.corner) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const f2sum other = {__shfl_xor_sync(0xffffffffu, alt.hi, o),
+                                 __shfl_xor_sync(0xffffffffu, alt.lo, o)};
+            alt = f2_add2(alt, other);
+        }
+        if (lane == 0) {
+            const long long w = __float2ll_rn(alt.hi) + __float2ll_rn(alt.lo);
+            if (w != 0)
+                atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)w);
+        }
+    }
 }
 
 // Halo layer of one tile (the cells at local x = ext_x, y = ext_y or z = ext_z),
@@ -502,7 +506,7 @@ constexpr int kTileThreads = 512;
 __device__ __forceinline__ float fixed_to_float(long long v, float inv_scale)
 {
     // One rounding (int64 -> float), then an exact power-of-two scaling.
-    return __ll2float_rn(v) * inv_scale;
+    return i64_to_f32_rn(v) * inv_scale;
 }
 
 __device__ __forceinline__ void tile_coords(const TileParams &p, int t, int &tx, int &ty, int &tz)
@@ -510,6 +514,46 @@ __device__ __forceinline__ void tile_coords(const TileParams &p, int t, int &tx,
     tz = t % p.ntz;
     ty = (t / p.ntz) % p.nty;
     tx = t / (p.ntz * p.nty);
+}
+
+// 64-bit cell sum kept as two 32-bit shared words: lo takes each weight with a
+// native 32-bit atomic, and the rare carry out of it (weights are < 2^28, so at
+// most one add in 2^4 carries) goes to hi.  Exact and order-independent.
+__device__ __forceinline__ void acc_add(unsigned *lo, unsigned *hi, int idx, unsigned w, bool neg)
+{
+    if (w == 0u)
+        return;
+    if (!neg) {
+        const unsigned old = atomicAdd(&lo[idx], w);
+        if (old + w < old)
+            atomicAdd(&hi[idx], 1u);
+    } else {  // adding -w: lo += 2^32 - w, hi += carry - 1
+        const unsigned wl = 0u - w;
+        const unsigned old = atomicAdd(&lo[idx], wl);
+        if (!(old + wl < old))
+            atomicAdd(&hi[idx], 0xffffffffu);
+    }
+}
+
+__device__ __forceinline__ long long acc_get(const unsigned *lo, const unsigned *hi, int idx)
+{
+    return (long long)(((unsigned long long)hi[idx] << 32) | lo[idx]);
+}
+
+// CIC corner weight in 2^-s mass units from the 24-bit fractions, integer
+// instructions only.  a, b, c are the per-axis factors (2^24 - q or q, so
+// a*b*c / 2^72 is the product of the CIC factors); the particle's mass is
+// mant * 2^(e - 23) and sh = 54 - s - e.  Intermediate truncations keep
+// ~31 bits; the result is rounded to nearest.
+__device__ __forceinline__ unsigned corner_weight(unsigned long long ab, unsigned c, unsigned mant,
+                                                  int sh)
+{
+    const unsigned p2 = (unsigned)(ab >> 17);
+    const unsigned y = (unsigned)(((unsigned long long)p2 * c) >> 24);
+    const unsigned long long z = (unsigned long long)y * mant;
+    if (sh >= 64)
+        return 0u;
+    return (unsigned)((z + (1ull << (sh - 1))) >> sh);
 }
 
 template <int TX, int TY, int TZ, bool VARMASS, bool CLEAN>
@@ -520,37 +564,58 @@ __global__ void __launch_bounds__(kTileThreads)
                    long long *__restrict__ halo)
 {
     using L = TileLayout<TX, TY, TZ>;
-    extern __shared__ unsigned long long acc[];
+    extern __shared__ unsigned acc_words[];
+    unsigned *lo = acc_words, *hi = acc_words + L::NACC;
     const int t = blockIdx.x;
     int tx, ty, tz;
     tile_coords(p, t, tx, ty, tz);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
     const int ex = min(TX, p.dims - x0), ey = min(TY, p.dims - y0), ez = min(TZ, p.dims - z0);
-    for (int i = threadIdx.x; i < L::NACC; i += blockDim.x)
-        acc[i] = 0ull;
+    for (int i = threadIdx.x; i < 2 * L::NACC; i += blockDim.x)
+        acc_words[i] = 0u;
     __syncthreads();
 
     const int s = st->fx_shift;
-    const float scale = ldexpf(1.f, s), inv_scale = ldexpf(1.f, -s);
+    const float inv_scale = ldexpf(1.f, -s);
+    // Uniform mass as mantissa and exponent.
+    const unsigned ubits = __float_as_uint(p.mass);
+    const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
+    const int ush = 54 - s - (int)((ubits >> 23) & 0xffu) + 127;
+    const bool uneg = (ubits >> 31) != 0u;
+    const bool uzero = ((ubits >> 23) & 0xffu) == 0u;
     const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
     for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         const uint4 w = sorted[i];
-        const float dx = q24_to_frac(w.x), dy = q24_to_frac(w.y), dz = q24_to_frac(w.z);
-        const float m = (VARMASS ? __uint_as_float(w.w) : p.mass) * scale;
+        unsigned mant = umant;
+        int sh = ush;
+        bool neg = uneg, zero = uzero;
+        if (VARMASS) {
+            const unsigned mb = w.w;
+            const unsigned ef = (mb >> 23) & 0xffu;
+            mant = (mb & 0x7fffffu) | 0x800000u;
+            sh = 54 - s - (int)ef + 127;
+            neg = (mb >> 31) != 0u;
+            zero = ef == 0u;  // zero or subnormal mass deposits nothing
+        }
+        if (zero)
+            continue;
+        sh = max(sh, 1);
+        const unsigned qx = w.x & 0xffffffu, qy = w.y & 0xffffffu, qz = w.z & 0xffffffu;
+        const unsigned rx = 0x1000000u - qx, ry = 0x1000000u - qy, rz = 0x1000000u - qz;
         const int base = L::acc_index((int)(w.x >> 24), (int)(w.y >> 24), (int)(w.z >> 24));
-        const float tx_ = 1.f - dx, ty_ = 1.f - dy, tz_ = 1.f - dz;
-        // Weight order follows fieldize.cpp:77-84: ((m*wx)*wy)*wz.
-        const float mtx = m * tx_, mdx = m * dx;
-        const float a00 = mtx * ty_, a10 = mdx * ty_, a01 = mtx * dy, a11 = mdx * dy;
         constexpr int DX = L::SY * L::SZ, DY = L::SZ;
-        atomicAdd(&acc[base], (unsigned long long)__float2ll_rn(a00 * tz_));
-        atomicAdd(&acc[base + DX], (unsigned long long)__float2ll_rn(a10 * tz_));
-        atomicAdd(&acc[base + DY], (unsigned long long)__float2ll_rn(a01 * tz_));
-        atomicAdd(&acc[base + DX + DY], (unsigned long long)__float2ll_rn(a11 * tz_));
-        atomicAdd(&acc[base + 1], (unsigned long long)__float2ll_rn(a00 * dz));
-        atomicAdd(&acc[base + DX + 1], (unsigned long long)__float2ll_rn(a10 * dz));
-        atomicAdd(&acc[base + DY + 1], (unsigned long long)__float2ll_rn(a01 * dz));
-        atomicAdd(&acc[base + DX + DY + 1], (unsigned long long)__float2ll_rn(a11 * dz));
+        const unsigned long long a00 = (unsigned long long)rx * ry;  // (x, y) lower corners
+        const unsigned long long a10 = (unsigned long long)qx * ry;
+        const unsigned long long a01 = (unsigned long long)rx * qy;
+        const unsigned long long a11 = (unsigned long long)qx * qy;
+        acc_add(lo, hi, base, corner_weight(a00, rz, mant, sh), neg);
+        acc_add(lo, hi, base + DX, corner_weight(a10, rz, mant, sh), neg);
+        acc_add(lo, hi, base + DY, corner_weight(a01, rz, mant, sh), neg);
+        acc_add(lo, hi, base + DX + DY, corner_weight(a11, rz, mant, sh), neg);
+        acc_add(lo, hi, base + 1, corner_weight(a00, qz, mant, sh), neg);
+        acc_add(lo, hi, base + DX + 1, corner_weight(a10, qz, mant, sh), neg);
+        acc_add(lo, hi, base + DY + 1, corner_weight(a01, qz, mant, sh), neg);
+        acc_add(lo, hi, base + DX + DY + 1, corner_weight(a11, qz, mant, sh), neg);
     }
     __syncthreads();
 
@@ -561,7 +626,7 @@ __global__ void __launch_bounds__(kTileThreads)
         const int y = (i / TZ) % TY;
         const int z = i % TZ;
         if (x >= 1 && y >= 1 && z >= 1 && x < ex && y < ey && z < ez) {
-            const long long sum = (long long)acc[L::acc_index(x, y, z)];
+            const long long sum = acc_get(lo, hi, L::acc_index(x, y, z));
             const float v = fixed_to_float(sum - mean, inv_scale);
             float *dst = grid + cell_index(p.plane, p.row, x0 + x, y0 + y, z0 + z);
             if (CLEAN)
@@ -574,13 +639,13 @@ __global__ void __launch_bounds__(kTileThreads)
     for (int e = threadIdx.x; e < L::NFACE; e += blockDim.x) {
         int x, y, z;
         if (L::face_decode(e, ex, ey, ez, x, y, z))
-            f[e] = (long long)acc[L::acc_index(x, y, z)];
+            f[e] = acc_get(lo, hi, L::acc_index(x, y, z));
     }
     long long *h = halo + (size_t)t * L::NHALO;
     for (int e = threadIdx.x; e < L::NHALO; e += blockDim.x) {
         int x, y, z;
         if (L::halo_decode(e, ex, ey, ez, x, y, z))
-            h[e] = (long long)acc[L::acc_index(x, y, z)];
+            h[e] = acc_get(lo, hi, L::acc_index(x, y, z));
     }
 }
 
@@ -645,7 +710,7 @@ __global__ void __launch_bounds__(256)
 // subtracted mean contributes nothing: the signs balance on an even grid.)
 __global__ void k_pass_finish(const DeviceStatus *__restrict__ st, double *field_corner)
 {
-    *field_corner += ldexp((double)st->alt_sum, -st->fx_shift);
+    *field_corner += ldexp((double)st->alt_sum, -(st->fx_shift + 4));
 }
 
 int ilog2(int v)
@@ -670,7 +735,7 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
     tp.nty = g.nty;
     tp.ntz = g.ntz;
     tp.mass = a.mass;
-    const size_t smem = sizeof(unsigned long long) * L::NACC;
+    const size_t smem = 2 * sizeof(unsigned) * L::NACC;
     const bool var = a.masses != nullptr;
     cudaError_t err;
 #define GENPK_TILE_LAUNCH(V, C)                                                                \

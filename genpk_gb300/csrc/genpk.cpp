@@ -29,6 +29,8 @@ namespace {
 enum FieldState { F_CLEAN = 0, F_DENSITY = 1, F_SPECTRUM = 2, F_GRADIENT = 3 };
 
 constexpr int kMaxStages = 64;
+// Below this many particles a pass always uses the sorted engine.
+constexpr int64_t kWindowMinParticles = (int64_t)1 << 20;
 
 struct Pending {
     bool active = false;
@@ -70,6 +72,10 @@ struct genpk_ctx {
     // deposit
     TileShape tile{16, 16, 16};
     DepositScratch dscr;
+    int engine = GENPK_ENGINE_AUTO;   // requested deposit engine
+    int last_engine = GENPK_ENGINE_AUTO;  // engine the latest pass used
+    long long *d_probe = nullptr;     // window-engine probe results
+    size_t probe_cap = 0;
 
     // staging of host particles
     float *stage_pos = nullptr;
@@ -244,24 +250,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     if (n > 0xffffffffLL - 1)
         return fail(ctx, GENPK_ERR_UNSUPPORTED, "more than 2^32-1 particles in one pass");
     const DepositGeom g = deposit_geom(ctx, boxsize);
-    const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
     DepositScratch &s = ctx->dscr;
-    if (deposit_shared_hist(g)) {
-        GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
-    } else {
-        GENPK_TRY(grow(ctx, &s.cursor, &s.cursor_cap, (size_t)g.ntiles));
-    }
-    GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
-    GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
-    GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
-    size_t nface = 0, nhalo = 0;
-    deposit_scratch_sizes(g, &nface, &nhalo);
-    GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface));
-    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo));
-    size_t mp = (size_t)s.mass_part_cap;
-    GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
-    s.mass_part_cap = (int)mp;
-
     DepositArgs a;
     a.pos = pos;
     a.masses = masses;
@@ -272,9 +261,59 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     a.field_sub = ctx->d_field_mass + ctx->nfields + f;
     a.field_corner = ctx->d_field_mass + 2 * ctx->nfields + f;
     a.clean = ctx->state[(size_t)f] == F_CLEAN;
+    StageHook hook = (ctx->flags & GENPK_FLAG_TIMING) ? deposit_hook : nullptr;
+
+    int engine = ctx->engine;
+    if (engine == GENPK_ENGINE_AUTO) {
+        // Spatially coherent order (most snapshot layouts) -> window engine;
+        // anything else -> sorted engine.  Decided on a sample of chunks.
+        engine = GENPK_ENGINE_SORTED;
+        if (n >= kWindowMinParticles) {
+            const int samples = 64;
+            GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)samples));
+            GENPK_CUDA(window_probe(g, a, ctx->d_probe, samples, ctx->stream, &ctx->launches));
+            long long vol[64];
+            const int64_t chunks = (n + window_chunk(g.grid.dims) - 1) / window_chunk(g.grid.dims);
+            const int got = (int)std::min<int64_t>(samples, chunks);
+            GENPK_CUDA(cudaMemcpyAsync(vol, ctx->d_probe, sizeof(long long) * got,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            int fit = 0;
+            for (int i = 0; i < got; i++)
+                fit += vol[i] <= (long long)(0.9 * kWindowCapCells) ? 1 : 0;
+            if (got > 0 && fit * 10 >= got * 9)
+                engine = GENPK_ENGINE_WINDOW;
+        }
+    }
+    ctx->last_engine = engine;
     timing_touch(ctx);
-    GENPK_CUDA(deposit_pass(g, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
-                            (ctx->flags & GENPK_FLAG_TIMING) ? deposit_hook : nullptr, ctx));
+    if (engine == GENPK_ENGINE_WINDOW) {
+        const int mass_ctas = ctx->num_sms * 4;
+        size_t mp = (size_t)s.mass_part_cap;
+        GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)mass_ctas));
+        s.mass_part_cap = (int)mp;
+        GENPK_CUDA(deposit_window_pass(g, a, s.mass_part, mass_ctas, ctx->d_status, ctx->stream,
+                                       &ctx->launches, hook, ctx));
+    } else {
+        const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
+        if (deposit_shared_hist(g)) {
+            GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
+        } else {
+            GENPK_TRY(grow(ctx, &s.cursor, &s.cursor_cap, (size_t)g.ntiles));
+        }
+        GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
+        GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
+        GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
+        size_t nface = 0, nhalo = 0;
+        deposit_scratch_sizes(g, &nface, &nhalo);
+        GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface));
+        GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo));
+        size_t mp = (size_t)s.mass_part_cap;
+        GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
+        s.mass_part_cap = (int)mp;
+        GENPK_CUDA(deposit_pass(g, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
+                                hook, ctx));
+    }
     ctx->state[(size_t)f] = F_DENSITY;
     ctx->auto_valid[(size_t)f] = false;
     return GENPK_OK;
@@ -587,6 +626,7 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->d_power);
     cudaFree(ctx->d_gcoef);
     cudaFree(ctx->adj_buf);
+    cudaFree(ctx->d_probe);
     for (auto &e : ctx->ev)
         if (e)
             cudaEventDestroy(e);
@@ -977,6 +1017,23 @@ int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z)
     ctx->tile = TileShape{tile_x, tile_y, tile_z};
     (void)old;
     return GENPK_OK;
+}
+
+int genpk_set_deposit_engine(genpk_ctx *ctx, int engine)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (engine != GENPK_ENGINE_AUTO && engine != GENPK_ENGINE_SORTED &&
+        engine != GENPK_ENGINE_WINDOW)
+        return fail(ctx, GENPK_ERR_INVALID, "unknown deposit engine");
+    GENPK_TRY(flush_pending(ctx));
+    ctx->engine = engine;
+    return GENPK_OK;
+}
+
+int genpk_last_deposit_engine(const genpk_ctx *ctx)
+{
+    return ctx ? ctx->last_engine : -1;
 }
 
 int64_t genpk_kernel_launches(const genpk_ctx *ctx)

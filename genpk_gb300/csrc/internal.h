@@ -67,6 +67,7 @@ struct DeviceStatus {
     long long alt_sum;                 // sum over cells of (-1)^(x+y+z) * cell, fixed point
     int fx_shift;                      // weights are accumulated as round(w * 2^fx_shift)
     unsigned max_mass_bits;            // max |mass| of the pass, as float bits
+    float win_mean;                    // window engine: mean subtracted from every cell
 };
 
 struct DepositArgs {
@@ -105,6 +106,17 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
                          DeviceStatus *dstat, int sort_ctas, cudaStream_t stream,
                          int64_t *launches, StageHook hook, void *hook_user);
 
+// Window engine (deposit_window.cu) for spatially coherent particle order.
+constexpr int kWindowCapCells = 53248;  // shared window: 208 KB of FP32 cells
+int window_chunk(int dims);             // particles per CTA chunk
+// Box volume (cells) of `samples` evenly spread chunks, written to vol_dev.
+cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,
+                         int samples, cudaStream_t stream, int64_t *launches);
+// One window-engine pass; mass_part needs mass_ctas doubles (variable masses).
+cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, double *mass_part,
+                                int mass_ctas, DeviceStatus *dstat, cudaStream_t stream,
+                                int64_t *launches, StageHook hook, void *hook_user);
+
 // ---------------------------------------------------------------------------
 // Binning (deconvolution + log-k shells)
 // ---------------------------------------------------------------------------
@@ -123,6 +135,22 @@ struct BinTables {
 // Build all tables with the reference's expressions.  Returns false and sets
 // *err on failure (non-monotone bins, bin index out of range).
 bool build_bin_tables(int64_t dims, int nrbins, BinTables *t, std::string *err);
+
+// The same tables written into caller storage (no allocation):
+// thr[nrbins+1], iw[dims], count[nrbins], keffs[nrbins], lut[table_kk2max+1],
+// cnt2[table_r2max+1] (work space).
+struct TableSpans {
+    uint32_t *thr;
+    float *iw;
+    int64_t *count;
+    double *keffs;
+    int32_t *lut;
+    int64_t *cnt2;
+};
+int64_t table_kk2max(int64_t dims);
+int64_t table_r2max(int64_t dims);
+bool build_bin_tables_into(int64_t dims, int nrbins, const TableSpans &o, double *binsperunit,
+                           const char **why);
 double ref_onedinvwindow(int64_t k, int64_t n);
 double ref_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
 

@@ -55,77 +55,110 @@ int64_t ref_bin(int64_t kk2, double binsperunit)
 
 }  // namespace
 
-bool build_bin_tables(int64_t dims, int nrbins, BinTables *t, std::string *err)
+int64_t table_kk2max(int64_t dims)
 {
-    t->dims = dims;
-    t->nrbins = nrbins;
-    t->binsperunit = (nrbins - 1) / log(sqrt(3) * dims / 2.0);
     const int64_t half = dims / 2;
-    const int64_t kz_hi = half;  // largest stored kz
-    const int64_t r2max = 2 * half * half;
-    t->kk2max = r2max + kz_hi * kz_hi;
-    if (t->kk2max > 0x7fffffffLL) {
-        *err = "grid too large for 32-bit |k|^2";
+    return 3 * half * half;
+}
+
+int64_t table_r2max(int64_t dims)
+{
+    const int64_t half = dims / 2;
+    return 2 * half * half;
+}
+
+bool build_bin_tables_into(int64_t dims, int nrbins, const TableSpans &o, double *binsperunit_out,
+                           const char **why)
+{
+    const double binsperunit = (nrbins - 1) / log(sqrt(3) * dims / 2.0);
+    *binsperunit_out = binsperunit;
+    const int64_t half = dims / 2;
+    const int64_t r2max = table_r2max(dims);
+    const int64_t kk2max = table_kk2max(dims);
+    if (kk2max > 0x7fffffffLL) {
+        *why = "grid too large for 32-bit |k|^2";
         return false;
     }
-
     // Bin of every integer |k|^2, and the thresholds thr[b] = min{kk2 : bin >= b}.
-    t->lut.assign((size_t)t->kk2max + 1, -1);
-    t->thr.assign((size_t)nrbins + 1, 0xffffffffu);
+    o.lut[0] = -1;
+    for (int b = 0; b <= nrbins; b++)
+        o.thr[b] = 0xffffffffu;
     int64_t prev = -1;
-    for (int64_t kk2 = 1; kk2 <= t->kk2max; kk2++) {
-        const int64_t b = ref_bin(kk2, t->binsperunit);
+    for (int64_t kk2 = 1; kk2 <= kk2max; kk2++) {
+        const int64_t b = ref_bin(kk2, binsperunit);
         if (b < 0 || b >= nrbins) {
-            char buf[160];
-            snprintf(buf, sizeof buf, "bin index %lld out of [0,%d) at |k|^2=%lld",
-                     (long long)b, nrbins, (long long)kk2);
-            *err = buf;
+            *why = "bin index out of range";
             return false;
         }
         if (b < prev) {
-            *err = "bin index not monotone in |k|^2";
+            *why = "bin index not monotone in |k|^2";
             return false;
         }
         for (int64_t q = prev + 1; q <= b; q++)
-            t->thr[(size_t)q] = (uint32_t)kk2;
+            o.thr[q] = (uint32_t)kk2;
         prev = b;
-        t->lut[(size_t)kk2] = (int32_t)b;
+        o.lut[kk2] = (int32_t)b;
     }
-
-    t->iw.resize((size_t)dims);
     for (int64_t i = 0; i < dims; i++)
-        t->iw[(size_t)i] = (float)ref_onedinvwindow(kval_host(i, dims), dims);
+        o.iw[i] = (float)ref_onedinvwindow(kval_host(i, dims), dims);
 
     // Weighted mode counts and mean |k| per bin.  The (i, j) pairs are grouped by
     // r2 = ki^2 + kj^2 first, so the loop is over distinct r2 values times kz.
-    std::vector<int64_t> cnt2((size_t)r2max + 1, 0);
+    for (int64_t r2 = 0; r2 <= r2max; r2++)
+        o.cnt2[r2] = 0;
     for (int64_t i = 0; i < dims; i++) {
         const int64_t ki = kval_host(i, dims);
         for (int64_t j = 0; j < dims; j++) {
             const int64_t kj = kval_host(j, dims);
-            cnt2[(size_t)(ki * ki + kj * kj)]++;
+            o.cnt2[ki * ki + kj * kj]++;
         }
     }
-    t->count.assign((size_t)nrbins, 0);
-    std::vector<double> ksum((size_t)nrbins, 0.0);
+    for (int b = 0; b < nrbins; b++) {
+        o.count[b] = 0;
+        o.keffs[b] = 0.0;
+    }
     for (int64_t r2 = 0; r2 <= r2max; r2++) {
-        const int64_t c2 = cnt2[(size_t)r2];
+        const int64_t c2 = o.cnt2[r2];
         if (!c2)
             continue;
-        for (int64_t kz = 0; kz <= kz_hi; kz++) {
+        for (int64_t kz = 0; kz <= half; kz++) {
             const int64_t kk2 = r2 + kz * kz;
             if (kk2 == 0)
                 continue;
             const int64_t w = (kz == 0 || kz == half) ? 1 : 2;
-            const int32_t b = t->lut[(size_t)kk2];
-            t->count[(size_t)b] += w * c2;
-            ksum[(size_t)b] += (double)(w * c2) * sqrt((double)kk2);
+            const int32_t b = o.lut[kk2];
+            o.count[b] += w * c2;
+            o.keffs[b] += (double)(w * c2) * sqrt((double)kk2);
         }
     }
-    t->keffs.assign((size_t)nrbins, 0.0);
     for (int b = 0; b < nrbins; b++)
-        if (t->count[(size_t)b])
-            t->keffs[(size_t)b] = ksum[(size_t)b] / (double)t->count[(size_t)b];
+        if (o.count[b])
+            o.keffs[b] /= (double)o.count[b];
+    return true;
+}
+
+bool build_bin_tables(int64_t dims, int nrbins, BinTables *t, std::string *err)
+{
+    t->dims = dims;
+    t->nrbins = nrbins;
+    t->kk2max = table_kk2max(dims);
+    if (t->kk2max > 0x7fffffffLL) {
+        *err = "grid too large for 32-bit |k|^2";
+        return false;
+    }
+    t->lut.assign((size_t)t->kk2max + 1, -1);
+    t->thr.assign((size_t)nrbins + 1, 0xffffffffu);
+    t->iw.assign((size_t)dims, 0.f);
+    t->count.assign((size_t)nrbins, 0);
+    t->keffs.assign((size_t)nrbins, 0.0);
+    std::vector<int64_t> cnt2((size_t)table_r2max(dims) + 1, 0);
+    TableSpans o{t->thr.data(), t->iw.data(), t->count.data(), t->keffs.data(), t->lut.data(),
+                 cnt2.data()};
+    const char *why = nullptr;
+    if (!build_bin_tables_into(dims, nrbins, o, &t->binsperunit, &why)) {
+        *err = why;
+        return false;
+    }
     return true;
 }
 

@@ -47,6 +47,8 @@ ABI = {
     "genpk_kernel_launches": (ctypes.c_int64, [c_void_p]),
     "genpk_set_deposit_tile": (ctypes.c_int, [c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "genpk_timing_reset": (ctypes.c_int, [c_void_p]),
+    "genpk_set_deposit_engine": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "genpk_last_deposit_engine": (ctypes.c_int, [c_void_p]),
 }
 
 COMPAT_ABI = {

@@ -167,9 +167,25 @@ int genpk_timing_reset(genpk_ctx *ctx);
 int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
                          int *sort_ctas);
 
-/* Choose the deposit tile (cells per edge; supported: 8^3, 16^3, 16x32x32,
- * 32^3).  Results do not depend on it beyond FP32 summation order. */
+/* Choose the deposit tile of the sorted engine (cells per edge; supported:
+ * 8^3, 16^3, 16x16x32).  The sorted engine's grid does not depend on it. */
 int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z);
+
+/* Deposit engines.
+ *  SORTED: counting sort into cell tiles, exact 64-bit fixed-point shared
+ *          accumulation; bit-reproducible whatever the particle order.
+ *  WINDOW: for spatially coherent particle order (lattice or Peano-Hilbert
+ *          order of most snapshots): per-chunk shared windows flushed with
+ *          FP32 atomics, no sort; the last bits depend on summation order.
+ *  AUTO (default): WINDOW when a sample of particle chunks is coherent, else
+ *          SORTED. */
+#define GENPK_ENGINE_AUTO 0
+#define GENPK_ENGINE_SORTED 1
+#define GENPK_ENGINE_WINDOW 2
+int genpk_set_deposit_engine(genpk_ctx *ctx, int engine);
+
+/* Engine the most recent deposit pass used (GENPK_ENGINE_SORTED or _WINDOW). */
+int genpk_last_deposit_engine(const genpk_ctx *ctx);
 
 /* Number of kernels the library launched on ctx since creation. */
 int64_t genpk_kernel_launches(const genpk_ctx *ctx);

@@ -188,6 +188,7 @@ def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
     grids = []
     for tile in [(8, 8, 8), (16, 16, 16), (16, 16, 32)]:
         with gp.Context(dims, 16) as ctx:
+            ctx.set_engine(gp.api.ENGINE_SORTED)
             ctx.set_tile(*tile)
             ctx.deposit(0, box, pos, masses)
             grids.append(ctx.read_field(0))
@@ -199,6 +200,79 @@ def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
         assert np.array_equal(g, grids[0])
 
 
+@pytest.mark.parametrize("var", [False, True])
+def test_window_engine_matches_oracle(gp, var):
+    """Lattice-ordered particles through the window engine (shared windows
+    per chunk, no sort)."""
+    from genpk_gb300 import synth
+    dims, box, nrbins = 128, 25000.0, 64
+    pos = synth.zeldovich(128, box, seed=3)
+    masses = np.linspace(0.5, 1.5, len(pos)).astype(np.float32) if var else None
+    mass = 0.0 if var else 1.0e-2
+    m = O.total_mass(len(pos), masses, mass)
+    ref = O.deposit(pos, box, dims, masses, mass)
+    pr, cr, _ = O.pk(pos, box, dims, nrbins, masses, mass, m_norm=m)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.deposit(0, box, pos, masses, mass)
+        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        grid_close(ctx.read_field(0), ref, tol=1e-6)
+        p, c, _ = ctx.power(0, 0, m, m)
+    assert np.array_equal(c, cr)
+    bins_close(p, pr, c)
+
+
+def test_window_engine_direct_fallback_on_random_order(gp):
+    """Randomly ordered particles: no chunk fits a window, every corner takes a
+    global atomic.  Still correct."""
+    from genpk_gb300 import synth
+    dims, box, nrbins = 64, 1000.0, 32
+    pos = synth.uniform(300000, box, seed=4)
+    m = O.total_mass(len(pos), None, 1.0)
+    pr, cr, _ = O.pk(pos, box, dims, nrbins, None, 1.0, m_norm=m)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.deposit(0, box, pos, None, 1.0)
+        grid_close(ctx.read_field(0), O.deposit(pos, box, dims, None, 1.0), tol=1e-6)
+        p, c, _ = ctx.power(0, 0, m, m)
+    bins_close(p, pr, c)
+
+
+def test_auto_engine_choice(gp):
+    from genpk_gb300 import synth
+    box = 1000.0
+    lattice = synth.zeldovich(128, box, seed=5)              # 2^21 particles, coherent
+    rand = synth.uniform(len(lattice), box, seed=6)           # same count, random order
+    with gp.Context(128, 16) as ctx:
+        ctx.deposit(0, box, lattice, None, 1.0)
+        ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        ctx.zero(0)
+        ctx.deposit(0, box, rand, None, 1.0)
+        ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_SORTED
+        ctx.zero(0)
+        ctx.deposit(0, box, lattice[:1000], None, 1.0)       # small pass: sorted
+        ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_SORTED
+
+
+def test_window_and_sorted_engines_agree(gp):
+    """Same particles, both engines, accumulate semantics across passes."""
+    from genpk_gb300 import synth
+    dims, box = 96, 1000.0
+    pos = synth.zeldovich(96, box, seed=7)
+    with gp.Context(dims, 16) as ctx:
+        grids = []
+        for eng in (gp.api.ENGINE_SORTED, gp.api.ENGINE_WINDOW):
+            ctx.set_engine(eng)
+            ctx.zero(0)
+            ctx.deposit(0, box, pos[:400000], None, 1.0)
+            ctx.deposit(0, box, pos[400000:], None, 1.0)
+            grids.append(ctx.read_field(0))
+    grid_close(grids[1], grids[0], tol=1e-6)
+
+
 def test_global_counter_sort_mode(gp):
     """More tiles than a shared histogram holds (8^3 tiles on 288^3: 46656
     tiles) switches the sort to warp-aggregated global counters."""
@@ -208,6 +282,7 @@ def test_global_counter_sort_mode(gp):
     ref = O.deposit(pos, box, dims, None, 1.0)
     m = O.total_mass(len(pos), None, 1.0)
     with gp.Context(dims, nrbins) as ctx:
+        ctx.set_engine(gp.api.ENGINE_SORTED)
         ctx.set_tile(8, 8, 8)
         ctx.deposit(0, box, pos, None, 1.0)
         g8 = ctx.read_field(0)
