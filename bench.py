@@ -275,11 +275,12 @@ def main():
     pk_, pk_src = peaks()
     peak = float(pk_["hbm_gbs"])
     b_dep, b_bin = algorithmic_bytes(npart, n)
-    t_dep = sum(v for k, v in stages.items() if k.startswith("dep_")) * 1e-3
+    t_dep = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_"))) * 1e-3
     t_bin = stages.get("bin", 0.0) * 1e-3
     ach_dep = b_dep / t_dep / 1e9
     ach_bin = b_bin / t_bin / 1e9 if t_bin > 0 else None
-    roofline = {"kernel": "deposit pass (k_sort_hist .. k_halo_merge)", "bound": "hbm",
+    engine = {1: "sorted", 2: "window"}.get(ctx.last_engine, "?")
+    roofline = {"kernel": f"deposit pass ({engine} engine: all its kernels)", "bound": "hbm",
                 "achieved": ach_dep, "peak": peak, "unit": "GB/s", "frac": ach_dep / peak,
                 "peak_source": pk_src, "traffic": NCU_DEPOSIT_TRAFFIC,
                 "algorithmic_bytes": b_dep,
@@ -294,7 +295,8 @@ def main():
             "config": config_dict(args, npart), "ms_per_spectrum": ms_step,
             "wall_ms_per_step": wall / args.steps * 1e3,
             "stages_ms": {k: round(v, 5) for k, v in stages.items()},
-            "roofline": roofline, "gpu_launches": launches, "clocks": clk}
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk,
+            "deposit_engine": engine}
 
     # forward + adjoint / forward
     if not args.no_adjoint:

@@ -442,9 +442,15 @@ WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk,
 
 }  // namespace
 
+// Chunk length: small enough that a lattice-ordered chunk (rows of dims
+// particles) covers well under half of the grid along any axis, large enough
+// that a window is reused by many particles.
 int window_chunk(int dims)
 {
-    return dims > 512 ? 4096 : 8192;
+    if (dims > 512)
+        return 4096;
+    const int64_t quarter_plane = (int64_t)dims * dims / 8;
+    return (int)std::max<int64_t>(1024, std::min<int64_t>(8192, quarter_plane));
 }
 
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,

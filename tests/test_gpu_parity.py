@@ -215,6 +215,7 @@ def test_window_engine_matches_oracle(gp, var):
     with gp.Context(dims, nrbins) as ctx:
         ctx.set_engine(gp.api.ENGINE_WINDOW)
         ctx.deposit(0, box, pos, masses, mass)
+        ctx.sync()
         assert ctx.last_engine == gp.api.ENGINE_WINDOW
         grid_close(ctx.read_field(0), ref, tol=1e-6)
         p, c, _ = ctx.power(0, 0, m, m)
