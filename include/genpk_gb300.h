@@ -190,6 +190,36 @@ int genpk_last_deposit_engine(const genpk_ctx *ctx);
 /* Number of kernels the library launched on ctx since creation. */
 int64_t genpk_kernel_launches(const genpk_ctx *ctx);
 
+/* Largest sizes genpk_power_noalloc accepts. */
+#define GENPK_NOALLOC_MAX_DIMS 1024
+#define GENPK_NOALLOC_MAX_NRBINS 1024
+
+/* Deconvolution + log-k binning of a spectrum already on the GPU, without
+ * allocating any memory.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- code running under an allocator that
+ * owns the device, or a loop that cannot afford an allocation's implicit
+ * synchronisation -- and so cannot create a genpk_ctx.
+ *
+ * spectrum_a / spectrum_b: device pointers to FP32 half-complex spectra of a
+ *   dims^3 grid in the in-place r2c layout (dims*dims*(dims/2+1) interleaved
+ *   re, im pairs, rows of dims/2+1 complex values); spectrum_b may be NULL or
+ *   equal to spectrum_a for an auto spectrum.
+ * power: device pointer, nrbins doubles, written in stream order.
+ * count, keffs: host arrays of nrbins (may be NULL), filled before returning.
+ * stream: a cudaStream_t, or NULL for the default stream.
+ * Same normalisation as genpk_power; the last bin uses the spectrum's own
+ * (k = N/2, N/2, N/2) value.  dims <= GENPK_NOALLOC_MAX_DIMS and
+ * nrbins <= GENPK_NOALLOC_MAX_NRBINS, else GENPK_ERR_UNSUPPORTED.
+ *
+ * Its scratch (about 2.5 MB: bin tables and per-block partial sums) is a
+ * static array in the library's device image, held by every GPU that loads the
+ * library until the process exits.  The first call on each device looks up
+ * the array's device address.  Every call shares the array and keeps its last
+ * contents, so calls that overlap on the GPU race; serialise them. */
+int genpk_power_noalloc(const float *spectrum_a, const float *spectrum_b, int64_t dims,
+                        int nrbins, double mass_a, double mass_b, double *power, int *count,
+                        double *keffs, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
