@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--engine", choices=["auto", "sorted", "window"], default="auto",
+                    help="deposit engine (default: the library's automatic choice)")
     return ap.parse_args()
 
 
@@ -231,6 +233,7 @@ def main():
     dpos = synth.zeldovich(nside, box, seed=1 + rank, device="cuda")
     torch.cuda.synchronize()
     ctx = gp.Context(n, nrbins, timing=True)
+    ctx.set_engine({"auto": 0, "sorted": 1, "window": 2}[args.engine])
 
     def step(src):
         ctx.timing_reset()

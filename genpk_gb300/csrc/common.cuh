@@ -127,6 +127,60 @@ __device__ __forceinline__ f2sum one_minus_2frac(float p, float uh, float ul)
     return renorm(u.hi, __fsub_rn(u.lo, 2.f * d.lo));
 }
 
+// One axis of a particle in full: the wrapped cell and FP32 fraction exactly as
+// split_cell computes them, plus what the exact corner-mode term needs:
+// u = 1 - 2*(xh - floor) for the final cell (exact in FP32 for xh >= 1; off by
+// at most 2^-25 below) and xl, the low part of x = xh + xl, so that
+// 1 - 2d = u - 2*xl exactly.
+struct AxisSplit {
+    int cell;
+    float frac;
+    float u;
+    float xl;
+};
+
+__device__ __forceinline__ AxisSplit split_axis(float p, float uh, float ul, int dims)
+{
+    const float xh = __fmul_rn(p, uh);
+    const float xe = fmaf(p, uh, -xh);
+    const float xl = fmaf(p, ul, xe);
+    const float f = floorf(xh);
+    const float a = __fsub_rn(xh, f);
+    float d = __fadd_rn(a, xl);
+    float u = __fsub_rn(1.f, __fmul_rn(2.f, a));
+    int fi = (int)f;
+    if (d < 0.f) {
+        d = __fadd_rn(d, 1.f);
+        fi -= 1;
+        u = __fsub_rn(u, 2.f);
+    }
+    if (d >= 1.f) {
+        d = __fsub_rn(d, 1.f);
+        fi += 1;
+        u = __fadd_rn(u, 2.f);
+    }
+    if ((unsigned)fi >= (unsigned)dims) {
+        fi %= dims;
+        if (fi < 0)
+            fi += dims;
+    }
+    return {fi, d, u, xl};
+}
+
+// prod_a (1 - 2 d_a) = prod_a (u_a - 2 xl_a) as a float pair: the product of
+// the u's with two-product steps (error ~2^-47) plus the first-order xl terms
+// in FP32 (second-order terms are ~2^-48 and dropped).
+__device__ __forceinline__ f2sum corner_factor(const AxisSplit &x, const AxisSplit &y,
+                                               const AxisSplit &z)
+{
+    const float p = __fmul_rn(x.u, y.u);
+    const float pl = fmaf(x.u, y.u, -p);
+    const float q = __fmul_rn(p, z.u);
+    const float ql = fmaf(p, z.u, -q) + pl * z.u;
+    const float corr = -2.f * (x.xl * (y.u * z.u) + y.xl * (x.u * z.u) + z.xl * (x.u * y.u));
+    return {q, ql + corr};
+}
+
 // 24-bit fixed point of a fraction in [0,1); exact in FP32 on the way back.
 __device__ __forceinline__ uint32_t frac_to_q24(float d)
 {

@@ -1,13 +1,14 @@
 // spectrum.cu -- fused CIC deconvolution + log-k shell binning over the
 // half-complex spectrum (the GPU counterpart of powerspectrum.c:35-111).
 //
-// Work split: one warp per (i, j) row of N/2+1 modes.  A row is walked in
+// Work split: each warp takes a contiguous block of (i, j) rows of N/2+1
+// modes (the row counter is carried incrementally).  A row is walked in
 // pieces of 32*RP modes; each piece is loaded coalesced into the warp's shared
 // buffer and then every lane takes a contiguous run of RP modes (RP odd, so the
 // strided shared reads are bank-conflict free).  Along a row |k| grows with kz,
 // so a lane's bins are non-decreasing: the lane keeps one FP32 running sum per
 // spectrum pair and flushes it (shared FP32 atomic) only when the bin changes.
-// After each row the touched bin range is promoted into the warp's FP64
+// Every 16 rows the touched bin range is promoted into the warp's FP64
 // histogram.  At the end the CTA sums its warps in a fixed order and writes one
 // FP64 partial histogram; k_bin_finalize sums the partials of all CTAs in a
 // fixed order and normalises, so results do not depend on scheduling.
@@ -41,6 +42,7 @@ struct BinParams {
 };
 
 constexpr int kBinBuf = 288;  // 32 * max RP (9) float2 per field per warp
+constexpr int kPromoteRows = 16;  // rows summed in FP32 before promotion to FP64
 
 // fv[idx] for a runtime idx without spilling fv to local memory.
 template <int NF>
@@ -105,13 +107,18 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
 
+    // Each warp takes a contiguous block of rows; (i, j) advance incrementally.
     const int64_t nrows = (int64_t)p.dims * p.dims;
     const int64_t gw = (int64_t)blockIdx.x * p.warps + wid;
     const int64_t nw = (int64_t)gridDim.x * p.warps;
+    const int64_t per = (nrows + nw - 1) / nw;
+    const int64_t r_begin = min(nrows, gw * per), r_end = min(nrows, r_begin + per);
     const int rp = p.rp;
     const int piece = 32 * rp;
-    for (int64_t r = gw; r < nrows; r += nw) {
-        const int i = (int)(r / p.dims), j = (int)(r - (int64_t)i * p.dims);
+    int i = (int)(r_begin / p.dims), j = (int)(r_begin - (int64_t)i * p.dims);
+    int bmin = nrb, bmax = -1;  // this lane's bins since the last FP64 promotion
+    int rows_since = 0;
+    for (int64_t r = r_begin; r < r_end; r++) {
         const int ki = kval_dev(i, p.dims), kj = kval_dev(j, p.dims);
         const uint32_t r2 = (uint32_t)(ki * ki + kj * kj);
         const float pxy = __ldg(iw_g + i) * __ldg(iw_g + j);
@@ -121,7 +128,6 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int q = 0; q < NP; q++)
             acc[q] = 0.f;
-        int bmin = nrb, bmax = -1;
         for (int pb = 0; pb < p.hc; pb += piece) {
             __syncwarp();
             for (int t = 0; t < rp; t++) {
@@ -189,18 +195,28 @@ __global__ void __launch_bounds__(256)
             for (int s = 0; s < NP; s++)
                 atomicAdd(&rhist[s * nrb + cb], acc[s]);
         }
-        // Promote the row's FP32 sums into the warp's FP64 histogram.
-        bmin = __reduce_min_sync(0xffffffffu, (unsigned)bmin);
-        bmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)(bmax + 1)) - 1;
-        __syncwarp();
-        for (int b = bmin + lane; b <= bmax; b += 32) {
-#pragma unroll
-            for (int s = 0; s < NP; s++) {
-                whist[s * nrb + b] += (double)rhist[s * nrb + b];
-                rhist[s * nrb + b] = 0.f;
-            }
+        if (++j == p.dims) {
+            j = 0;
+            i++;
         }
-        __syncwarp();
+        // Every kPromoteRows rows (and at the end) promote the FP32 sums of the
+        // touched bins into the warp's FP64 histogram.
+        if (++rows_since == kPromoteRows || r + 1 == r_end) {
+            rows_since = 0;
+            const int lo = (int)__reduce_min_sync(0xffffffffu, (unsigned)bmin);
+            const int hi = (int)__reduce_max_sync(0xffffffffu, (unsigned)(bmax + 1)) - 1;
+            __syncwarp();
+            for (int b = lo + lane; b <= hi; b += 32) {
+#pragma unroll
+                for (int s = 0; s < NP; s++) {
+                    whist[s * nrb + b] += (double)rhist[s * nrb + b];
+                    rhist[s * nrb + b] = 0.f;
+                }
+            }
+            __syncwarp();
+            bmin = nrb;
+            bmax = -1;
+        }
     }
     __syncthreads();
     // CTA reduction in warp order -> one partial histogram per CTA.
@@ -218,17 +234,30 @@ struct NormParams {
     double ma[kMaxBinPairs], mb[kMaxBinPairs];
 };
 
-__global__ void k_bin_finalize(const double *__restrict__ partial, int ctas, int np, int nrbins,
-                               const double *__restrict__ count, NormParams mn,
-                               double *__restrict__ power)
+// One block per (pair, bin): strided sums over the CTA partials, then a
+// fixed-order tree, so the result does not depend on scheduling.
+constexpr int kFinalizeThreads = 256;
+
+__global__ void __launch_bounds__(kFinalizeThreads)
+    k_bin_finalize(const double *__restrict__ partial, int ctas, int np, int nrbins,
+                   const double *__restrict__ count, NormParams mn, double *__restrict__ power)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= np * nrbins)
-        return;
+    __shared__ double sh[kFinalizeThreads];
+    const int k = blockIdx.x;
     const int s = k / nrbins, b = k - s * nrbins;
-    double acc = 0.0;
-    for (int c = 0; c < ctas; c++)
-        acc += partial[(size_t)c * np * nrbins + k];
+    double part = 0.0;
+    for (int c = threadIdx.x; c < ctas; c += blockDim.x)
+        part += partial[(size_t)c * np * nrbins + k];
+    sh[threadIdx.x] = part;
+    __syncthreads();
+    for (int w = kFinalizeThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0)
+        return;
+    const double acc = sh[0];
     const double cnt = count[b];
     double out = 0.0;
     if (cnt > 0.0) {
@@ -338,7 +367,7 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
         mn.mb[q] = q < l.npairs ? l.pairs[q].mass_b : 1.0;
     }
     const int k = l.npairs * t.nrbins;
-    k_bin_finalize<<<(k + 255) / 256, 256, 0, stream>>>(partial, ctas, l.npairs, t.nrbins, d.count,
+    k_bin_finalize<<<k, kFinalizeThreads, 0, stream>>>(partial, ctas, l.npairs, t.nrbins, d.count,
                                                         mn, out_power);
     (*launches)++;
     return cudaGetLastError();

@@ -382,9 +382,10 @@ def test_cross_and_multi_spectra(gp):
             rel = np.abs(p[q][ok] - ref[ok]) / np.abs(ref[ok]).max()
             # cross spectra can cross zero: compare relative to the bin scale
             assert rel.max() <= (P_RTOL if auto else 1e-5), (pr, rel.max())
-        # a single cross call after the FFTs are done re-bins without new FFTs
+        # a single cross call after the FFTs are done re-bins without new FFTs; the
+        # launch shape differs, so FP32 partial sums group differently (~1e-8)
         p01, _, _ = ctx.power(0, 1, ma, mb)
-        np.testing.assert_allclose(p01, p[pairs.index((0, 1))], rtol=1e-12)
+        np.testing.assert_allclose(p01, p[pairs.index((0, 1))], rtol=1e-6)
 
 
 def test_compat_bound_fields_route_to_device(gp):
