@@ -6,24 +6,30 @@
 // contiguous run of a few thousand particles occupies a small region of the
 // grid, and the tile sort in deposit.cu is unnecessary work.  This engine:
 //
-//   k_window_deposit  one CTA per chunk of `chunk` consecutive particles.
-//     pass A  reads the chunk and finds the periodic bounding box of its cells
-//             (cells from a plain FP32 product, which is one cell off for a few
-//             positions next to a cell face: pass B sends those, if they fall
-//             outside the box, down the global path); an axis the chunk spans
-//             completely is taken whole, with wrap-around.
-//     pass B  re-reads the chunk (from L2) and splits every position exactly
-//             (split_axis).  If the box fits the shared window the eight CIC
-//             weights go to it with shared FP32 atomics, and the window's
-//             non-zero cells are then flushed to the grid row by row with
-//             coalesced global atomic adds; otherwise every corner takes a
-//             global atomic add.  Pass B also sums the chunk's share of the
-//             exact corner mode (see deposit.cu).
+//   k_window_deposit  persistent: one CTA per SM walks chunks of kWinChunk
+//     consecutive particles (chunk b, b + gridDim, ...).  Chunks arrive in
+//     shared memory by bulk asynchronous copy (cp.async.bulk + mbarrier),
+//     double-buffered so the next chunk streams in while this one is worked.
+//     pass A  finds the periodic bounding box of the chunk's cells (cells from
+//             a plain FP32 product, one cell off for a few positions next to a
+//             cell face: pass B sends those, if they fall outside the box,
+//             down the global path); an axis the chunk spans completely is
+//             taken whole, with one extra layer for the wrapped CIC corner.
+//             Invalid particles are counted and marked (x := NaN).
+//     pass B  splits every position exactly (split_axis) and adds the eight
+//             CIC weights to the shared window as 28-bit fixed-point integers
+//             (native shared integer atomics; a signed overflow of a window
+//             cell is carried straight to the grid as +-2^32 units).  Pass B
+//             also sums the chunk's share of the exact corner mode.
+//     flush   every non-zero window cell is added to the FP32 grid (16-byte
+//             vector atomics along whole rows) and cleared, so the window is
+//             zero again for the next chunk.
 //
 // The grid is first filled with -mean (k_grid_fill / k_grid_add), the pass mean
 // computed in k_window_prep, so the result is mean-subtracted like the sorted
-// engine's.  FP32 atomics make the low bits depend on summation order; the
-// sorted engine (deposit.cu) is the exact, bit-reproducible alternative.
+// engine's.  FP32 atomics into the grid make its low bits depend on summation
+// order; the sorted engine (deposit.cu) is the exact, bit-reproducible
+// alternative.
 #include "common.cuh"
 #include "internal.h"
 
@@ -33,227 +39,483 @@ namespace genpk {
 namespace {
 
 constexpr int kWinThreads = 1024;
+constexpr int kWinChunk = 4096;               // particles per chunk
+constexpr int kWinSmemBytes = 225 * 1024;     // dynamic shared memory per CTA
+constexpr float kPosLimit = 1.0e9f;           // |pos * units| above this: invalid
 
 struct WinParams {
     const float *pos;
     const float *masses;
     int64_t n;
+    int64_t nchunks;
     int chunk;
-    int cap;     // window capacity in cells
+    int cap;      // window capacity in cells
+    int win_off;  // byte offset of the window in dynamic shared memory
     int dims;
+    float fdims, inv_dims;
     float uh, ul;
     float umass;
     int64_t plane;
     int row;
     int corner;  // accumulate the exact (N/2,N/2,N/2) mode (even grids)
+    int bulk;    // positions (and masses) 16-byte aligned: full chunks by bulk copy
 };
 
-__device__ __forceinline__ bool pos_ok(const WinParams &p, float x, float y, float z)
+// ---- bulk asynchronous copies and mbarriers (inline PTX) -------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
-    if (!finite3(x, y, z))
-        return false;
-    const float lim = 1.0e9f;
-    return !(fabsf(x * p.uh) > lim || fabsf(y * p.uh) > lim || fabsf(z * p.uh) > lim);
+    return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Cell from a plain FP32 product: exact or one cell off.
-__device__ __forceinline__ int approx_cell(float x, float uh, int dims)
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
 {
-    int c = (int)floorf(x * uh);
-    if ((unsigned)c >= (unsigned)dims) {
-        c %= dims;
-        if (c < 0)
-            c += dims;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes,
+                                          unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// Bounded wait for a phase of `bar`: false after ~2^31 clocks (about a second).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > (1ll << 31))
+            return false;
     }
-    return c;
+    return true;
 }
 
-// Signed offset of cell c from ref on a periodic axis, in [-N/2, N/2).
-__device__ __forceinline__ int periodic_offset(int c, int ref, int n)
+// Orders this thread's (and, after a barrier, the block's) generic-proxy
+// accesses of shared memory before later bulk-copy writes to it.
+__device__ __forceinline__ void fence_proxy_async()
 {
-    int o = c - ref;
-    if (o < -(n >> 1))
-        o += n;
-    if (o >= n - (n >> 1))
-        o -= n;
-    return o;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// ---- helpers ---------------------------------------------------------------
 
 __device__ __forceinline__ int wrap_once(int v, int n)
 {
     return v < 0 ? v + n : (v >= n ? v - n : v);
 }
 
-// Periodic bounding box of this thread block's approximate cell offsets:
-// reduce (lo, hi) per axis and add one cell for the CIC corner.
-__device__ __forceinline__ void block_box(int omin[3], int omax[3], const int ref[3], int dims,
-                                          int cap, int (*sh_min)[32], int (*sh_max)[32],
-                                          int *sh_box)
+// Integer-valued float cell in [0, dims) near position v along one axis; 0
+// for an invalid position.  Only needs to be close to the chunk's particles.
+__device__ __forceinline__ float ref_cell(const WinParams &p, float v)
+{
+    float r = floorf(v * p.uh);
+    r = fmaf(-p.fdims, floorf(r * p.inv_dims), r);
+    return (r >= 0.f && r < p.fdims) ? r : 0.f;
+}
+
+// 23-bit fixed point of a fraction d in [0,1): round(d * 2^23), in [0, 2^23].
+__device__ __forceinline__ unsigned frac_q23(float d)
+{
+    return (unsigned)(__float_as_int(fmaf(d, 8388608.f, 8388608.f)) - 0x4B000000);
+}
+
+struct WinBox {
+    int org[3];
+    int ext[3];  // window extent per axis (cells)
+    bool use;    // the box fits the window
+};
+
+// Block-wide periodic bounding box from the per-thread float offset ranges
+// [fmn, fmx] (offsets from ref; empty when fmn > fmx).  Two barriers.
+__device__ __forceinline__ WinBox window_box(const float fmn[3], const float fmx[3],
+                                             const float ref[3], const WinParams &p,
+                                             int (*sh_mm)[32], int *sh_box)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned bias = 1u << 30;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        omin[a] = (int)__reduce_min_sync(0xffffffffu, (unsigned)(omin[a] + (1 << 30))) - (1 << 30);
-        omax[a] = (int)__reduce_max_sync(0xffffffffu, (unsigned)(omax[a] + (1 << 30))) - (1 << 30);
+        const int lo = fmn[a] <= fmx[a] ? (int)floorf(fmaxf(fmn[a], -1.0e9f)) : (1 << 29);
+        const int hi = fmn[a] <= fmx[a] ? (int)floorf(fminf(fmx[a], 1.0e9f)) : -(1 << 29);
+        const unsigned rlo = __reduce_min_sync(0xffffffffu, (unsigned)(lo + (int)bias));
+        const unsigned rhi = __reduce_max_sync(0xffffffffu, (unsigned)(hi + (int)bias));
         if (lane == 0) {
-            sh_min[a][wid] = omin[a];
-            sh_max[a][wid] = omax[a];
+            sh_mm[a][wid] = (int)(rlo - bias);
+            sh_mm[3 + a][wid] = (int)(rhi - bias);
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        long long vol = 1;
+    if (wid == 0) {
         const int nw = blockDim.x >> 5;
+        long long vol = 1;
+#pragma unroll
         for (int a = 0; a < 3; a++) {
-            int lo = 1 << 30, hi = -(1 << 30);
-            for (int w = 0; w < nw; w++) {
-                lo = min(lo, sh_min[a][w]);
-                hi = max(hi, sh_max[a][w]);
-            }
-            int span, origin;
-            if (hi < lo) {  // no valid particle
-                span = 1;
-                origin = 0;
-            } else if (hi - lo + 2 >= dims) {  // the whole axis, wrapping
-                span = dims;
-                origin = 0;
+            const int lo = lane < nw ? sh_mm[a][lane] : (1 << 29);
+            const int hi = lane < nw ? sh_mm[3 + a][lane] : -(1 << 29);
+            const int mlo = (int)(__reduce_min_sync(0xffffffffu, (unsigned)(lo + (int)bias)) - bias);
+            const int mhi = (int)(__reduce_max_sync(0xffffffffu, (unsigned)(hi + (int)bias)) - bias);
+            int org, ext;
+            if (mhi < mlo) {  // no valid particle
+                org = 0;
+                ext = 1;
+            } else if (mhi - mlo + 2 >= p.dims) {  // the whole axis (+1 wrapped layer)
+                org = 0;
+                ext = p.dims + 1;
             } else {  // +1 for the CIC corner
-                span = hi - lo + 2;
-                origin = wrap_once(ref[a] + lo, dims);
+                org = wrap_once((int)ref[a] + mlo, p.dims);
+                ext = mhi - mlo + 2;
             }
-            sh_box[a] = origin;
-            sh_box[3 + a] = span;
-            vol *= span;
+            if (lane == 0) {
+                sh_box[a] = org;
+                sh_box[3 + a] = ext;
+            }
+            vol *= ext;
         }
-        sh_box[6] = vol <= cap ? 1 : 0;
+        if (lane == 0)
+            sh_box[6] = vol <= p.cap ? 1 : 0;
     }
     __syncthreads();
+    WinBox b;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        b.org[a] = sh_box[a];
+        b.ext[a] = sh_box[3 + a];
+    }
+    b.use = sh_box[6] != 0;
+    return b;
+}
+
+__device__ __forceinline__ int64_t chunk_first(const WinParams &p, int64_t c)
+{
+    return c * (int64_t)p.chunk;
+}
+
+__device__ __forceinline__ bool chunk_by_bulk(const WinParams &p, int64_t c)
+{
+    return p.bulk && (c + 1) * (int64_t)p.chunk <= p.n;
+}
+
+// One thread: bulk copies of chunk c into (P, M), completing on `bar`.
+template <bool VARMASS>
+__device__ __forceinline__ void issue_chunk(const WinParams &p, int64_t c, float *P, float *M,
+                                            unsigned long long *bar)
+{
+    const unsigned pb = (unsigned)p.chunk * 12u, mb = VARMASS ? (unsigned)p.chunk * 4u : 0u;
+    fence_proxy_async();
+    mbar_expect_tx(bar, pb + mb);
+    bulk_load(P, p.pos + 3 * chunk_first(p, c), pb, bar);
+    if (VARMASS)
+        bulk_load(M, p.masses + chunk_first(p, c), mb, bar);
+}
+
+// All threads: plain copy of chunk c (tail chunk, or unaligned input).
+template <bool VARMASS>
+__device__ __forceinline__ void copy_chunk(const WinParams &p, int64_t c, int cnt, float *P,
+                                           float *M)
+{
+    const float *src = p.pos + 3 * chunk_first(p, c);
+    for (int i = threadIdx.x; i < 3 * cnt; i += blockDim.x)
+        P[i] = src[i];
+    if (VARMASS) {
+        const float *ms = p.masses + chunk_first(p, c);
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+            M[i] = ms[i];
+    }
+}
+
+// Global-path adds of one particle's eight corners (cells c, weights w[k] for
+// corner k = dx | dy << 1 | dz << 2).
+__device__ __noinline__ void global_corners(const WinParams &p, float *grid, const int c[3],
+                                            const float w[8])
+{
+    const int h0 = c[0] + 1 == p.dims ? 0 : c[0] + 1;
+    const int h1 = c[1] + 1 == p.dims ? 0 : c[1] + 1;
+    const int h2 = c[2] + 1 == p.dims ? 0 : c[2] + 1;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        if (w[k] != 0.f) {
+            const int x = (k & 1) ? h0 : c[0], y = (k & 2) ? h1 : c[1], z = (k & 4) ? h2 : c[2];
+            atomicAdd(grid + cell_index(p.plane, p.row, x, y, z), w[k]);
+        }
+    }
+}
+
+// Window cells of corners in `mask` overflowed: carry `carry` (+-2^32 window
+// units, as grid units) to their grid cells.
+__device__ __noinline__ void carry_corners(const WinParams &p, float *grid, const int c[3],
+                                           unsigned mask, float carry)
+{
+    float w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        w[k] = ((mask >> k) & 1u) ? carry : 0.f;
+    global_corners(p, grid, c, w);
 }
 
 template <bool VARMASS>
-__global__ void __launch_bounds__(kWinThreads)
+__global__ void __launch_bounds__(kWinThreads, 1)
     k_window_deposit(WinParams p, DeviceStatus *st, float *__restrict__ grid)
 {
-    extern __shared__ float win[];
-    __shared__ int sh_ref[3];
-    __shared__ int sh_min[3][32], sh_max[3][32];
-    __shared__ int sh_box[7];  // origin[3], span[3], use_window
-    const int64_t b = (int64_t)blockIdx.x * p.chunk;
-    const int64_t e = min(p.n, b + (int64_t)p.chunk);
+    extern __shared__ __align__(128) unsigned char win_smem[];
+    float *pbuf = reinterpret_cast<float *>(win_smem);              // [2][chunk * 3]
+    float *mbuf = pbuf + 6 * p.chunk;                               // [2][chunk] (VARMASS)
+    int *win = reinterpret_cast<int *>(win_smem + p.win_off);       // [cap]
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int sh_mm[6][32];
+    __shared__ int sh_box[8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+
+    for (int i = threadIdx.x; i < p.cap; i += blockDim.x)
+        win[i] = 0;
     if (threadIdx.x == 0) {
-        const float x = p.pos[3 * b], y = p.pos[3 * b + 1], z = p.pos[3 * b + 2];
-        const bool ok = pos_ok(p, x, y, z);
-        sh_ref[0] = ok ? approx_cell(x, p.uh, p.dims) : 0;
-        sh_ref[1] = ok ? approx_cell(y, p.uh, p.dims) : 0;
-        sh_ref[2] = ok ? approx_cell(z, p.uh, p.dims) : 0;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        fence_proxy_async();
     }
     __syncthreads();
-    const int ref[3] = {sh_ref[0], sh_ref[1], sh_ref[2]};
 
-    // Pass A: bounding box of the approximate cells.
-    int omin[3] = {1 << 30, 1 << 30, 1 << 30}, omax[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        const float v[3] = {__ldg(p.pos + 3 * i), __ldg(p.pos + 3 * i + 1),
-                            __ldg(p.pos + 3 * i + 2)};
-        if (!pos_ok(p, v[0], v[1], v[2]))
-            continue;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const int o = periodic_offset(approx_cell(v[a], p.uh, p.dims), ref[a], p.dims);
-            omin[a] = min(omin[a], o);
-            omax[a] = max(omax[a], o);
-        }
-    }
-    block_box(omin, omax, ref, p.dims, p.cap, sh_min, sh_max, sh_box);
-    const int org[3] = {sh_box[0], sh_box[1], sh_box[2]};
-    const int span[3] = {sh_box[3], sh_box[4], sh_box[5]};
-    const bool use_window = sh_box[6] != 0;
-    const int sz = span[2], syz = span[1] * span[2];
-    if (use_window) {
-        const int vol = span[0] * syz;
-        for (int i = threadIdx.x; i < vol; i += blockDim.x)
-            win[i] = 0.f;
-        __syncthreads();
-    }
-
-    // Pass B: exact split, weights, corner-mode share.
+    // Window units: uniform mass -> 2^-28 * mass; variable -> 2^-s with
+    // s = 154 - (exponent field of the largest |mass|).
+    const unsigned mbits_max = st->max_mass_bits;
+    const int emax = VARMASS ? (int)((mbits_max >> 23) & 0xffu) : 0;
+    const float unit = VARMASS ? ldexpf(1.f, emax - 154) : p.umass * (1.f / 268435456.f);
     const float mscale = ldexpf(1.f, st->fx_shift + 4);
+    const float carry_val = 4294967296.f * unit;
+
     f2sum alt = {0.f, 0.f};
-    unsigned bad = 0;
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        const float x = __ldg(p.pos + 3 * i), y = __ldg(p.pos + 3 * i + 1),
-                    z = __ldg(p.pos + 3 * i + 2);
-        const float m = VARMASS ? __ldg(p.masses + i) : p.umass;
-        if (!pos_ok(p, x, y, z) || !isfinite(m)) {
-            bad++;
-            continue;
+    unsigned bad = 0, timeouts = 0;
+    const int64_t c0 = blockIdx.x;
+    if (threadIdx.x == 0 && c0 < p.nchunks && chunk_by_bulk(p, c0))
+        issue_chunk<VARMASS>(p, c0, pbuf, mbuf, &bar[0]);
+
+    int k = 0;
+    for (int64_t c = c0; c < p.nchunks; c += gridDim.x, k++) {
+        const int buf = k & 1;
+        float *P = pbuf + buf * 3 * p.chunk;
+        float *M = mbuf + buf * p.chunk;
+        const int cnt = (int)min((int64_t)p.chunk, p.n - chunk_first(p, c));
+        if (chunk_by_bulk(p, c)) {
+            if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
+                timeouts++;
+        } else {
+            copy_chunk<VARMASS>(p, c, cnt, P, M);
+            __syncthreads();
         }
-        const AxisSplit ax = split_axis(x, p.uh, p.ul, p.dims);
-        const AxisSplit ay = split_axis(y, p.uh, p.ul, p.dims);
-        const AxisSplit az = split_axis(z, p.uh, p.ul, p.dims);
-        if (p.corner) {
-            f2sum v = corner_factor(ax, ay, az);
-            if (VARMASS) {
-                const float mm = m * mscale;
-                const float h = __fmul_rn(v.hi, mm);
-                v = f2sum{h, fmaf(v.hi, mm, -h) + v.lo * mm};
-            }
-            if ((ax.cell + ay.cell + az.cell) & 1)
-                v = f2sum{-v.hi, -v.lo};
-            alt = f2_add2(alt, v);
-        }
-        const float tx = 1.f - ax.frac, ty = 1.f - ay.frac, tz = 1.f - az.frac;
-        // Weight order follows fieldize.cpp:77-84: ((m*wx)*wy)*wz.
-        const float mtx = m * tx, mdx = m * ax.frac;
-        const float a00 = mtx * ty, a10 = mdx * ty, a01 = mtx * ay.frac, a11 = mdx * ay.frac;
-        int w0[3], w1[3];
-        bool inwin = use_window;
-        if (use_window) {
-            const int c[3] = {ax.cell, ay.cell, az.cell};
+
+        // Pass A: float offsets of the approximate cells from the chunk's
+        // first particle, periodic-wrapped into [-N/2, N/2].
+        const float ref[3] = {ref_cell(p, P[0]), ref_cell(p, P[1]), ref_cell(p, P[2])};
+        float fmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, fmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+            float f[3];
+            bool ok = true;
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                int o = c[a] - org[a];
-                if (o < 0)
-                    o += p.dims;
-                w0[a] = o;
-                if (span[a] == p.dims) {
-                    // whole (wrapping) axis: the +1 corner wraps inside the window
-                    w1[a] = o + 1 == p.dims ? 0 : o + 1;
-                } else {
-                    w1[a] = o + 1;
-                    // The box came from approximate cells (a plain FP32 product
-                    // is one cell off for ~1e-4 of positions near a cell face):
-                    // a particle whose exact cell falls outside the window takes
-                    // the global path.
-                    inwin = inwin && (o + 1 < span[a]);
+                f[a] = fmaf(P[3 * j + a], p.uh, -ref[a]);
+                ok = ok && fabsf(f[a]) <= kPosLimit;
+            }
+            if (VARMASS)
+                ok = ok && fabsf(M[j]) <= 3.4028235e38f;
+            if (!ok) {
+                P[3 * j] = __int_as_float(0x7fffffff);
+                fence_proxy_async();  // before a later bulk copy into this buffer
+                bad++;
+                continue;
+            }
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const float w = fmaf(-p.fdims, rintf(f[a] * p.inv_dims), f[a]);
+                fmn[a] = fminf(fmn[a], w);
+                fmx[a] = fmaxf(fmx[a], w);
+            }
+        }
+        // Prefetch the chunk after this one into the other buffer (its last
+        // reader, pass B of the previous chunk, finished before the previous
+        // flush's barrier).
+        if (threadIdx.x == 0 && c + gridDim.x < p.nchunks && chunk_by_bulk(p, c + gridDim.x))
+            issue_chunk<VARMASS>(p, c + gridDim.x, pbuf + (buf ^ 1) * 3 * p.chunk,
+                                 mbuf + (buf ^ 1) * p.chunk, &bar[buf ^ 1]);
+        const WinBox box = window_box(fmn, fmx, ref, p, sh_mm, sh_box);
+        const int e0 = box.ext[0] - 1, e1 = box.ext[1] - 1, e2 = box.ext[2] - 1;
+        const int DY = box.ext[2], DX = box.ext[1] * box.ext[2];
+
+        // Pass B: exact split, fixed-point weights, corner-mode share.
+        for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+            const float x = P[3 * j], y = P[3 * j + 1], z = P[3 * j + 2];
+            if (isnan(x))
+                continue;
+            float m = p.umass;
+            unsigned mant7 = 0u;
+            int dsh = 0;
+            bool neg = false;
+            if (VARMASS) {
+                m = M[j];
+                const unsigned mb = __float_as_uint(m);
+                const int ef = (int)((mb >> 23) & 0xffu);
+                dsh = emax - ef;
+                if (ef == 0 || dsh > 30)  // zero, subnormal or below 2^-30 of the largest
+                    continue;
+                mant7 = ((mb & 0x7fffffu) | 0x800000u) << 7;
+                neg = (mb >> 31) != 0u;
+            }
+            const AxisSplit ax = split_axis(x, p.uh, p.ul, p.dims);
+            const AxisSplit ay = split_axis(y, p.uh, p.ul, p.dims);
+            const AxisSplit az = split_axis(z, p.uh, p.ul, p.dims);
+            if (p.corner) {
+                f2sum v = corner_factor(ax, ay, az);
+                if (VARMASS) {
+                    const float mm = m * mscale;
+                    const float h = __fmul_rn(v.hi, mm);
+                    v = f2sum{h, fmaf(v.hi, mm, -h) + v.lo * mm};
+                }
+                if ((ax.cell + ay.cell + az.cell) & 1)
+                    v = f2sum{-v.hi, -v.lo};
+                alt = f2_add2(alt, v);
+            }
+            // Weights: per-axis factors r = 2^23 - q (lower cell) and q (upper)
+            // from 23-bit fractions; pair products a = rx*ry / 2^16 (<= 2^30,
+            // times mant / 2^24 >> dsh for variable masses); corner weight
+            // a * rz / 2^25 (<= 2^28).
+            const unsigned qx = frac_q23(ax.frac), qy = frac_q23(ay.frac), qz = frac_q23(az.frac);
+            const unsigned rx = 0x800000u - qx, ry = 0x800000u - qy, rz = 0x800000u - qz;
+            unsigned a00 = __umulhi(rx << 8, ry << 8), a10 = __umulhi(qx << 8, ry << 8);
+            unsigned a01 = __umulhi(rx << 8, qy << 8), a11 = __umulhi(qx << 8, qy << 8);
+            if (VARMASS) {
+                a00 = __umulhi(a00 << 1, mant7) >> dsh;
+                a10 = __umulhi(a10 << 1, mant7) >> dsh;
+                a01 = __umulhi(a01 << 1, mant7) >> dsh;
+                a11 = __umulhi(a11 << 1, mant7) >> dsh;
+            }
+            const unsigned cz0 = rz << 7, cz1 = qz << 7;
+            unsigned w[8] = {__umulhi(a00, cz0), __umulhi(a10, cz0), __umulhi(a01, cz0),
+                             __umulhi(a11, cz0), __umulhi(a00, cz1), __umulhi(a10, cz1),
+                             __umulhi(a01, cz1), __umulhi(a11, cz1)};
+            const int cell[3] = {ax.cell, ay.cell, az.cell};
+            int o0 = ax.cell - box.org[0], o1 = ay.cell - box.org[1], o2 = az.cell - box.org[2];
+            o0 += o0 < 0 ? p.dims : 0;
+            o1 += o1 < 0 ? p.dims : 0;
+            o2 += o2 < 0 ? p.dims : 0;
+            if (box.use && o0 < e0 && o1 < e1 && o2 < e2) {
+                int *wp = win + (o0 * box.ext[1] + o1) * DY + o2;
+                const int off[8] = {0, DX, DY, DX + DY, 1, DX + 1, DY + 1, DX + DY + 1};
+                unsigned ovf = 0u;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int sw = neg ? -(int)w[q] : (int)w[q];
+                    const int old = atomicAdd(wp + off[q], sw);
+                    const int nw = (int)((unsigned)old + (unsigned)sw);
+                    ovf |= (unsigned)(neg ? nw > old : nw < old) << q;
+                }
+                if (ovf)
+                    carry_corners(p, grid, cell, ovf, neg ? -carry_val : carry_val);
+            } else {
+                float wf[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    wf[q] = (neg ? -(float)w[q] : (float)w[q]) * unit;
+                global_corners(p, grid, cell, wf);
+            }
+        }
+        __syncthreads();
+
+        // Flush and clear: one warp per window row, lanes along z.
+        if (box.use) {
+            const int nrows = box.ext[0] * box.ext[1];
+            const bool whole_z = box.ext[2] == p.dims + 1 && p.dims >= 8;
+            for (int r = wid; r < nrows; r += nwarps) {
+                const int wx = r / box.ext[1];
+                const int wy = r - wx * box.ext[1];
+                const int gx = wrap_once(box.org[0] + wx, p.dims);
+                const int gy = wrap_once(box.org[1] + wy, p.dims);
+                float *grow = grid + (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
+                int *wrow = win + (size_t)r * DY;
+                if (whole_z) {
+                    // [zv, zend) as float4; the (at most 3 + 3) cells either
+                    // side and the wrapped layer z = N (-> 0) one by one.
+                    const int zv = (int)(((16u - ((unsigned)(uintptr_t)grow & 15u)) & 15u) >> 2);
+                    const int zend = zv + ((p.dims - zv) & ~3);
+                    for (int z = zv + 4 * lane; z < zend; z += 128) {
+                        const int v0 = wrow[z], v1 = wrow[z + 1], v2 = wrow[z + 2],
+                                  v3 = wrow[z + 3];
+                        if ((v0 | v1 | v2 | v3) != 0) {
+                            wrow[z] = 0;
+                            wrow[z + 1] = 0;
+                            wrow[z + 2] = 0;
+                            wrow[z + 3] = 0;
+                            atomicAdd((float4 *)(grow + z),
+                                      make_float4((float)v0 * unit, (float)v1 * unit,
+                                                  (float)v2 * unit, (float)v3 * unit));
+                        }
+                    }
+                    int ze = -1, zg = 0;
+                    if (lane < zv) {
+                        ze = lane;
+                        zg = lane;
+                    } else if (lane - zv < p.dims - zend) {
+                        ze = zend + lane - zv;
+                        zg = ze;
+                    } else if (lane == 31) {
+                        ze = p.dims;
+                        zg = 0;
+                    }
+                    if (ze >= 0) {
+                        const int v = wrow[ze];
+                        if (v != 0) {
+                            wrow[ze] = 0;
+                            atomicAdd(grow + zg, (float)v * unit);
+                        }
+                    }
+                    continue;
+                }
+                for (int z = lane; z < box.ext[2]; z += 32) {
+                    const int v = wrow[z];
+                    if (v != 0) {
+                        wrow[z] = 0;
+                        int gz = box.org[2] + z;
+                        gz -= gz >= p.dims ? p.dims : 0;
+                        atomicAdd(grow + gz, (float)v * unit);
+                    }
                 }
             }
         }
-        if (inwin) {
-            const int x0 = w0[0] * syz, x1 = w1[0] * syz, y0 = w0[1] * sz, y1 = w1[1] * sz;
-            atomicAdd(&win[x0 + y0 + w0[2]], a00 * tz);
-            atomicAdd(&win[x1 + y0 + w0[2]], a10 * tz);
-            atomicAdd(&win[x0 + y1 + w0[2]], a01 * tz);
-            atomicAdd(&win[x1 + y1 + w0[2]], a11 * tz);
-            atomicAdd(&win[x0 + y0 + w1[2]], a00 * az.frac);
-            atomicAdd(&win[x1 + y0 + w1[2]], a10 * az.frac);
-            atomicAdd(&win[x0 + y1 + w1[2]], a01 * az.frac);
-            atomicAdd(&win[x1 + y1 + w1[2]], a11 * az.frac);
-        } else {
-            const int cx = ax.cell, cy = ay.cell, cz = az.cell;
-            const int hx = cx + 1 == p.dims ? 0 : cx + 1, hy = cy + 1 == p.dims ? 0 : cy + 1,
-                      hz = cz + 1 == p.dims ? 0 : cz + 1;
-            atomicAdd(grid + cell_index(p.plane, p.row, cx, cy, cz), a00 * tz);
-            atomicAdd(grid + cell_index(p.plane, p.row, hx, cy, cz), a10 * tz);
-            atomicAdd(grid + cell_index(p.plane, p.row, cx, hy, cz), a01 * tz);
-            atomicAdd(grid + cell_index(p.plane, p.row, hx, hy, cz), a11 * tz);
-            atomicAdd(grid + cell_index(p.plane, p.row, cx, cy, hz), a00 * az.frac);
-            atomicAdd(grid + cell_index(p.plane, p.row, hx, cy, hz), a10 * az.frac);
-            atomicAdd(grid + cell_index(p.plane, p.row, cx, hy, hz), a01 * az.frac);
-            atomicAdd(grid + cell_index(p.plane, p.row, hx, hy, hz), a11 * az.frac);
-        }
+        // The next chunk's window writes come after the two barriers of its
+        // window_box, so the flush needs no barrier of its own.
     }
+
     if (p.corner) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -267,55 +529,17 @@ __global__ void __launch_bounds__(kWinThreads)
                 const float h = __fmul_rn(alt.hi, mm);
                 alt = f2sum{h, fmaf(alt.hi, mm, -h) + alt.lo * mm};
             }
-            const long long w = __float2ll_rn(alt.hi) + __float2ll_rn(alt.lo);
-            if (w != 0)
-                atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)w);
+            const long long v = __float2ll_rn(alt.hi) + __float2ll_rn(alt.lo);
+            if (v != 0)
+                atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
         }
     }
     bad = __reduce_add_sync(0xffffffffu, bad);
+    timeouts = __reduce_add_sync(0xffffffffu, timeouts);
     if (lane == 0 && bad)
         atomicAdd(&st->bad_particles, (unsigned long long)bad);
-    if (!use_window)
-        return;
-    __syncthreads();
-    // Flush: one warp per window row (one division per row), lanes along z.
-    // Whole rows (the window spans all of z) go out as 16-byte vector atomics
-    // from the first 16-byte-aligned cell on; everything else cell by cell.
-    const int nrows = span[0] * span[1];
-    const int nwarps = blockDim.x >> 5;
-    const bool whole_z = span[2] == p.dims && p.dims >= 8;
-    for (int r = wid; r < nrows; r += nwarps) {
-        const int wx = r / span[1];
-        const int wy = r - wx * span[1];
-        const int gx = wrap_once(org[0] + wx, p.dims), gy = wrap_once(org[1] + wy, p.dims);
-        float *grow = grid + (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
-        const float *wrow = win + (size_t)r * sz;
-        if (whole_z) {
-            // [zv, zend) as float4; the (at most 3 + 3) cells either side scalar
-            const int zv = (int)(((16u - ((unsigned)(uintptr_t)grow & 15u)) & 15u) >> 2);
-            const int zend = zv + ((p.dims - zv) & ~3);
-            for (int z = zv + 4 * lane; z < zend; z += 128) {
-                const float4 v = make_float4(wrow[z], wrow[z + 1], wrow[z + 2], wrow[z + 3]);
-                if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
-                    atomicAdd((float4 *)(grow + z), v);
-            }
-            const int ze = lane < zv ? lane : zend + lane - zv;
-            if (ze < p.dims && (lane < zv || lane - zv < p.dims - zend)) {
-                const float v = wrow[ze];
-                if (v != 0.f)
-                    atomicAdd(grow + ze, v);
-            }
-            continue;
-        }
-        for (int z = lane; z < sz; z += 32) {
-            const float v = wrow[z];
-            if (v != 0.f) {
-                int gz = org[2] + z;
-                gz -= gz >= p.dims ? p.dims : 0;
-                atomicAdd(grow + gz, v);
-            }
-        }
-    }
+    if (lane == 0 && timeouts)
+        atomicAdd(&st->timeouts, (unsigned long long)timeouts);
 }
 
 // Per-CTA FP64 mass partials (Kahan in FP32 first) and the max |mass|.
@@ -421,90 +645,90 @@ __global__ void k_window_finish(const DeviceStatus *__restrict__ st, double *fie
     *field_corner += ldexp((double)st->alt_sum, -(st->fx_shift + 4));
 }
 
-// Probe: for up to `samples` evenly spread chunks, the box volume in cells
-// (computed as pass A of k_window_deposit does).
+// Probe: for up to `samples` evenly spread chunks, the window volume in cells
+// (the box k_window_deposit's pass A computes for that chunk).
 __global__ void __launch_bounds__(256)
-    k_window_probe(WinParams p, int samples, int64_t nchunks, long long *__restrict__ vol_out)
+    k_window_probe(WinParams p, int samples, long long *__restrict__ vol_out)
 {
-    const int s = blockIdx.x;
-    const int64_t chunk_id = (int64_t)s * nchunks / samples;
-    const int64_t b = chunk_id * p.chunk;
-    const int64_t e = min(p.n, b + (int64_t)p.chunk);
-    __shared__ int sh_ref[3];
-    __shared__ int sh_min[3][32], sh_max[3][32];
-    __shared__ int sh_box[7];
-    if (threadIdx.x == 0) {
-        const float x = p.pos[3 * b], y = p.pos[3 * b + 1], z = p.pos[3 * b + 2];
-        const bool ok = pos_ok(p, x, y, z);
-        sh_ref[0] = ok ? approx_cell(x, p.uh, p.dims) : 0;
-        sh_ref[1] = ok ? approx_cell(y, p.uh, p.dims) : 0;
-        sh_ref[2] = ok ? approx_cell(z, p.uh, p.dims) : 0;
-    }
-    __syncthreads();
-    const int ref[3] = {sh_ref[0], sh_ref[1], sh_ref[2]};
-    int omin[3] = {1 << 30, 1 << 30, 1 << 30}, omax[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        const float v[3] = {p.pos[3 * i], p.pos[3 * i + 1], p.pos[3 * i + 2]};
-        if (!pos_ok(p, v[0], v[1], v[2]))
+    __shared__ int sh_mm[6][32];
+    __shared__ int sh_box[8];
+    const int64_t c = (int64_t)blockIdx.x * p.nchunks / samples;
+    const float *P = p.pos + 3 * chunk_first(p, c);
+    const int cnt = (int)min((int64_t)p.chunk, p.n - chunk_first(p, c));
+    const float ref[3] = {ref_cell(p, P[0]), ref_cell(p, P[1]), ref_cell(p, P[2])};
+    float fmn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, fmx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+        float f[3];
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            f[a] = fmaf(P[3 * j + a], p.uh, -ref[a]);
+            ok = ok && fabsf(f[a]) <= kPosLimit;
+        }
+        if (!ok)
             continue;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const int o = periodic_offset(approx_cell(v[a], p.uh, p.dims), ref[a], p.dims);
-            omin[a] = min(omin[a], o);
-            omax[a] = max(omax[a], o);
+            const float w = fmaf(-p.fdims, rintf(f[a] * p.inv_dims), f[a]);
+            fmn[a] = fminf(fmn[a], w);
+            fmx[a] = fmaxf(fmx[a], w);
         }
     }
-    block_box(omin, omax, ref, p.dims, p.cap, sh_min, sh_max, sh_box);
+    const WinBox box = window_box(fmn, fmx, ref, p, sh_mm, sh_box);
     if (threadIdx.x == 0)
-        vol_out[s] = (long long)sh_box[3] * sh_box[4] * sh_box[5];
+        vol_out[blockIdx.x] = (long long)box.ext[0] * box.ext[1] * box.ext[2];
 }
 
-WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk, int cap)
+WinParams make_win_params(const DepositGeom &g, const DepositArgs &a)
 {
     WinParams p;
+    const bool var = a.masses != nullptr;
     p.pos = a.pos;
     p.masses = a.masses;
     p.n = a.n;
-    p.chunk = chunk;
-    p.cap = cap;
+    p.chunk = kWinChunk;
+    p.nchunks = (a.n + kWinChunk - 1) / kWinChunk;
+    p.win_off = kWinChunk * (var ? 32 : 24);
+    p.cap = window_cap_cells(var);
     p.dims = g.grid.dims;
+    p.fdims = (float)g.grid.dims;
+    p.inv_dims = 1.f / (float)g.grid.dims;
     p.uh = g.units_hi;
     p.ul = g.units_lo;
     p.umass = a.mass;
     p.plane = g.grid.plane;
     p.row = g.grid.row;
     p.corner = (g.grid.dims % 2 == 0) ? 1 : 0;
+    p.bulk = ((uintptr_t)a.pos % 16 == 0 && (!var || (uintptr_t)a.masses % 16 == 0)) ? 1 : 0;
     return p;
 }
 
 }  // namespace
 
-// Chunk length: small enough that a lattice-ordered chunk (rows of dims
-// particles) covers well under half of the grid along any axis, large enough
-// that a window is reused by many particles.
-int window_chunk(int dims)
+int window_chunk(int)
 {
-    if (dims > 512)
-        return 4096;
-    const int64_t quarter_plane = (int64_t)dims * dims / 8;
-    return (int)std::max<int64_t>(1024, std::min<int64_t>(8192, quarter_plane));
+    return kWinChunk;
+}
+
+int window_cap_cells(bool variable_masses)
+{
+    return (kWinSmemBytes - kWinChunk * (variable_masses ? 32 : 24)) / 4;
 }
 
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,
                          int samples, cudaStream_t stream, int64_t *launches)
 {
-    const int chunk = window_chunk(g.grid.dims);
-    const WinParams p = make_win_params(g, a, chunk, kWindowCapCells);
-    const int64_t nchunks = (a.n + chunk - 1) / chunk;
-    const int s = (int)std::min<int64_t>(samples, nchunks);
-    k_window_probe<<<s, 256, 0, stream>>>(p, s, nchunks, vol_dev);
+    const WinParams p = make_win_params(g, a);
+    const int s = (int)std::min<int64_t>(samples, p.nchunks);
+    k_window_probe<<<s, 256, 0, stream>>>(p, s, vol_dev);
     (*launches)++;
     return cudaGetLastError();
 }
 
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, double *mass_part,
-                                int mass_ctas, DeviceStatus *dstat, cudaStream_t stream,
-                                int64_t *launches, StageHook hook, void *hook_user)
+                                int mass_ctas, int num_sms, DeviceStatus *dstat,
+                                cudaStream_t stream, int64_t *launches, StageHook hook,
+                                void *hook_user)
 {
     auto mark = [&](const char *name) {
         (*launches)++;
@@ -533,27 +757,19 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, doub
     mark("win_fill");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    const int chunk = window_chunk(g.grid.dims);
-    const WinParams p = make_win_params(g, a, chunk, kWindowCapCells);
-    const int64_t nchunks = (a.n + chunk - 1) / chunk;
-    const size_t smem = sizeof(float) * (size_t)kWindowCapCells;
-    if (a.masses) {
-        if ((err = cudaFuncSetAttribute(k_window_deposit<true>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
+    const WinParams p = make_win_params(g, a);
+    if (p.nchunks > 0) {
+        const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
+        const int smem = p.win_off + 4 * p.cap;
+        auto kern = a.masses ? k_window_deposit<true> : k_window_deposit<false>;
+        if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        smem)) != cudaSuccess)
             return err;
-        k_window_deposit<true><<<(unsigned)nchunks, kWinThreads, smem, stream>>>(p, dstat, a.grid);
-    } else {
-        if ((err = cudaFuncSetAttribute(k_window_deposit<false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
+        kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, a.grid);
+        mark("win_deposit");
+        if ((err = cudaGetLastError()) != cudaSuccess)
             return err;
-        k_window_deposit<false><<<(unsigned)nchunks, kWinThreads, smem, stream>>>(p, dstat,
-                                                                                a.grid);
     }
-    mark("win_deposit");
-    if ((err = cudaGetLastError()) != cudaSuccess)
-        return err;
     k_window_finish<<<1, 1, 0, stream>>>(dstat, a.field_corner);
     (*launches)++;
     return cudaGetLastError();

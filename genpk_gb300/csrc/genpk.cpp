@@ -280,7 +280,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
             GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
             int fit = 0;
             for (int i = 0; i < got; i++)
-                fit += vol[i] <= (long long)(0.9 * kWindowCapCells) ? 1 : 0;
+                fit += vol[i] <= (long long)(0.9 * window_cap_cells(masses != nullptr)) ? 1 : 0;
             if (got > 0 && fit * 10 >= got * 9)
                 engine = GENPK_ENGINE_WINDOW;
         }
@@ -292,8 +292,8 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         size_t mp = (size_t)s.mass_part_cap;
         GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)mass_ctas));
         s.mass_part_cap = (int)mp;
-        GENPK_CUDA(deposit_window_pass(g, a, s.mass_part, mass_ctas, ctx->d_status, ctx->stream,
-                                       &ctx->launches, hook, ctx));
+        GENPK_CUDA(deposit_window_pass(g, a, s.mass_part, mass_ctas, ctx->num_sms,
+                                       ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
     } else {
         const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
         if (deposit_shared_hist(g)) {

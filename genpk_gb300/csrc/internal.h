@@ -107,15 +107,16 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
                          int64_t *launches, StageHook hook, void *hook_user);
 
 // Window engine (deposit_window.cu) for spatially coherent particle order.
-constexpr int kWindowCapCells = 53248;  // shared window: 208 KB of FP32 cells
-int window_chunk(int dims);             // particles per CTA chunk
+int window_chunk(int dims);                   // particles per chunk
+int window_cap_cells(bool variable_masses);  // shared window capacity in cells
 // Box volume (cells) of `samples` evenly spread chunks, written to vol_dev.
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,
                          int samples, cudaStream_t stream, int64_t *launches);
 // One window-engine pass; mass_part needs mass_ctas doubles (variable masses).
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, double *mass_part,
-                                int mass_ctas, DeviceStatus *dstat, cudaStream_t stream,
-                                int64_t *launches, StageHook hook, void *hook_user);
+                                int mass_ctas, int num_sms, DeviceStatus *dstat,
+                                cudaStream_t stream, int64_t *launches, StageHook hook,
+                                void *hook_user);
 
 // ---------------------------------------------------------------------------
 // Binning (deconvolution + log-k shells)

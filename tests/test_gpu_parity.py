@@ -223,6 +223,68 @@ def test_window_engine_matches_oracle(gp, var):
     bins_close(p, pr, c)
 
 
+@pytest.mark.parametrize("case", ["unaligned_tail", "dense_carry", "negative_mass_carry",
+                                  "tiny_grid", "grid_8"])
+def test_window_engine_edge_cases(gp, case):
+    """Window-engine paths the lattice case does not reach: an input pointer
+    that is not 16-byte aligned (chunks copied by threads, not bulk copies) with
+    a partial last chunk; window cells whose 32-bit fixed-point sum overflows
+    (carried to the grid), for positive and negative masses; grids so small
+    that every axis is taken whole with the wrapped extra layer."""
+    import torch
+    from genpk_gb300 import synth
+    rng = np.random.default_rng(11)
+    masses, mass = None, 1.0
+    if case == "unaligned_tail":
+        dims, box = 64, 1000.0
+        full = synth.zeldovich(64, box, seed=12)[: 3 * 4096 + 1235]
+        pos = full[1:]
+        dev = torch.from_numpy(full).cuda()[1:]
+        assert dev.data_ptr() % 16 != 0
+    elif case in ("dense_carry", "negative_mass_carry"):
+        dims, box = 16, 16.0
+        lat = synth.zeldovich(16, box, seed=13)
+        clump = (np.array([3.0, 4.0, 5.0]) + rng.random((9000, 3)) * 0.5).astype(np.float32)
+        pos = np.concatenate([lat, clump, lat]).astype(np.float32)
+        if case == "negative_mass_carry":
+            masses = rng.uniform(-1.0, 1.0, len(pos)).astype(np.float32)
+            masses[len(lat): len(lat) + 9000] = -rng.uniform(0.5, 1.0, 9000)
+            mass = 0.0
+        dev = torch.from_numpy(pos).cuda()
+    else:
+        dims = 6 if case == "tiny_grid" else 8
+        box = 3.0
+        pos = (rng.random((50000, 3)) * box).astype(np.float32)
+        pos = pos[np.lexsort((pos[:, 2], pos[:, 1], pos[:, 0]))]
+        dev = torch.from_numpy(pos).cuda()
+    ref = O.deposit(pos, box, dims, masses, mass)
+    with gp.Context(dims, 8) as ctx:
+        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.deposit(0, box, dev, None if masses is None else torch.from_numpy(masses).cuda(), mass)
+        ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        grid_close(ctx.read_field(0), ref, tol=1e-6)
+
+
+def test_window_engine_reports_non_finite(gp):
+    from genpk_gb300 import synth
+    dims, box = 32, 100.0
+    pos = synth.zeldovich(32, box, seed=14)
+    bad = pos.copy()
+    bad[5, 2] = np.nan
+    bad[9000, 0] = -np.inf
+    keep = np.ones(len(pos), bool)
+    keep[[5, 9000]] = False
+    with gp.Context(dims, 8) as ctx:
+        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.deposit(0, box, bad, None, 1.0)
+        with pytest.raises(gp.GenPKError) as e:
+            ctx.sync()
+        assert e.value.status == 5
+        g = ctx.read_field(0)
+    grid_close(g, O.deposit(pos[keep], box, dims, None, 1.0), tol=1e-6)
+
+
 def test_window_engine_direct_fallback_on_random_order(gp):
     """Randomly ordered particles: no chunk fits a window, every corner takes a
     global atomic.  Still correct."""
