@@ -432,16 +432,26 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             if (box.use && o0 < e0 && o1 < e1 && o2 < e2) {
                 int *wp = win + (o0 * box.ext[1] + o1) * DY + o2;
                 const int off[8] = {0, DX, DY, DX + DY, 1, DX + 1, DY + 1, DX + DY + 1};
-                unsigned ovf = 0u;
+                int old[8];
+                unsigned any = 0u;
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
-                    const int sw = neg ? -(int)w[q] : (int)w[q];
-                    const int old = atomicAdd(wp + off[q], sw);
-                    const int nw = (int)((unsigned)old + (unsigned)sw);
-                    ovf |= (unsigned)(neg ? nw > old : nw < old) << q;
+                    old[q] = atomicAdd(wp + off[q], neg ? -(int)w[q] : (int)w[q]);
+                    any |= (unsigned)old[q];
                 }
-                if (ovf)
-                    carry_corners(p, grid, cell, ovf, neg ? -carry_val : carry_val);
+                // An add of |w| <= 2^28 can only overflow a cell that held at
+                // least 2^31 - 2^28 or a negative value: test exactly only then.
+                if (any >= 0x70000000u) {
+                    unsigned ovf = 0u;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const int sw = neg ? -(int)w[q] : (int)w[q];
+                        const int nw = (int)((unsigned)old[q] + (unsigned)sw);
+                        ovf |= (unsigned)(neg ? nw > old[q] : nw < old[q]) << q;
+                    }
+                    if (ovf)
+                        carry_corners(p, grid, cell, ovf, neg ? -carry_val : carry_val);
+                }
             } else {
                 float wf[8];
 #pragma unroll

@@ -504,7 +504,7 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
             for (int e = 0; e < 2; e++) {
                 const float2 *fp = (const float2 *)grid_of(ctx, pairs[2 * q + e]);
                 slot[e] = -1;
-                for (int k = 0; k < l.nfields; k++)
+                for (int k = 0; k < l.nfields + added; k++)
                     if (l.fields[k] == fp)
                         slot[e] = k;
                 if (slot[e] < 0) {

@@ -2,16 +2,17 @@
 // half-complex spectrum (the GPU counterpart of powerspectrum.c:35-111).
 //
 // Work split: each warp takes a contiguous block of (i, j) rows of N/2+1
-// modes (the row counter is carried incrementally).  A row is walked in
-// pieces of 32*RP modes; each piece is loaded coalesced into the warp's shared
-// buffer and then every lane takes a contiguous run of RP modes (RP odd, so the
-// strided shared reads are bank-conflict free).  Along a row |k| grows with kz,
-// so a lane's bins are non-decreasing: the lane keeps one FP32 running sum per
-// spectrum pair and flushes it (shared FP32 atomic) only when the bin changes.
-// Every 16 rows the touched bin range is promoted into the warp's FP64
-// histogram.  At the end the CTA sums its warps in a fixed order and writes one
-// FP64 partial histogram; k_bin_finalize sums the partials of all CTAs in a
-// fixed order and normalises, so results do not depend on scheduling.
+// modes, walked in pieces of 32*RP modes with the next piece's loads in
+// flight.  Every lane bins a contiguous run of RP modes; bins only grow along a
+// run, so a lane keeps one FP32 running sum per spectrum pair and compares
+// |k|^2 with the next threshold held in a register.  The lanes' open sums are
+// combined at the end of a piece by a segmented warp scan over their bins (no
+// atomics); a bin completed inside a run (only where bins are narrower than a
+// run) goes to the warp's FP32 histogram with a shared atomic.  Every 16 rows
+// the touched bins are promoted into the warp's FP64 histogram.  At the end
+// the CTA sums its warps in a fixed order and writes one FP64 partial
+// histogram; k_bin_finalize sums the partials of all CTAs in a fixed order and
+// normalises, so results do not depend on scheduling.
 //
 // Per mode (powerspectrum.c:55-91): bin = max{b : thr[b] <= |k|^2} with the
 // integer thresholds built on the host from the reference's own bin
@@ -41,7 +42,6 @@ struct BinParams {
     int warps;       // warps per CTA
 };
 
-constexpr int kBinBuf = 288;  // 32 * max RP (9) float2 per field per warp
 constexpr int kPromoteRows = 16;  // rows summed in FP32 before promotion to FP64
 
 // fv[idx] for a runtime idx without spilling fv to local memory.
@@ -74,9 +74,95 @@ __device__ __forceinline__ int bin_lookup(uint32_t kk2, const uint32_t *thr, int
     return b;
 }
 
-// Shared layout (bytes):
-//   thr  [nrbins+1] u32 | iw [hc] f32 | per warp: whist [NP][nrbins] f64,
-//   rhist [NP][nrbins] f32, buf [NF][kBinBuf] float2
+// Shared layout (bytes, each block 16-byte aligned):
+//   thr [nrbins+1] u32 | izc [hc] float2 {iw(kz), mode weight 1 or 2} |
+//   per warp: whist [NP][nrbins] f64, rhist [NP][nrbins] f32, buf [NF][32*RP] float2
+struct BinLayout {
+    size_t izc, warps, whist, rhist, buf, per_warp;
+};
+
+__host__ __device__ inline size_t align16(size_t v)
+{
+    return (v + 15) & ~(size_t)15;
+}
+
+__host__ __device__ inline BinLayout bin_layout(int nrbins, int hc, int np, int nf, int rp)
+{
+    BinLayout L;
+    L.izc = align16(sizeof(uint32_t) * (nrbins + 1));
+    L.warps = L.izc + align16(sizeof(float2) * hc);
+    L.whist = 0;
+    L.rhist = align16(sizeof(double) * np * nrbins);
+    L.buf = L.rhist + align16(sizeof(float) * np * nrbins);
+    L.per_warp = L.buf + sizeof(float2) * nf * 32 * rp;
+    return L;
+}
+
+constexpr int kMaxRP = 9;
+
+// One piece of a row: 32*RP consecutive modes from kz = pb, field values into
+// registers (coalesced loads; zero past the row's end).
+template <int NF>
+__device__ __forceinline__ void load_piece(const BinParams &p, int64_t r, int pb, int lane,
+                                           float2 (&v)[NF][kMaxRP])
+{
+    const size_t rowoff = (size_t)r * p.hc;
+#pragma unroll
+    for (int t = 0; t < kMaxRP; t++) {
+        const int m = pb + t * 32 + lane;
+        const bool in = t < p.rp && m < p.hc;
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            v[f][t] = in ? __ldg(p.f[f] + rowoff + m) : make_float2(0.f, 0.f);
+    }
+}
+
+// Registers -> the warp's staging buffer, with the two special modes fixed:
+// (0,0,0) is skipped (zeroed) and the exact corner value replaces the
+// transform's (N/2,N/2,N/2) mode.
+template <int NF>
+__device__ __forceinline__ void stage_piece(const BinParams &p, int64_t r, int pb, int lane,
+                                            float2 (&v)[NF][kMaxRP], float2 *buf, int piece)
+{
+    if (r == 0 && pb == 0 && lane == 0) {
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            v[f][0] = make_float2(0.f, 0.f);
+    }
+    if (r == p.corner_row) {
+#pragma unroll
+        for (int t = 0; t < kMaxRP; t++) {
+            if (pb + t * 32 + lane == p.half) {
+#pragma unroll
+                for (int f = 0; f < NF; f++)
+                    if (p.corner[f])
+                        v[f][t] = make_float2((float)*p.corner[f], 0.f);
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < kMaxRP; t++) {
+        if (t < p.rp) {
+#pragma unroll
+            for (int f = 0; f < NF; f++)
+                buf[f * piece + t * 32 + lane] = v[f][t];
+        }
+    }
+    __syncwarp();
+}
+
+// Work split: each warp takes a contiguous block of (i, j) rows; a row is
+// walked in pieces of 32*RP modes, the next piece's loads in flight while the
+// current one is binned.  Lane l bins the contiguous run [l*RP, (l+1)*RP) of a
+// piece (RP odd: conflict-free strided shared reads) with a running FP32 sum
+// per spectrum pair.  Along a run |k|^2 grows, so the bin only moves up: the
+// next threshold is kept in a register and a completed bin inside a run is
+// added to the warp's FP32 histogram with a shared atomic (rare: only where
+// bins are narrower than a run).  At the end of a piece the lanes' open sums
+// are combined by a segmented warp scan over their (non-decreasing) bins and
+// each bin's last lane adds the total without atomics.  Every kPromoteRows
+// rows the touched FP32 bins are promoted into the warp's FP64 histogram.
 template <int NF, int NP>
 __global__ void __launch_bounds__(256)
     k_bin(BinParams p, const uint32_t *__restrict__ thr_g, const float *__restrict__ iw_g,
@@ -84,128 +170,119 @@ __global__ void __launch_bounds__(256)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nrb = p.nrbins;
+    const int rp = p.rp, piece = 32 * rp;
+    const BinLayout L = bin_layout(nrb, p.hc, NP, NF, rp);
     uint32_t *thr = (uint32_t *)smem;
-    float *iwz = (float *)(thr + nrb + 1);
-    size_t off = sizeof(uint32_t) * (nrb + 1) + sizeof(float) * p.hc;
-    off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = ((sizeof(double) * NP * nrb + sizeof(float) * NP * nrb + 15) & ~(size_t)15) +
-                            sizeof(float2) * NF * kBinBuf;
+    float2 *izc = (float2 *)(smem + L.izc);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char *wbase = smem + off + per_warp * wid;
-    double *whist = (double *)wbase;
-    float *rhist = (float *)(whist + NP * nrb);
-    float2 *buf = (float2 *)(wbase + ((sizeof(double) * NP * nrb + sizeof(float) * NP * nrb + 15) &
-                                      ~(size_t)15));
+    unsigned char *wbase = smem + L.warps + L.per_warp * wid;
+    double *whist = (double *)(wbase + L.whist);
+    float *rhist = (float *)(wbase + L.rhist);
+    float2 *buf = (float2 *)(wbase + L.buf);
 
     for (int i = threadIdx.x; i <= nrb; i += blockDim.x)
-        thr[i] = thr_g[i];
+        thr[i] = thr_g[i];  // thr[nrb] = 0xffffffff: the bin never runs past nrb-1
     for (int i = threadIdx.x; i < p.hc; i += blockDim.x)
-        iwz[i] = iw_g[i];
+        izc[i] = make_float2(iw_g[i], (i == 0 || i == p.half) ? 1.f : 2.f);
     for (int i = lane; i < NP * nrb; i += 32) {
         whist[i] = 0.0;
         rhist[i] = 0.f;
     }
     __syncthreads();
 
-    // Each warp takes a contiguous block of rows; (i, j) advance incrementally.
     const int64_t nrows = (int64_t)p.dims * p.dims;
     const int64_t gw = (int64_t)blockIdx.x * p.warps + wid;
     const int64_t nw = (int64_t)gridDim.x * p.warps;
     const int64_t per = (nrows + nw - 1) / nw;
     const int64_t r_begin = min(nrows, gw * per), r_end = min(nrows, r_begin + per);
-    const int rp = p.rp;
-    const int piece = 32 * rp;
     int i = (int)(r_begin / p.dims), j = (int)(r_begin - (int64_t)i * p.dims);
-    int bmin = nrb, bmax = -1;  // this lane's bins since the last FP64 promotion
+    int bmin = nrb, bmax = -1;  // bins touched since the last FP64 promotion
     int rows_since = 0;
+    float2 v[NF][kMaxRP];
+    if (r_begin < r_end)
+        load_piece<NF>(p, r_begin, 0, lane, v);
     for (int64_t r = r_begin; r < r_end; r++) {
         const int ki = kval_dev(i, p.dims), kj = kval_dev(j, p.dims);
         const uint32_t r2 = (uint32_t)(ki * ki + kj * kj);
         const float pxy = __ldg(iw_g + i) * __ldg(iw_g + j);
-        const size_t rowoff = (size_t)r * p.hc;
-        int cb = -1;
-        float acc[NP];
-#pragma unroll
-        for (int q = 0; q < NP; q++)
-            acc[q] = 0.f;
         for (int pb = 0; pb < p.hc; pb += piece) {
-            __syncwarp();
-            for (int t = 0; t < rp; t++) {
-                const int m = pb + t * 32 + lane;
-                if (m < p.hc) {
+            stage_piece<NF>(p, r, pb, lane, v, buf, piece);
+            // next piece (this row's, or the next row's first) in flight
+            if (pb + piece < p.hc)
+                load_piece<NF>(p, r, pb + piece, lane, v);
+            else if (r + 1 < r_end)
+                load_piece<NF>(p, r + 1, 0, lane, v);
+
+            const int kz0 = pb + lane * rp;
+            int cb = nrb;  // key of a lane without modes: sorts after every bin
+            float acc[NP];
 #pragma unroll
-                    for (int f = 0; f < NF; f++)
-                        buf[f * kBinBuf + t * 32 + lane] = __ldg(p.f[f] + rowoff + m);
-                }
-            }
-            __syncwarp();
-            for (int t = 0; t < rp; t++) {
-                const int q = lane * rp + t;
-                const int kz = pb + q;
-                if (kz >= p.hc)
-                    break;
-                const uint32_t kk2 = r2 + (uint32_t)(kz * kz);
-                if (kk2 == 0)
-                    continue;
-                int b;
-                if (cb < 0) {
-                    b = bin_lookup(kk2, thr, nrb, p.bpu_half);
-                } else {
-                    b = cb;
-                    while (b + 1 < nrb && kk2 >= thr[b + 1])
-                        b++;
-                }
-                if (b != cb) {
-                    if (cb >= 0) {
+            for (int s = 0; s < NP; s++)
+                acc[s] = 0.f;
+            if (kz0 < p.hc) {
+                uint32_t kk2 = r2 + (uint32_t)(kz0 * kz0);
+                cb = bin_lookup(kk2, thr, nrb, p.bpu_half);
+                bmin = min(bmin, cb);
+                uint32_t nx = thr[cb + 1];
+                const int lim = min(rp, p.hc - kz0);
+                const float2 *bl = buf + lane * rp;
+                for (int t = 0; t < lim; t++) {
+                    const int kz = kz0 + t;
+                    if (kk2 >= nx) {
 #pragma unroll
                         for (int s = 0; s < NP; s++) {
                             atomicAdd(&rhist[s * nrb + cb], acc[s]);
                             acc[s] = 0.f;
                         }
+                        do {
+                            cb++;
+                            nx = thr[cb + 1];
+                        } while (kk2 >= nx);
                     }
-                    cb = b;
-                    bmin = min(bmin, b);
-                    bmax = max(bmax, b);
-                }
-                const float pz = pxy * iwz[kz];
-                const float p2 = pz * pz;
-                const float v = (kz == 0 || kz == p.half) ? p2 * p2 : 2.f * (p2 * p2);
-                float2 fv[NF];
-#pragma unroll
-                for (int f = 0; f < NF; f++)
-                    fv[f] = buf[f * kBinBuf + q];
-                if (r == p.corner_row && kz == p.half) {
-                    // The last log-k bin holds this single mode; its exact value
-                    // (an alternating sum computed by the deposit) replaces the
-                    // FP32 transform's, whose rounding noise it cannot average.
+                    const float2 ic = izc[kz];
+                    const float pz = pxy * ic.x;
+                    const float p2 = pz * pz;
+                    const float w = ic.y * (p2 * p2);
+                    float2 fv[NF];
 #pragma unroll
                     for (int f = 0; f < NF; f++)
-                        if (p.corner[f])
-                            fv[f] = make_float2((float)*p.corner[f], 0.f);
+                        fv[f] = bl[f * piece + t];
+#pragma unroll
+                    for (int s = 0; s < NP; s++) {
+                        const float2 a = pick<NF>(fv, p.pa[s]), c = pick<NF>(fv, p.pb[s]);
+                        acc[s] = fmaf(w, fmaf(a.x, c.x, a.y * c.y), acc[s]);
+                    }
+                    kk2 += (uint32_t)(2 * kz + 1);
                 }
+                bmax = max(bmax, cb);
+            }
+            // Segmented inclusive scan over lanes with equal open bin.
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int ku = __shfl_up_sync(0xffffffffu, cb, o);
 #pragma unroll
                 for (int s = 0; s < NP; s++) {
-                    const float2 a = pick<NF>(fv, p.pa[s]), c = pick<NF>(fv, p.pb[s]);
-                    acc[s] = fmaf(v, fmaf(a.x, c.x, a.y * c.y), acc[s]);
+                    const float x = __shfl_up_sync(0xffffffffu, acc[s], o);
+                    if (lane >= o && ku == cb)
+                        acc[s] += x;
                 }
             }
-        }
-        if (cb >= 0) {
+            const int kd = __shfl_down_sync(0xffffffffu, cb, 1);
+            if (cb < nrb && (lane == 31 || kd != cb)) {
 #pragma unroll
-            for (int s = 0; s < NP; s++)
-                atomicAdd(&rhist[s * nrb + cb], acc[s]);
+                for (int s = 0; s < NP; s++)
+                    rhist[s * nrb + cb] += acc[s];
+            }
+            __syncwarp();
         }
         if (++j == p.dims) {
             j = 0;
             i++;
         }
-        // Every kPromoteRows rows (and at the end) promote the FP32 sums of the
-        // touched bins into the warp's FP64 histogram.
         if (++rows_since == kPromoteRows || r + 1 == r_end) {
             rows_since = 0;
             const int lo = (int)__reduce_min_sync(0xffffffffu, (unsigned)bmin);
             const int hi = (int)__reduce_max_sync(0xffffffffu, (unsigned)(bmax + 1)) - 1;
-            __syncwarp();
             for (int b = lo + lane; b <= hi; b += 32) {
 #pragma unroll
                 for (int s = 0; s < NP; s++) {
@@ -223,7 +300,7 @@ __global__ void __launch_bounds__(256)
     for (int k = threadIdx.x; k < p.np * nrb; k += blockDim.x) {
         double s = 0.0;
         for (int w = 0; w < p.warps; w++) {
-            const double *wh = (const double *)(smem + off + per_warp * w);
+            const double *wh = (const double *)(smem + L.warps + L.per_warp * w + L.whist);
             s += wh[k];
         }
         partial[(size_t)blockIdx.x * p.np * nrb + k] = s;
@@ -267,14 +344,15 @@ __global__ void __launch_bounds__(kFinalizeThreads)
     power[k] = out;
 }
 
+int bin_rp(int hc)
+{
+    return hc <= 32 ? 1 : hc <= 96 ? 3 : hc <= 160 ? 5 : 9;
+}
+
 size_t bin_smem(int nrbins, int hc, int np, int nf, int warps)
 {
-    size_t off = sizeof(uint32_t) * (nrbins + 1) + sizeof(float) * hc;
-    off = (off + 15) & ~(size_t)15;
-    const size_t per_warp = ((sizeof(double) * np * nrbins + sizeof(float) * np * nrbins + 15) &
-                             ~(size_t)15) +
-                            sizeof(float2) * nf * kBinBuf;
-    return off + per_warp * warps;
+    const BinLayout L = bin_layout(nrbins, hc, np, nf, bin_rp(hc));
+    return L.warps + L.per_warp * warps;
 }
 
 // Instantiated (fields, pairs) shapes; a request is rounded up to the first
@@ -336,7 +414,7 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
     p.half = g.half;
     p.nrbins = t.nrbins;
     p.bpu_half = (float)(0.5 * t.binsperunit);
-    p.rp = g.hc <= 32 ? 1 : g.hc <= 96 ? 3 : g.hc <= 160 ? 5 : 9;
+    p.rp = bin_rp(g.hc);
     p.warps = warps;
     cudaError_t err;
 #define GENPK_BIN_LAUNCH(NF, NP)                                                              \
