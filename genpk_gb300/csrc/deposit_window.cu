@@ -240,19 +240,32 @@ __device__ __forceinline__ void issue_chunk(const WinParams &p, int64_t c, float
         bulk_load(M, p.masses + chunk_first(p, c), mb, bar);
 }
 
-// All threads: plain copy of chunk c (tail chunk, or unaligned input).
+// All threads: n floats src -> dst (dst 16-byte aligned), 16 bytes at a time
+// where src allows.
+__device__ __forceinline__ void copy_floats(float *dst, const float *src, int n)
+{
+    int done = 0;
+    if (((uintptr_t)src & 15u) == 0u) {
+        const int n4 = n >> 2;
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+        for (int i = threadIdx.x; i < n4; i += blockDim.x)
+            d4[i] = s4[i];
+        done = n4 << 2;
+    }
+    for (int i = done + threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+}
+
+// All threads: plain copy of chunk c (tail chunk, unaligned input, or pinned
+// host memory read in place).
 template <bool VARMASS>
 __device__ __forceinline__ void copy_chunk(const WinParams &p, int64_t c, int cnt, float *P,
                                            float *M)
 {
-    const float *src = p.pos + 3 * chunk_first(p, c);
-    for (int i = threadIdx.x; i < 3 * cnt; i += blockDim.x)
-        P[i] = src[i];
-    if (VARMASS) {
-        const float *ms = p.masses + chunk_first(p, c);
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
-            M[i] = ms[i];
-    }
+    copy_floats(P, p.pos + 3 * chunk_first(p, c), 3 * cnt);
+    if (VARMASS)
+        copy_floats(M, p.masses + chunk_first(p, c), cnt);
 }
 
 // Global-path adds of one particle's eight corners (cells c, weights w[k] for
@@ -709,7 +722,12 @@ WinParams make_win_params(const DepositGeom &g, const DepositArgs &a)
     p.plane = g.grid.plane;
     p.row = g.grid.row;
     p.corner = (g.grid.dims % 2 == 0) ? 1 : 0;
-    p.bulk = ((uintptr_t)a.pos % 16 == 0 && (!var || (uintptr_t)a.masses % 16 == 0)) ? 1 : 0;
+    // Bulk copies only from device memory; pinned host memory is read in place
+    // by plain loads (the transfer over the host link is the bound there).
+    p.bulk = (!a.host_mapped && (uintptr_t)a.pos % 16 == 0 &&
+              (!var || (uintptr_t)a.masses % 16 == 0))
+                 ? 1
+                 : 0;
     return p;
 }
 

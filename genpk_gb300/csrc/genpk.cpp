@@ -31,6 +31,7 @@ enum FieldState { F_CLEAN = 0, F_DENSITY = 1, F_SPECTRUM = 2, F_GRADIENT = 3 };
 constexpr int kMaxStages = 64;
 // Below this many particles a pass always uses the sorted engine.
 constexpr int64_t kWindowMinParticles = (int64_t)1 << 20;
+constexpr int64_t kZeroCopyMinParticles = (int64_t)1 << 20;
 
 struct Pending {
     bool active = false;
@@ -152,6 +153,22 @@ bool is_device_ptr(const void *p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Device address of pinned (page-locked, mapped) host memory, or null for
+// anything else.  Kernels may read such memory in place over the host link.
+const float *mapped_host(const float *p)
+{
+    if (!p)
+        return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+        return nullptr;
+    return (const float *)a.devicePointer;
+}
+
 template <typename T>
 int grow(genpk_ctx *ctx, T **ptr, size_t *cap, size_t need)
 {
@@ -243,9 +260,12 @@ DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize)
     return g;
 }
 
-// One deposit pass from device particle arrays.
+int ensure_stage(genpk_ctx *ctx, int64_t need);
+
+// One deposit pass from device particle arrays, or (host_mapped) from pinned
+// host arrays read in place by the window engine.
 int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const float *masses,
-                float mass, int64_t n)
+                float mass, int64_t n, bool host_mapped = false)
 {
     if (n > 0xffffffffLL - 1)
         return fail(ctx, GENPK_ERR_UNSUPPORTED, "more than 2^32-1 particles in one pass");
@@ -285,6 +305,20 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
                 engine = GENPK_ENGINE_WINDOW;
         }
     }
+    if (host_mapped && engine != GENPK_ENGINE_WINDOW) {
+        // The sorted engine reads positions twice: copy them over once instead.
+        GENPK_TRY(ensure_stage(ctx, n));
+        GENPK_CUDA(cudaMemcpyAsync(ctx->stage_pos, pos, sizeof(float) * 3 * (size_t)n,
+                                   cudaMemcpyDefault, ctx->stream));
+        a.pos = ctx->stage_pos;
+        if (masses) {
+            GENPK_CUDA(cudaMemcpyAsync(ctx->stage_mass, masses, sizeof(float) * (size_t)n,
+                                       cudaMemcpyDefault, ctx->stream));
+            a.masses = ctx->stage_mass;
+        }
+        host_mapped = false;
+    }
+    a.host_mapped = host_mapped;
     ctx->last_engine = engine;
     timing_touch(ctx);
     if (engine == GENPK_ENGINE_WINDOW) {
@@ -738,6 +772,19 @@ int genpk_deposit(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     if (pos_dev && mass_dev) {
         GENPK_TRY(flush_pending(ctx));
         return run_deposit(ctx, field, boxsize, pos, masses, (float)mass, n);
+    }
+    // Large pinned host arrays: the pass reads them in place, so the transfer
+    // over the host link overlaps the deposit instead of preceding it.
+    if (!pos_dev && n >= kZeroCopyMinParticles) {
+        const float *pm = mapped_host(pos);
+        const float *mm = masses ? (mass_dev ? masses : mapped_host(masses)) : nullptr;
+        if (pm && (!masses || mm)) {
+            GENPK_TRY(flush_pending(ctx));
+            GENPK_TRY(run_deposit(ctx, field, boxsize, pm, mm, (float)mass, n, true));
+            // The caller may free or reuse its buffers as soon as we return.
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            return GENPK_OK;
+        }
     }
     // Stage host data on the device; merge with the pending pass when compatible.
     const bool var = masses != nullptr;

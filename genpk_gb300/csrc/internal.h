@@ -80,6 +80,7 @@ struct DepositArgs {
     double *field_sub;     // device: running sum of the means subtracted from it
     double *field_corner;  // device: exact DFT value at k = (N/2, N/2, N/2), even N
     bool clean;            // grid content is undefined and must be overwritten
+    bool host_mapped = false;  // pos/masses are pinned host memory read in place
 };
 
 // Tile shapes the deposit kernels are instantiated for.

@@ -266,6 +266,40 @@ def test_window_engine_edge_cases(gp, case):
         grid_close(ctx.read_field(0), ref, tol=1e-6)
 
 
+@pytest.mark.parametrize("var", [False, True])
+def test_pinned_host_input_read_in_place(gp, var):
+    """Large pinned host arrays are read in place by the window engine (no
+    staging copy); the sorted engine gets them copied once.  Same grids as
+    from device memory."""
+    import torch
+    from genpk_gb300 import synth
+    dims, box = 128, 1000.0
+    pos = synth.zeldovich(128, box, seed=15)
+    hpos = torch.from_numpy(pos).pin_memory()
+    masses = hmass = None
+    mass = 1.0
+    if var:
+        masses = np.linspace(0.5, 1.5, len(pos)).astype(np.float32)
+        hmass = torch.from_numpy(masses).pin_memory()
+        mass = 0.0
+    dpos = hpos.cuda()
+    dmass = hmass.cuda() if var else None
+    with gp.Context(dims, 16) as ctx:
+        out = {}
+        for eng in (gp.api.ENGINE_WINDOW, gp.api.ENGINE_SORTED):
+            ctx.set_engine(eng)
+            for name, p_, m_ in (("dev", dpos, dmass), ("pinned", hpos, hmass)):
+                ctx.zero(0)
+                ctx.deposit(0, box, p_, m_, mass)
+                ctx.sync()
+                assert ctx.last_engine == eng
+                out[(eng, name)] = ctx.read_field(0)
+    grid_close(out[(gp.api.ENGINE_WINDOW, "pinned")], out[(gp.api.ENGINE_WINDOW, "dev")], tol=1e-6)
+    assert np.array_equal(out[(gp.api.ENGINE_SORTED, "pinned")], out[(gp.api.ENGINE_SORTED, "dev")])
+    grid_close(out[(gp.api.ENGINE_WINDOW, "pinned")], O.deposit(pos, box, dims, masses, mass),
+               tol=1e-6)
+
+
 def test_window_engine_reports_non_finite(gp):
     from genpk_gb300 import synth
     dims, box = 32, 100.0
