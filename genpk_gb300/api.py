@@ -21,6 +21,7 @@ from . import native
 
 GENPK_FLAG_TIMING = 0x1
 ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW = 0, 1, 2
+FFT_AUTO, FFT_CUFFT3D = 0, 1
 
 
 class GenPKError(RuntimeError):
@@ -203,6 +204,11 @@ class Context:
     def set_engine(self, engine: int):
         """Deposit engine: ENGINE_AUTO, ENGINE_SORTED (exact) or ENGINE_WINDOW."""
         self._chk(self.lib.genpk_set_deposit_engine(self.h, int(engine)))
+
+    def set_fft_mode(self, mode: int):
+        """Forward-FFT path: FFT_AUTO (2-D cuFFT + fused x-pass/binning where
+        supported) or FFT_CUFFT3D (3-D cuFFT + binning kernel)."""
+        self._chk(self.lib.genpk_set_fft_mode(self.h, int(mode)))
 
     @property
     def last_engine(self) -> int:

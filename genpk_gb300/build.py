@@ -25,7 +25,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["deposit.cu", "deposit_window.cu", "spectrum.cu", "adjoint.cu", "noalloc.cu"]
+CU_SOURCES = ["deposit.cu", "deposit_window.cu", "spectrum.cu", "xfft.cu", "adjoint.cu",
+              "noalloc.cu"]
 CXX_SOURCES = {"genpk.cpp": ["-O2"], "tables.cpp": ["-O2", "-ffast-math"]}
 COMPAT_SOURCE = "compat.cpp"
 

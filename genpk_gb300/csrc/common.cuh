@@ -129,8 +129,8 @@ __device__ __forceinline__ f2sum one_minus_2frac(float p, float uh, float ul)
 
 // One axis of a particle in full: the wrapped cell and FP32 fraction exactly as
 // split_cell computes them, plus what the exact corner-mode term needs:
-// u = 1 - 2*(xh - floor) for the final cell (exact in FP32 for xh >= 1; off by
-// at most 2^-25 below) and xl, the low part of x = xh + xl, so that
+// u = 1 - 2*(xh - floor) for the final cell (exact in FP32 for xh >= 1; one
+// rounding below) and xl, the low part of x = xh + xl, so that
 // 1 - 2d = u - 2*xl exactly.
 struct AxisSplit {
     int cell;
@@ -147,7 +147,7 @@ __device__ __forceinline__ AxisSplit split_axis(float p, float uh, float ul, int
     const float f = floorf(xh);
     const float a = __fsub_rn(xh, f);
     float d = __fadd_rn(a, xl);
-    float u = __fsub_rn(1.f, __fmul_rn(2.f, a));
+    float u = fmaf(-2.f, a, 1.f);
     int fi = (int)f;
     if (d < 0.f) {
         d = __fadd_rn(d, 1.f);

@@ -297,7 +297,7 @@ __device__ __noinline__ void carry_corners(const WinParams &p, float *grid, cons
     global_corners(p, grid, c, w);
 }
 
-template <bool VARMASS>
+template <bool VARMASS, bool CORNER>
 __global__ void __launch_bounds__(kWinThreads, 1)
     k_window_deposit(WinParams p, DeviceStatus *st, float *__restrict__ grid)
 {
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             const AxisSplit ax = split_axis(x, p.uh, p.ul, p.dims);
             const AxisSplit ay = split_axis(y, p.uh, p.ul, p.dims);
             const AxisSplit az = split_axis(z, p.uh, p.ul, p.dims);
-            if (p.corner) {
+            if (CORNER) {
                 f2sum v = corner_factor(ax, ay, az);
                 if (VARMASS) {
                     const float mm = m * mscale;
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         // window_box, so the flush needs no barrier of its own.
     }
 
-    if (p.corner) {
+    if (CORNER) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const f2sum other = {__shfl_xor_sync(0xffffffffu, alt.hi, o),
@@ -789,7 +789,8 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, doub
     if (p.nchunks > 0) {
         const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
         const int smem = p.win_off + 4 * p.cap;
-        auto kern = a.masses ? k_window_deposit<true> : k_window_deposit<false>;
+        auto kern = a.masses ? (p.corner ? k_window_deposit<true, true> : k_window_deposit<true, false>)
+                             : (p.corner ? k_window_deposit<false, true> : k_window_deposit<false, false>);
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem)) != cudaSuccess)
             return err;

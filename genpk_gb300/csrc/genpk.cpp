@@ -63,8 +63,11 @@ struct genpk_ctx {
     BinTables tables;
     BinDevice bdev;
 
-    // cuFFT: r2c plans by batch size, one c2r plan; one shared work area.
+    // cuFFT: r2c plans by batch size (3-D plans under +batch, batched 2-D
+    // x-plane plans under -batch), one c2r plan; one shared work area.
     std::map<int, cufftHandle> r2c;
+    int fft_mode = GENPK_FFT_AUTO;  // requested forward-FFT path
+    float2 *d_xtw = nullptr;        // x-pass twiddles, null when unsupported
     cufftHandle c2r = 0;
     bool c2r_made = false;
     void *fft_work = nullptr;
@@ -393,23 +396,35 @@ int ensure_stage(genpk_ctx *ctx, int64_t need)
     return GENPK_OK;
 }
 
-int make_r2c(genpk_ctx *ctx, int batch, cufftHandle *out)
+// planes: a batched 2-D R2C over every x-plane of `batch` consecutive grids
+// (the x-axis pass then runs in xfft.cu); else the full 3-D R2C.
+int make_r2c(genpk_ctx *ctx, int batch, bool planes, cufftHandle *out)
 {
-    auto it = ctx->r2c.find(batch);
+    const int key = planes ? -batch : batch;
+    auto it = ctx->r2c.find(key);
     if (it != ctx->r2c.end()) {
         *out = it->second;
         return GENPK_OK;
     }
     const long long n = ctx->dims;
-    long long dims3[3] = {n, n, n};
-    long long inembed[3] = {n, n, (long long)ctx->gg.row};
-    long long onembed[3] = {n, n, (long long)ctx->gg.hc};
     cufftHandle h;
     GENPK_CUFFT(cufftCreate(&h));
     GENPK_CUFFT(cufftSetAutoAllocation(h, 0));
     size_t ws = 0;
-    cufftResult r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat, onembed,
-                                        1, (long long)ctx->gg.nfloat / 2, CUFFT_R2C, batch, &ws);
+    cufftResult r;
+    if (planes) {
+        long long dims2[2] = {n, n};
+        long long inembed[2] = {n, (long long)ctx->gg.row};
+        long long onembed[2] = {n, (long long)ctx->gg.hc};
+        r = cufftMakePlanMany64(h, 2, dims2, inembed, 1, n * ctx->gg.row, onembed, 1,
+                                n * ctx->gg.hc, CUFFT_R2C, (long long)batch * n, &ws);
+    } else {
+        long long dims3[3] = {n, n, n};
+        long long inembed[3] = {n, n, (long long)ctx->gg.row};
+        long long onembed[3] = {n, n, (long long)ctx->gg.hc};
+        r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat, onembed, 1,
+                                (long long)ctx->gg.nfloat / 2, CUFFT_R2C, batch, &ws);
+    }
     if (r != CUFFT_SUCCESS) {
         cufftDestroy(h);
         return fail(ctx, GENPK_ERR_CUFFT, "cufftMakePlanMany64 (r2c) failed: " + std::to_string((int)r));
@@ -427,7 +442,7 @@ int make_r2c(genpk_ctx *ctx, int batch, cufftHandle *out)
             GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
     }
     GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
-    ctx->r2c[batch] = h;
+    ctx->r2c[key] = h;
     *out = h;
     return GENPK_OK;
 }
@@ -468,7 +483,20 @@ int make_c2r(genpk_ctx *ctx)
 
 // Bring every field in `need` to SPECTRUM form: pending deposits first, then
 // one batched r2c per run of consecutive field indices.
-int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need)
+bool use_xfft(const genpk_ctx *ctx)
+{
+    return ctx->fft_mode == GENPK_FFT_AUTO && ctx->d_xtw != nullptr;
+}
+
+// fused: when not null and its field is transformed alone, the x-pass also
+// bins that field's auto spectrum into fused->bin (fused->done := true).
+struct FusedAuto {
+    int field;
+    XfftBin bin;
+    bool done;
+};
+
+int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused = nullptr)
 {
     GENPK_TRY(flush_pending(ctx));
     std::vector<int> todo;
@@ -495,10 +523,20 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need)
         while (j < todo.size() && todo[j] == todo[j - 1] + 1)
             j++;
         const int batch = (int)(j - i);
+        const bool planes = use_xfft(ctx);
         cufftHandle h;
-        GENPK_TRY(make_r2c(ctx, batch, &h));
+        GENPK_TRY(make_r2c(ctx, batch, planes, &h));
         float *base = grid_of(ctx, todo[i]);
         GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
+        if (planes) {
+            const bool bin = fused && batch == 1 && todo[i] == fused->field;
+            stage_event(ctx, "fft");
+            GENPK_CUDA(xfft_pass(ctx->gg, base, batch, ctx->d_xtw, bin ? &fused->bin : nullptr,
+                                 ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches));
+            stage_event(ctx, bin ? "xfft_bin" : "xfft");
+            if (bin)
+                fused->done = true;
+        }
         for (size_t k = i; k < j; k++) {
             ctx->state[(size_t)todo[k]] = F_SPECTRUM;
             ctx->corner_valid[(size_t)todo[k]] = true;
@@ -519,14 +557,37 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         GENPK_TRY(check_field(ctx, pairs[q]));
         fields.push_back(pairs[q]);
     }
-    GENPK_TRY(to_spectrum(ctx, fields));
-    std::sort(fields.begin(), fields.end());
-    fields.erase(std::unique(fields.begin(), fields.end()), fields.end());
-
     const int nrb = ctx->nrbins;
     GENPK_TRY(grow(ctx, &ctx->d_power, &ctx->power_cap, (size_t)np * nrb));
+    // A single auto spectrum of a field still to be transformed: bin it inside
+    // the x-axis FFT pass.
+    FusedAuto fa;
+    fa.done = false;
+    FusedAuto *fused = nullptr;
+    if (np == 1 && pairs[0] == pairs[1] && pair_mass[0] == pair_mass[1] && use_xfft(ctx) &&
+        xfft_bin_supported(ctx->dims, nrb) && ctx->state[(size_t)pairs[0]] != F_SPECTRUM &&
+        ctx->state[(size_t)pairs[0]] != F_GRADIENT) {
+        const int ctas = xfft_bin_ctas(ctx->dims, 1, ctx->num_sms);
+        GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * nrb));
+        fa.field = pairs[0];
+        fa.bin.nrbins = nrb;
+        fa.bin.bpu_half = (float)(0.5 * ctx->tables.binsperunit);
+        fa.bin.thr = ctx->bdev.thr;
+        fa.bin.iw = ctx->bdev.iw;
+        fa.bin.corner = ctx->d_field_mass + 2 * ctx->nfields + pairs[0];
+        fa.bin.partial = ctx->d_partial;
+        fused = &fa;
+    }
+    GENPK_TRY(to_spectrum(ctx, fields, fused));
+    std::sort(fields.begin(), fields.end());
+    fields.erase(std::unique(fields.begin(), fields.end()), fields.end());
+    if (fa.done) {
+        GENPK_CUDA(finalize_power(ctx->d_partial, xfft_bin_ctas(ctx->dims, 1, ctx->num_sms), nrb,
+                                  ctx->bdev.count, pair_mass[0], pair_mass[1], ctx->d_power,
+                                  ctx->stream, &ctx->launches));
+    }
     // Pairs are binned in groups whose fields fit one kernel instantiation.
-    int q0 = 0;
+    int q0 = fa.done ? np : 0;
     while (q0 < np) {
         BinLaunch l;
         l.nfields = 0;
@@ -643,6 +704,7 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->grids);
     cudaFree(ctx->d_field_mass);
     cudaFree(ctx->d_status);
+    cudaFree(ctx->d_xtw);
     cudaFree(ctx->bdev.thr);
     cudaFree(ctx->bdev.iw);
     cudaFree(ctx->bdev.count);
@@ -724,6 +786,13 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     CREATE_CUDA(cudaMemcpy(ctx->bdev.count, cnt.data(), sizeof(double) * nrbins,
                            cudaMemcpyHostToDevice));
     CREATE_CUDA(cudaMalloc(&ctx->d_gcoef, sizeof(float) * nrbins));
+    if (xfft_supported((int)dims)) {
+        std::vector<float> tw;
+        xfft_twiddles((int)dims, &tw);
+        CREATE_CUDA(cudaMalloc(&ctx->d_xtw, sizeof(float) * tw.size()));
+        CREATE_CUDA(cudaMemcpy(ctx->d_xtw, tw.data(), sizeof(float) * tw.size(),
+                               cudaMemcpyHostToDevice));
+    }
 #undef CREATE_CUDA
     ctx->state.assign((size_t)nfields, F_CLEAN);
     ctx->auto_power.assign((size_t)nfields, {});
@@ -1075,6 +1144,16 @@ int genpk_set_deposit_engine(genpk_ctx *ctx, int engine)
         return fail(ctx, GENPK_ERR_INVALID, "unknown deposit engine");
     GENPK_TRY(flush_pending(ctx));
     ctx->engine = engine;
+    return GENPK_OK;
+}
+
+int genpk_set_fft_mode(genpk_ctx *ctx, int mode)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (mode != GENPK_FFT_AUTO && mode != GENPK_FFT_CUFFT3D)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_set_fft_mode: unknown mode");
+    ctx->fft_mode = mode;
     return GENPK_OK;
 }
 

@@ -156,6 +156,24 @@ bool build_bin_tables_into(int64_t dims, int nrbins, const TableSpans &o, double
 double ref_onedinvwindow(int64_t k, int64_t n);
 double ref_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
 
+// x-axis FFT pass with optional fused auto-spectrum binning (xfft.cu): the
+// grid's (z, y) transforms come from a batched 2-D cuFFT R2C over x-planes.
+struct XfftBin {
+    int nrbins;
+    float bpu_half;         // 0.5 * binsperunit (first-guess bin)
+    const uint32_t *thr;    // [nrbins+1]
+    const float *iw;        // [dims]
+    const double *corner;   // exact (N/2,N/2,N/2) value, or null
+    double *partial;        // [ctas][nrbins] FP64 partial sums
+};
+bool xfft_supported(int dims);
+bool xfft_bin_supported(int dims, int nrbins);
+void xfft_twiddles(int dims, std::vector<float> *out);  // 2*dims floats
+int xfft_bin_ctas(int dims, int nbatch, int num_sms);
+cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
+                      const XfftBin *bin, int num_sms, DeviceStatus *dstat, cudaStream_t stream,
+                      int64_t *launches);
+
 struct BinDevice {
     uint32_t *thr = nullptr;   // [nrbins+1]
     float *iw = nullptr;       // [dims]
@@ -187,6 +205,10 @@ int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms
 
 // Runs the binning kernel and the finalize kernel; writes out_power[np][nrbins]
 // on the device.  partial must hold ctas*npairs*nrbins doubles.
+// power[b] = sum over the CTA partials / (ma * mb * count[b]) (count 0: 0).
+cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const double *count,
+                           double ma, double mb, double *out, cudaStream_t stream,
+                           int64_t *launches);
 cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
                         const BinLaunch &l, double *partial, double *out_power, int ctas,
                         int warps, size_t smem, cudaStream_t stream, int64_t *launches);

@@ -451,4 +451,19 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
     return cudaGetLastError();
 }
 
+cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const double *count,
+                           double ma, double mb, double *out, cudaStream_t stream,
+                           int64_t *launches)
+{
+    NormParams mn;
+    for (int q = 0; q < kMaxBinPairs; q++) {
+        mn.ma[q] = q == 0 ? ma : 1.0;
+        mn.mb[q] = q == 0 ? mb : 1.0;
+    }
+    k_bin_finalize<<<nrbins, kFinalizeThreads, 0, stream>>>(partial, ctas, 1, nrbins, count, mn,
+                                                            out);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
 }  // namespace genpk

@@ -1,0 +1,664 @@
+// xfft.cu -- the last (x-axis) pass of the forward 3-D FFT, fused with the
+// auto-spectrum binning (the GPU counterpart of the last FFTW pass of
+// gen-pk.cpp:186-193,233 followed by powerspectrum.c:35-111).
+//
+// The grid's (z, y) transforms are one batched 2-D cuFFT R2C per x-plane; this
+// kernel does the remaining length-N complex DFT along x for every (j, kz)
+// column, writes the spectrum back in place (the layout cuFFT's 3-D R2C
+// produces), and optionally bins |F|^2 for the auto spectrum in the same pass,
+// so the spectrum is read from HBM once instead of twice.
+//
+//   tiles     TZ = 4096/N consecutive columns f = j*(N/2+1) + kz (a 32 KB
+//             tile of N rows x TZ complex), moved by TMA (cp.async.bulk.tensor
+//             2-D loads and stores) into / out of shared memory; persistent
+//             CTAs (two per SM), double-buffered loads.
+//   FFT       Stockham autosort, radix 8 (one radix-2 or -4 stage last),
+//             in place in the tile with a barrier between the read and write
+//             half of every stage; 512 threads, each one radix-8 butterfly
+//             (or two radix-4, four radix-2) per stage; twiddles from an FP32
+//             table of exp(-2 pi i m/N) rounded from FP64 on the host.
+//   binning   the last stage also writes v = c * p^4 * |F|^2 (p = (iw_x iw_y)
+//             iw_z as in the binning kernel) into a [column][row] buffer;
+//             every thread then walks 8 modes along the columns of a row
+//             (|k|^2 grows with kz) with a running bin, flushing into a
+//             per-warp FP32 histogram;
+//             the lanes' open sums are combined by a segmented warp scan (rows
+//             of a warp lie in one half of the axis, so their bins are
+//             monotone); per tile the warps' histograms are summed in a fixed
+//             order into the CTA's FP64 histogram; k_bin_finalize reduces the
+//             CTA partials.
+#include "common.cuh"
+#include "internal.h"
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
+namespace genpk {
+namespace {
+
+constexpr int kXThreads = 512;
+constexpr int kXCtasPerSm = 2;
+constexpr int kXTileBytes = 32 * 1024;  // N rows x (4096/N) complex
+constexpr int kXMaxBins = 256;
+
+struct XParams {
+    int dims, hc, tz;
+    int log2n;
+    int n8;                // radix-8 stages before the last stage
+    int ncols;             // dims * hc columns per field
+    int tiles_per_field;
+    int ntiles;            // tiles_per_field * nbatch
+    int box_rows;          // rows per TMA box
+    const float2 *tw;      // [dims] exp(-2 pi i m / dims)
+    // binning of the batch's single field (nrbins == 0: no binning)
+    int nrbins;
+    float bpu_half;
+    const uint32_t *thr;   // [nrbins + 1]
+    const float *iw;       // [dims]
+    const double *corner;  // exact (N/2,N/2,N/2) value or null
+    double *partial;       // [gridDim.x][nrbins]
+};
+
+struct ColInfo {
+    int r2;      // ky^2 + kz^2, or -1 for a column past the end
+    float iwj;   // iw(ky)
+    float iwz;   // iw(kz)
+    float w;     // mode weight: 1 on the kz = 0 and kz = N/2 planes, else 2
+    int special; // 1: (j, kz) = (0, 0) (row 0 is the skipped k = 0 mode);
+                 // 2: (j, kz) = (N/2, N/2) (row N/2 is the exact corner mode)
+    int pad[3];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// Bounded wait (~2^31 clocks, about a second): false if it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > (1ll << 31))
+            return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y, const void *src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::
+                     "l"(map),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit()
+{
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_wait_read_all()
+{
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+    return make_float2(a.x + b.x, a.y + b.y);
+}
+
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    return make_float2(a.x - b.x, a.y - b.y);
+}
+
+// multiply by -i
+__device__ __forceinline__ float2 mul_mi(float2 a)
+{
+    return make_float2(a.y, -a.x);
+}
+
+// Forward R-point DFTs in registers, natural order in and out.
+__device__ __forceinline__ void dft2(float2 *v)
+{
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+
+__device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3)
+{
+    const float2 s0 = cadd(a0, a2), s1 = csub(a0, a2), s2 = cadd(a1, a3), s3 = mul_mi(csub(a1, a3));
+    a0 = cadd(s0, s2);
+    a2 = csub(s0, s2);
+    a1 = cadd(s1, s3);
+    a3 = csub(s1, s3);
+}
+
+__device__ __forceinline__ void dft8(float2 *v)
+{
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4(e0, e1, e2, e3);
+    dft4(o0, o1, o2, o3);
+    const float h = 0.70710678118654752440f;  // 1/sqrt(2)
+    // W8^1 = (1 - i)/sqrt2, W8^2 = -i, W8^3 = (-1 - i)/sqrt2
+    const float2 t1 = make_float2((o1.x + o1.y) * h, (o1.y - o1.x) * h);
+    const float2 t2 = mul_mi(o2);
+    const float2 t3 = make_float2((o3.y - o3.x) * h, -(o3.x + o3.y) * h);
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, t1);
+    v[5] = csub(e1, t1);
+    v[2] = cadd(e2, t2);
+    v[6] = csub(e2, t2);
+    v[3] = cadd(e3, t3);
+    v[7] = csub(e3, t3);
+}
+
+template <int R>
+__device__ __forceinline__ void dft(float2 *v)
+{
+    if (R == 8) {
+        dft8(v);
+    } else if (R == 4) {
+        dft4(v[0], v[1], v[2], v[3]);
+    } else {
+        dft2(v);
+    }
+}
+
+// Reads of one Stockham stage (radix R, current span NS, length N): 8 values
+// per thread (8/R butterflies), twiddled and transformed, kept in registers.
+// All strides are compile-time constants.
+template <int N, int NS, int R>
+__device__ __forceinline__ void stage_read(const float2 *tile, const float2 *tw, int c, int g,
+                                           float2 (&v)[8])
+{
+    constexpr int TZ = kXTileBytes / 8 / N;
+    constexpr int PER = 8 / R;
+    constexpr int NB = N / R;
+    constexpr int TSTEP = N / (NS * R);  // twiddle index step per k*r
+#pragma unroll
+    for (int m = 0; m < PER; m++) {
+        const int j = g + m * (N / 8);
+        const int k = j & (NS - 1);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            float2 x = tile[(j + r * NB) * TZ + c];
+            if (NS > 1 && r > 0)
+                x = cmul(x, tw[k * TSTEP * r]);
+            v[m * R + r] = x;
+        }
+        dft<R>(&v[m * R]);
+    }
+}
+
+// Output row of value (m, r) of a stage.
+template <int N, int NS, int R>
+__device__ __forceinline__ int stage_out_row(int g, int m, int r)
+{
+    const int j = g + m * (N / 8);
+    const int k = j & (NS - 1);
+    return (j - k) * R + k + r * NS;
+}
+
+template <int N, int NS, int R>
+__device__ __forceinline__ void stage_write(float2 *tile, int c, int g, const float2 (&v)[8])
+{
+    constexpr int TZ = kXTileBytes / 8 / N;
+    constexpr int PER = 8 / R;
+#pragma unroll
+    for (int m = 0; m < PER; m++)
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            tile[stage_out_row<N, NS, R>(g, m, r) * TZ + c] = v[m * R + r];
+}
+
+template <int N, int NS>
+__device__ __forceinline__ void stage(float2 *tile, const float2 *tw, int c, int g, float2 (&v)[8])
+{
+    stage_read<N, NS, 8>(tile, tw, c, g, v);
+    __syncthreads();
+    stage_write<N, NS, 8>(tile, c, g, v);
+    __syncthreads();
+}
+
+template <int N>
+struct FftPlan {
+    static constexpr int L = N == 64 ? 6 : N == 128 ? 7 : N == 256 ? 8 : N == 512 ? 9 : 10;
+    static constexpr int N8 = (L % 3 == 0) ? L / 3 - 1 : L / 3;  // radix-8 stages before the last
+    static constexpr int NSL = 1 << (3 * N8);                      // span before the last stage
+    static constexpr int RL = N / NSL;                             // last radix: 8, 4 or 2
+};
+
+// Every stage but the last written back; the last stage's values left in v.
+template <int N>
+__device__ __forceinline__ void fft_to_last(float2 *tile, const float2 *tw, int c, int g,
+                                            float2 (&v)[8])
+{
+    using P = FftPlan<N>;
+    if constexpr (P::N8 >= 1)
+        stage<N, 1>(tile, tw, c, g, v);
+    if constexpr (P::N8 >= 2)
+        stage<N, 8>(tile, tw, c, g, v);
+    if constexpr (P::N8 >= 3)
+        stage<N, 64>(tile, tw, c, g, v);
+    stage_read<N, P::NSL, P::RL>(tile, tw, c, g, v);
+}
+
+__device__ __forceinline__ int kval_x(int i, int n)
+{
+    return i <= n / 2 ? i : i - n;
+}
+
+__device__ __forceinline__ int bin_of(uint32_t kk2, const uint32_t *thr, int nrb, float bpu_half)
+{
+    int b = (int)(bpu_half * __logf((float)kk2));
+    b = max(0, min(nrb - 1, b));
+    while (kk2 >= thr[b + 1])
+        b++;
+    while (b > 0 && kk2 < thr[b])
+        b--;
+    return b;
+}
+
+// The last stage: write the outputs (natural row order) and, when binning,
+// the per-mode values v into vals[c * (N + 1) + row].
+template <int N, bool BIN>
+__device__ __forceinline__ void last_write(float2 *tile, float *vals, const ColInfo &ci, int c,
+                                           int g, const float2 (&v)[8], const float *iw_s)
+{
+    using P = FftPlan<N>;
+    constexpr int TZ = kXTileBytes / 8 / N;
+    constexpr int PER = 8 / P::RL;
+    const float cw = ci.w * 1.f;
+#pragma unroll
+    for (int m = 0; m < PER; m++)
+#pragma unroll
+        for (int r = 0; r < P::RL; r++) {
+            const int row = stage_out_row<N, P::NSL, P::RL>(g, m, r);
+            const float2 f = v[m * P::RL + r];
+            tile[row * TZ + c] = f;
+            if (BIN) {
+                const float p1 = (iw_s[row] * ci.iwj) * ci.iwz;
+                const float p2 = p1 * p1;
+                vals[c * (N + 1) + row] = cw * (p2 * p2) * fmaf(f.x, f.x, f.y * f.y);
+            }
+        }
+}
+
+template <int N, bool BIN>
+__global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
+    k_xfft(const __grid_constant__ CUtensorMap map, XParams p, DeviceStatus *st)
+{
+    constexpr int TZ = kXTileBytes / 8 / N;
+    constexpr int BOX = N < 256 ? N : 256;
+    constexpr int NBOX = N / BOX;
+    extern __shared__ __align__(1024) unsigned char xs[];
+    float2 *tiles = reinterpret_cast<float2 *>(xs);  // [2][N][TZ]
+    unsigned char *q = xs + 2 * kXTileBytes;
+    float2 *tw_s = reinterpret_cast<float2 *>(q);
+    q += sizeof(float2) * N;
+    float *iw_s = reinterpret_cast<float *>(q);
+    q += sizeof(float) * N;
+    ColInfo *cols = reinterpret_cast<ColInfo *>(q);
+    q += sizeof(ColInfo) * TZ;
+    float *vals = reinterpret_cast<float *>(q);                  // [TZ][N + 1]
+    q += BIN ? sizeof(float) * TZ * (N + 1) : 0;
+    q = xs + ((q - xs + 15) & ~(size_t)15);
+    float *whist = reinterpret_cast<float *>(q);                 // [warps][nrbins]
+    q += BIN ? sizeof(float) * (kXThreads / 32) * p.nrbins : 0;
+    q = xs + ((q - xs + 15) & ~(size_t)15);
+    double *chist = reinterpret_cast<double *>(q);               // [nrbins]
+    q += BIN ? sizeof(double) * p.nrbins : 0;
+    uint32_t *thr = reinterpret_cast<uint32_t *>(q);             // [nrbins + 1]
+    __shared__ __align__(8) unsigned long long bar[2];
+
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int c = tid % TZ, g = tid / TZ;  // FFT: column and butterfly group
+    for (int i = tid; i < N; i += kXThreads) {
+        tw_s[i] = p.tw[i];
+        iw_s[i] = BIN ? p.iw[i] : 0.f;
+    }
+    if (BIN) {
+        for (int i = tid; i < (kXThreads / 32) * p.nrbins; i += kXThreads)
+            whist[i] = 0.f;
+        for (int i = tid; i < p.nrbins; i += kXThreads)
+            chist[i] = 0.0;
+        for (int i = tid; i <= p.nrbins; i += kXThreads)
+            thr[i] = p.thr[i];
+    }
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_proxy_async();
+    }
+    __syncthreads();
+    const float corner_val = (BIN && p.corner) ? (float)*p.corner : 0.f;
+
+    auto issue = [&](int t, int buf) {
+        const int b = t / p.tiles_per_field, f0 = (t - b * p.tiles_per_field) * TZ;
+        float2 *dst = tiles + buf * (kXTileBytes / (int)sizeof(float2));
+        mbar_expect_tx(&bar[buf], (unsigned)kXTileBytes);
+#pragma unroll
+        for (int k = 0; k < NBOX; k++)
+            tma_load_2d(dst + k * BOX * TZ, &map, 2 * f0, b * N + k * BOX, &bar[buf]);
+    };
+
+    unsigned timeouts = 0;
+    if (tid == 0 && (int)blockIdx.x < p.ntiles)
+        issue(blockIdx.x, 0);
+    int k = 0;
+    for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, k++) {
+        const int buf = k & 1;
+        float2 *tile = tiles + buf * (kXTileBytes / (int)sizeof(float2));
+        if (tid == 0 && t + (int)gridDim.x < p.ntiles) {
+            bulk_wait_read_all();  // the store from the other buffer has read it
+            issue(t + gridDim.x, buf ^ 1);
+        }
+        const int b = t / p.tiles_per_field, f0 = (t - b * p.tiles_per_field) * TZ;
+        if (BIN && tid < TZ) {
+            const int f = f0 + tid;
+            ColInfo ci;
+            if (f < p.ncols) {
+                const int j = f / p.hc, kz = f - j * p.hc;
+                const int ky = kval_x(j, N);
+                ci.r2 = ky * ky + kz * kz;
+                ci.iwj = p.iw[j];
+                ci.iwz = p.iw[kz];
+                ci.w = (kz == 0 || kz == N / 2) ? 1.f : 2.f;
+                ci.special = (j == 0 && kz == 0) ? 1 : (j == N / 2 && kz == N / 2 && p.corner) ? 2 : 0;
+            } else {
+                ci.r2 = -1;
+                ci.iwj = ci.iwz = ci.w = 0.f;
+                ci.special = 0;
+            }
+            cols[tid] = ci;
+        }
+        if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
+            timeouts++;
+        __syncthreads();
+
+        float2 v[8];
+        fft_to_last<N>(tile, tw_s, c, g, v);
+        __syncthreads();
+        const ColInfo ci = BIN ? cols[c] : ColInfo{};
+        last_write<N, BIN>(tile, vals, ci, c, g, v, iw_s);
+        if (BIN && ci.special) {
+            // the skipped k = 0 mode and the exact corner mode
+            const int row = ci.special == 1 ? 0 : N / 2;
+            const float p1 = (iw_s[row] * ci.iwj) * ci.iwz;
+            const float p2 = p1 * p1;
+            const float pw = ci.special == 1 ? 0.f : corner_val * corner_val;
+            if (g == 0)  // one thread of the column writes it
+                vals[c * (N + 1) + row] = ci.w * (p2 * p2) * pw;
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll
+            for (int kb = 0; kb < NBOX; kb++)
+                tma_store_2d(&map, 2 * f0, b * N + kb * BOX, tile + kb * BOX * TZ);
+            bulk_commit();
+        }
+
+        if (BIN) {
+            // Walk columns of a row with a running bin: 8 modes per thread
+            // (8 columns of one row; for N = 1024, 4 columns of two rows).
+            constexpr int ROWS_PT = N > kXThreads ? N / kXThreads : 1;
+            constexpr int COLS_PT = (kXTileBytes / 8 / kXThreads) / ROWS_PT;
+#pragma unroll
+            for (int rr = 0; rr < ROWS_PT; rr++) {
+                const int row = N > kXThreads ? tid + rr * kXThreads : tid % N;
+                const int c0 = N > kXThreads ? 0 : (tid / N) * COLS_PT;
+                const int kx = kval_x(row, N);
+                const uint32_t kx2 = (uint32_t)(kx * kx);
+                int cb = p.nrbins;  // sentinel: no mode yet
+                uint32_t lo = 0, hi = 0;
+                float acc = 0.f;
+#pragma unroll
+                for (int cc = 0; cc < COLS_PT; cc++) {
+                    const int r2 = cols[c0 + cc].r2;
+                    if (r2 < 0)
+                        continue;
+                    const uint32_t kk2 = kx2 + (uint32_t)r2;
+                    const float val = vals[(c0 + cc) * (N + 1) + row];
+                    if (kk2 >= hi || kk2 < lo) {  // also true for the first mode
+                        if (cb < p.nrbins)
+                            atomicAdd(&whist[wid * p.nrbins + cb], acc);
+                        cb = bin_of(kk2, thr, p.nrbins, p.bpu_half);
+                        lo = thr[cb];
+                        hi = thr[cb + 1];
+                        acc = 0.f;
+                    }
+                    acc += val;
+                }
+                // Segmented scan over the lanes' open bins (the warp's rows lie
+                // in one half of the axis, so the bins are monotone across it).
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int ku = __shfl_up_sync(0xffffffffu, cb, o);
+                    const float x = __shfl_up_sync(0xffffffffu, acc, o);
+                    if (lane >= o && ku == cb)
+                        acc += x;
+                }
+                const int kd = __shfl_down_sync(0xffffffffu, cb, 1);
+                if (cb < p.nrbins && (lane == 31 || kd != cb))
+                    atomicAdd(&whist[wid * p.nrbins + cb], acc);
+            }
+            __syncthreads();
+            for (int bb = tid; bb < p.nrbins; bb += kXThreads) {
+                float s = 0.f;
+                for (int w = 0; w < kXThreads / 32; w++) {
+                    s += whist[w * p.nrbins + bb];
+                    whist[w * p.nrbins + bb] = 0.f;
+                }
+                chist[bb] += (double)s;
+            }
+        }
+    }
+    if (tid == 0)
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete
+    if (BIN) {
+        __syncthreads();
+        for (int bb = tid; bb < p.nrbins; bb += kXThreads)
+            p.partial[(size_t)blockIdx.x * p.nrbins + bb] = chist[bb];
+    }
+    timeouts = __reduce_add_sync(0xffffffffu, timeouts);
+    if (lane == 0 && timeouts)
+        atomicAdd(&st->timeouts, (unsigned long long)timeouts);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)f;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+int xfft_tz(int dims)
+{
+    return kXTileBytes / 8 / dims;
+}
+
+size_t xfft_smem(int dims, int nrbins)
+{
+    const int tz = xfft_tz(dims);
+    size_t s = 2 * (size_t)kXTileBytes + sizeof(float2) * dims + sizeof(float) * dims +
+               sizeof(ColInfo) * tz;
+    if (nrbins > 0) {
+        s += sizeof(float) * tz * (dims + 1);
+        s = (s + 15) & ~(size_t)15;
+        s += sizeof(float) * (kXThreads / 32) * nrbins;
+        s = (s + 15) & ~(size_t)15;
+        s += sizeof(double) * nrbins + sizeof(uint32_t) * (nrbins + 1);
+    }
+    return s;
+}
+
+}  // namespace
+
+bool xfft_supported(int dims)
+{
+    return dims >= 64 && dims <= 1024 && (dims & (dims - 1)) == 0 && encode_fn() != nullptr;
+}
+
+bool xfft_bin_supported(int dims, int nrbins)
+{
+    return xfft_supported(dims) && nrbins >= 1 && nrbins <= kXMaxBins &&
+           xfft_smem(dims, nrbins) <= 227 * 1024;
+}
+
+void xfft_twiddles(int dims, std::vector<float> *out)
+{
+    out->resize(2 * (size_t)dims);
+    const double pi = 3.14159265358979323846;
+    for (int m = 0; m < dims; m++) {
+        const double a = -2.0 * pi * (double)m / (double)dims;
+        (*out)[2 * (size_t)m] = (float)std::cos(a);
+        (*out)[2 * (size_t)m + 1] = (float)std::sin(a);
+    }
+}
+
+cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
+                      const XfftBin *bin, int num_sms, DeviceStatus *dstat, cudaStream_t stream,
+                      int64_t *launches)
+{
+    EncodeTiledFn enc = encode_fn();
+    if (!enc)
+        return cudaErrorNotSupported;
+    const int n = g.dims;
+    XParams p;
+    p.dims = n;
+    p.hc = g.hc;
+    p.tz = xfft_tz(n);
+    {
+        int l = 0;
+        while ((1 << l) < n)
+            l++;
+        p.log2n = l;
+        p.n8 = (l % 3 == 0) ? l / 3 - 1 : l / 3;  // the last stage is read separately
+    }
+    p.ncols = n * g.hc;
+    p.tiles_per_field = (p.ncols + p.tz - 1) / p.tz;
+    p.ntiles = p.tiles_per_field * nbatch;
+    p.box_rows = std::min(n, 256);
+    p.tw = tw;
+    p.nrbins = bin ? bin->nrbins : 0;
+    p.bpu_half = bin ? bin->bpu_half : 0.f;
+    p.thr = bin ? bin->thr : nullptr;
+    p.iw = bin ? bin->iw : nullptr;
+    p.corner = bin ? bin->corner : nullptr;
+    p.partial = bin ? bin->partial : nullptr;
+
+    CUtensorMap map;
+    const cuuint64_t gdim[2] = {(cuuint64_t)2 * p.ncols, (cuuint64_t)n * nbatch};
+    const cuuint64_t gstride[1] = {(cuuint64_t)p.ncols * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * p.tz), (cuuint32_t)p.box_rows};
+    const cuuint32_t estride[2] = {1, 1};
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, grids, gdim, gstride, box, estride,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const int ctas = std::min(p.ntiles, num_sms * kXCtasPerSm);
+    const size_t smem = xfft_smem(n, p.nrbins);
+    void (*kern)(const CUtensorMap, XParams, DeviceStatus *) = nullptr;
+#define GENPK_XFFT_PICK(NN)                                   \
+    case NN:                                                  \
+        kern = bin ? k_xfft<NN, true> : k_xfft<NN, false>;    \
+        break;
+    switch (n) {
+        GENPK_XFFT_PICK(64)
+        GENPK_XFFT_PICK(128)
+        GENPK_XFFT_PICK(256)
+        GENPK_XFFT_PICK(512)
+        GENPK_XFFT_PICK(1024)
+    default:
+        return cudaErrorNotSupported;
+    }
+#undef GENPK_XFFT_PICK
+    cudaError_t err;
+    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem)) != cudaSuccess)
+        return err;
+    kern<<<ctas, kXThreads, smem, stream>>>(map, p, dstat);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+int xfft_bin_ctas(int dims, int nbatch, int num_sms)
+{
+    const int tz = xfft_tz(dims);
+    const int tiles = (dims * (dims / 2 + 1) + tz - 1) / tz * nbatch;
+    return std::min(tiles, num_sms * kXCtasPerSm);
+}
+
+}  // namespace genpk

@@ -187,6 +187,17 @@ int genpk_set_deposit_engine(genpk_ctx *ctx, int engine);
 /* Engine the most recent deposit pass used (GENPK_ENGINE_SORTED or _WINDOW). */
 int genpk_last_deposit_engine(const genpk_ctx *ctx);
 
+/* Forward-FFT path (replaces the driver-owned FFTW plan, gen-pk.cpp:186-193,233).
+ *  AUTO (default): for power-of-two N in [64, 1024], a batched 2-D cuFFT R2C
+ *          over the x-planes, then the library's own x-axis pass, which also
+ *          bins a single auto spectrum in the same read of the spectrum; other
+ *          N use CUFFT3D.
+ *  CUFFT3D: one 3-D cuFFT R2C, then the binning kernel.
+ * Both leave the same half-complex spectrum in the grid. */
+#define GENPK_FFT_AUTO 0
+#define GENPK_FFT_CUFFT3D 1
+int genpk_set_fft_mode(genpk_ctx *ctx, int mode);
+
 /* Number of kernels the library launched on ctx since creation. */
 int64_t genpk_kernel_launches(const genpk_ctx *ctx);
 

@@ -446,6 +446,40 @@ def test_uniform_and_variable_mass_chunks_into_one_grid(gp):
         grid_close(ctx.read_field(0), ref)
 
 
+@pytest.mark.parametrize("dims", [64, 128, 256, 512])
+def test_fft_paths_agree(gp, dims):
+    """The fused path (2-D cuFFT over x-planes, own x-axis pass binning the
+    auto spectrum in the same read) against 3-D cuFFT + the binning kernel:
+    the same spectrum is left in the grid (a cross spectrum of two copies
+    binned from it equals the fused auto spectrum) and the bins agree."""
+    from genpk_gb300 import synth
+    box, nrbins = 1000.0, 48
+    pos = synth.zeldovich(min(dims, 128), box, seed=21)
+    m = O.total_mass(len(pos), None, 1.0)
+    out = {}
+    with gp.Context(dims, nrbins, nfields=2) as ctx:
+        for mode in (gp.api.FFT_AUTO, gp.api.FFT_CUFFT3D):
+            ctx.set_fft_mode(mode)
+            for f in (0, 1):
+                ctx.zero(f)
+                ctx.set_engine(gp.api.ENGINE_SORTED)
+                ctx.deposit(f, box, pos, None, 1.0)
+            p, c, _ = ctx.power(0, 0, m, m)      # fused when mode is AUTO
+            x, _, _ = ctx.power(0, 1, m, m)      # from the stored spectra
+            out[mode] = (p, c, x)
+    pa, ca, xa = out[gp.api.FFT_AUTO]
+    p3, c3, x3 = out[gp.api.FFT_CUFFT3D]
+    assert np.array_equal(ca, c3)
+    # two FP32 transforms: their difference is FP32 rounding, well inside the
+    # 1e-5 bar each meets against the FP64 oracle
+    bins_close(pa, p3, ca, rtol=1e-5)
+    bins_close(xa, pa, ca, rtol=2e-6)
+    bins_close(x3, p3, ca, rtol=1e-6)
+    if dims <= 256:
+        pr, cr, _ = O.pk(pos, box, dims, nrbins, None, 1.0, m_norm=m)
+        bins_close(pa, pr, cr)
+
+
 def test_cross_and_multi_spectra(gp):
     from genpk_gb300 import synth
     dims, box, nrbins = 64, 1000.0, 24
