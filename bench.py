@@ -41,9 +41,11 @@ if ROOT not in sys.path:
 METRIC = ("particles/s + ms/spectrum at 512^3 grid vs FP64 oracle; "
           "fwd+adjoint/fwd time ratio")
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-# dram bytes per launch of the deposit pass from an ncu capture of this
-# workload (sum over its kernels); None until a capture is recorded.
-NCU_DEPOSIT_TRAFFIC = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_window_deposit launch,
+# from an ncu capture of the default workload (512^3 Zel'dovich particles onto
+# a 512^3 grid, uniform mass): 2.151 GB read + 0.530 GB written.  Reported only
+# for that workload.
+NCU_WINDOW_TRAFFIC = {"nside": 512, "grid": 512, "bytes": 2.151e9 + 0.530e9}
 
 
 def parse():
@@ -274,22 +276,38 @@ def main():
     stages = {k: v / args.steps for k, v in stages.items()}
     value = npart * world / (ms_step * 1e-3)
 
-    # roofline of the deposit pass (dominant stage) and of the binning kernel
+    # roofline: the dominant kernel (k_window_deposit, or the sorted engine's
+    # whole pass), the deposit pass, and deposit + binning (SURVEY-style)
     pk_, pk_src = peaks()
     peak = float(pk_["hbm_gbs"])
     b_dep, b_bin = algorithmic_bytes(npart, n)
-    t_dep = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_"))) * 1e-3
-    t_bin = stages.get("bin", 0.0) * 1e-3
-    ach_dep = b_dep / t_dep / 1e9
-    ach_bin = b_bin / t_bin / 1e9 if t_bin > 0 else None
     engine = {1: "sorted", 2: "window"}.get(ctx.last_engine, "?")
-    roofline = {"kernel": f"deposit pass ({engine} engine: all its kernels)", "bound": "hbm",
-                "achieved": ach_dep, "peak": peak, "unit": "GB/s", "frac": ach_dep / peak,
-                "peak_source": pk_src, "traffic": NCU_DEPOSIT_TRAFFIC,
+    t_pass = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_"))) * 1e-3
+    # binning time: the fused x-axis FFT + binning kernel when it ran (it also
+    # does the last FFT pass, so this overstates the binning time), else k_bin
+    t_bin = (stages.get("xfft_bin", 0.0) + stages.get("bin", 0.0)) * 1e-3
+    if engine == "window":
+        t_k = stages.get("win_deposit", 0.0) * 1e-3
+        kname = "k_window_deposit"
+        traffic = (NCU_WINDOW_TRAFFIC["bytes"] if (nside, n) == (NCU_WINDOW_TRAFFIC["nside"],
+                                                                  NCU_WINDOW_TRAFFIC["grid"])
+                   else None)
+    else:
+        t_k = t_pass
+        kname = "deposit pass (sorted engine: all its kernels)"
+        traffic = None
+    ach = b_dep / t_k / 1e9
+    ach_bin = b_bin / t_bin / 1e9 if t_bin > 0 else None
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_source": pk_src, "traffic": traffic,
                 "algorithmic_bytes": b_dep,
-                "bin": {"achieved": ach_bin, "frac": (ach_bin / peak) if ach_bin else None,
-                        "algorithmic_bytes": b_bin},
-                "deposit_plus_bin_frac": (b_dep + b_bin) / (t_dep + t_bin) / 1e9 / peak}
+                "note": "achieved = algorithmic bytes (particles read once + grid written once) "
+                        "/ mean CUDA-event time of the kernel; peak = measured copy bandwidth",
+                "deposit_pass": {"ms": t_pass * 1e3, "frac": b_dep / t_pass / 1e9 / peak},
+                "bin": {"kernel": "k_xfft (x-axis FFT pass + binning)" if "xfft_bin" in stages
+                        else "k_bin", "achieved": ach_bin,
+                        "frac": (ach_bin / peak) if ach_bin else None, "algorithmic_bytes": b_bin},
+                "deposit_plus_bin_frac": (b_dep + b_bin) / (t_pass + t_bin) / 1e9 / peak}
 
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
