@@ -6,8 +6,10 @@
 // contiguous run of a few thousand particles occupies a small region of the
 // grid, and the tile sort in deposit.cu is unnecessary work.  This engine:
 //
-//   k_window_deposit  persistent: one CTA per SM walks chunks of kWinChunk
-//     consecutive particles (chunk b, b + gridDim, ...).  Chunks arrive in
+//   k_window_deposit  persistent: one CTA per SM walks chunks of `chunk`
+//     consecutive particles (chunk b, b + gridDim, ...); the chunk length
+//     (4096 down to 512) is the largest whose sampled windows fit, a smaller
+//     chunk leaving more shared memory to the window.  Chunks arrive in
 //     shared memory by bulk asynchronous copy (cp.async.bulk + mbarrier),
 //     double-buffered so the next chunk streams in while this one is worked.
 //     pass A  finds the periodic bounding box of the chunk's cells (cells from
@@ -39,7 +41,6 @@ namespace genpk {
 namespace {
 
 constexpr int kWinThreads = 1024;
-constexpr int kWinChunk = 4096;               // particles per chunk
 constexpr int kWinSmemBytes = 225 * 1024;     // dynamic shared memory per CTA
 constexpr float kPosLimit = 1.0e9f;           // |pos * units| above this: invalid
 
@@ -702,17 +703,17 @@ __global__ void __launch_bounds__(256)
         vol_out[blockIdx.x] = (long long)box.ext[0] * box.ext[1] * box.ext[2];
 }
 
-WinParams make_win_params(const DepositGeom &g, const DepositArgs &a)
+WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk)
 {
     WinParams p;
     const bool var = a.masses != nullptr;
     p.pos = a.pos;
     p.masses = a.masses;
     p.n = a.n;
-    p.chunk = kWinChunk;
-    p.nchunks = (a.n + kWinChunk - 1) / kWinChunk;
-    p.win_off = kWinChunk * (var ? 32 : 24);
-    p.cap = window_cap_cells(var);
+    p.chunk = chunk;
+    p.nchunks = (a.n + chunk - 1) / chunk;
+    p.win_off = chunk * (var ? 32 : 24);
+    p.cap = window_cap_cells(chunk, var);
     p.dims = g.grid.dims;
     p.fdims = (float)g.grid.dims;
     p.inv_dims = 1.f / (float)g.grid.dims;
@@ -733,28 +734,23 @@ WinParams make_win_params(const DepositGeom &g, const DepositArgs &a)
 
 }  // namespace
 
-int window_chunk(int)
+int window_cap_cells(int chunk, bool variable_masses)
 {
-    return kWinChunk;
+    return (kWinSmemBytes - chunk * (variable_masses ? 32 : 24)) / 4;
 }
 
-int window_cap_cells(bool variable_masses)
+cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
+                         long long *vol_dev, int samples, cudaStream_t stream, int64_t *launches)
 {
-    return (kWinSmemBytes - kWinChunk * (variable_masses ? 32 : 24)) / 4;
-}
-
-cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,
-                         int samples, cudaStream_t stream, int64_t *launches)
-{
-    const WinParams p = make_win_params(g, a);
+    const WinParams p = make_win_params(g, a, chunk);
     const int s = (int)std::min<int64_t>(samples, p.nchunks);
     k_window_probe<<<s, 256, 0, stream>>>(p, s, vol_dev);
     (*launches)++;
     return cudaGetLastError();
 }
 
-cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, double *mass_part,
-                                int mass_ctas, int num_sms, DeviceStatus *dstat,
+cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
+                                double *mass_part, int mass_ctas, int num_sms, DeviceStatus *dstat,
                                 cudaStream_t stream, int64_t *launches, StageHook hook,
                                 void *hook_user)
 {
@@ -785,7 +781,7 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, doub
     mark("win_fill");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    const WinParams p = make_win_params(g, a);
+    const WinParams p = make_win_params(g, a, chunk);
     if (p.nchunks > 0) {
         const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
         const int smem = p.win_off + 4 * p.cap;

@@ -32,6 +32,7 @@ constexpr int kMaxStages = 64;
 // Below this many particles a pass always uses the sorted engine.
 constexpr int64_t kWindowMinParticles = (int64_t)1 << 20;
 constexpr int64_t kZeroCopyMinParticles = (int64_t)1 << 20;
+constexpr double kWindowMaxCellsPerParticle = 64.0;
 
 struct Pending {
     bool active = false;
@@ -287,27 +288,44 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     StageHook hook = (ctx->flags & GENPK_FLAG_TIMING) ? deposit_hook : nullptr;
 
     int engine = ctx->engine;
-    if (engine == GENPK_ENGINE_AUTO) {
+    int chunk = kWindowChunks[0];
+    if (engine == GENPK_ENGINE_WINDOW || (engine == GENPK_ENGINE_AUTO && n >= kWindowMinParticles)) {
         // Spatially coherent order (most snapshot layouts) -> window engine;
-        // anything else -> sorted engine.  Decided on a sample of chunks.
-        engine = GENPK_ENGINE_SORTED;
-        if (n >= kWindowMinParticles) {
-            const int samples = 64;
-            GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)samples));
-            GENPK_CUDA(window_probe(g, a, ctx->d_probe, samples, ctx->stream, &ctx->launches));
-            long long vol[64];
-            const int64_t chunks = (n + window_chunk(g.grid.dims) - 1) / window_chunk(g.grid.dims);
-            const int got = (int)std::min<int64_t>(samples, chunks);
-            GENPK_CUDA(cudaMemcpyAsync(vol, ctx->d_probe, sizeof(long long) * got,
-                                       cudaMemcpyDeviceToHost, ctx->stream));
-            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        // anything else -> sorted engine.  Decided on a sample of chunks for
+        // each chunk length: the largest length whose windows fit (a smaller
+        // chunk leaves more shared memory to the window) and whose windows
+        // stay small per particle (the flush visits every window cell).
+        const int samples = 64, nq = (int)(sizeof(kWindowChunks) / sizeof(kWindowChunks[0]));
+        GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)samples * nq));
+        for (int q = 0; q < nq; q++)
+            GENPK_CUDA(window_probe(g, a, kWindowChunks[q], ctx->d_probe + (size_t)q * samples,
+                                    samples, ctx->stream, &ctx->launches));
+        long long vol[4 * 64];
+        GENPK_CUDA(cudaMemcpyAsync(vol, ctx->d_probe, sizeof(long long) * samples * nq,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        int best = -1;
+        for (int q = 0; q < nq && best < 0; q++) {
+            const int c = kWindowChunks[q];
+            const int got = (int)std::min<int64_t>(samples, (n + c - 1) / c);
+            const long long cap = window_cap_cells(c, masses != nullptr);
             int fit = 0;
-            for (int i = 0; i < got; i++)
-                fit += vol[i] <= (long long)(0.9 * window_cap_cells(masses != nullptr)) ? 1 : 0;
-            if (got > 0 && fit * 10 >= got * 9)
-                engine = GENPK_ENGINE_WINDOW;
+            double cells = 0.0;
+            for (int i = 0; i < got; i++) {
+                fit += vol[q * samples + i] <= (long long)(0.9 * cap) ? 1 : 0;
+                cells += (double)vol[q * samples + i];
+            }
+            if (got > 0 && fit * 10 >= got * 9 &&
+                cells / ((double)got * c) <= kWindowMaxCellsPerParticle)
+                best = q;
         }
+        if (engine == GENPK_ENGINE_AUTO)
+            engine = best >= 0 ? GENPK_ENGINE_WINDOW : GENPK_ENGINE_SORTED;
+        if (best >= 0)
+            chunk = kWindowChunks[best];
     }
+    if (engine == GENPK_ENGINE_AUTO)  // too few particles to judge the order
+        engine = GENPK_ENGINE_SORTED;
     if (host_mapped && engine != GENPK_ENGINE_WINDOW) {
         // The sorted engine reads positions twice: copy them over once instead.
         GENPK_TRY(ensure_stage(ctx, n));
@@ -329,7 +347,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         size_t mp = (size_t)s.mass_part_cap;
         GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)mass_ctas));
         s.mass_part_cap = (int)mp;
-        GENPK_CUDA(deposit_window_pass(g, a, s.mass_part, mass_ctas, ctx->num_sms,
+        GENPK_CUDA(deposit_window_pass(g, a, chunk, s.mass_part, mass_ctas, ctx->num_sms,
                                        ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
     } else {
         const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);

@@ -108,14 +108,15 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
                          int64_t *launches, StageHook hook, void *hook_user);
 
 // Window engine (deposit_window.cu) for spatially coherent particle order.
-int window_chunk(int dims);                   // particles per chunk
-int window_cap_cells(bool variable_masses);  // shared window capacity in cells
-// Box volume (cells) of `samples` evenly spread chunks, written to vol_dev.
-cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, long long *vol_dev,
-                         int samples, cudaStream_t stream, int64_t *launches);
+constexpr int kWindowChunks[4] = {4096, 2048, 1024, 512};  // chunk lengths tried, largest first
+// Shared window capacity in cells for a chunk length.
+int window_cap_cells(int chunk, bool variable_masses);
+// Window volume (cells) of `samples` evenly spread chunks, written to vol_dev.
+cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
+                         long long *vol_dev, int samples, cudaStream_t stream, int64_t *launches);
 // One window-engine pass; mass_part needs mass_ctas doubles (variable masses).
-cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, double *mass_part,
-                                int mass_ctas, int num_sms, DeviceStatus *dstat,
+cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
+                                double *mass_part, int mass_ctas, int num_sms, DeviceStatus *dstat,
                                 cudaStream_t stream, int64_t *launches, StageHook hook,
                                 void *hook_user);
 

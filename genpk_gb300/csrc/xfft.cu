@@ -566,9 +566,11 @@ size_t xfft_smem(int dims, int nrbins)
 
 }  // namespace
 
+// Used for N <= 512: at N = 1024 the tile is 4 columns wide (32-byte rows)
+// and the 3-D cuFFT + binning path was faster (6.6 ms against 10.3 ms).
 bool xfft_supported(int dims)
 {
-    return dims >= 64 && dims <= 1024 && (dims & (dims - 1)) == 0 && encode_fn() != nullptr;
+    return dims >= 64 && dims <= 512 && (dims & (dims - 1)) == 0 && encode_fn() != nullptr;
 }
 
 bool xfft_bin_supported(int dims, int nrbins)

@@ -188,7 +188,7 @@ int genpk_set_deposit_engine(genpk_ctx *ctx, int engine);
 int genpk_last_deposit_engine(const genpk_ctx *ctx);
 
 /* Forward-FFT path (replaces the driver-owned FFTW plan, gen-pk.cpp:186-193,233).
- *  AUTO (default): for power-of-two N in [64, 1024], a batched 2-D cuFFT R2C
+ *  AUTO (default): for power-of-two N in [64, 512], a batched 2-D cuFFT R2C
  *          over the x-planes, then the library's own x-axis pass, which also
  *          bins a single auto spectrum in the same read of the spectrum; other
  *          N use CUFFT3D.

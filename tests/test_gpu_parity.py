@@ -354,6 +354,20 @@ def test_auto_engine_choice(gp):
         assert ctx.last_engine == gp.api.ENGINE_SORTED
 
 
+def test_sparse_lattice_picks_a_shorter_window_chunk(gp):
+    """128^3 lattice particles on a 256^3 grid (two cells per lattice
+    spacing): a 4096-particle chunk's window does not fit, a 1024-particle
+    chunk's does, so the automatic choice is still the window engine."""
+    from genpk_gb300 import synth
+    dims, box = 256, 1000.0
+    pos = synth.zeldovich(128, box, seed=17)
+    with gp.Context(dims, 16) as ctx:
+        ctx.deposit(0, box, pos, None, 1.0)
+        ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        grid_close(ctx.read_field(0), O.deposit(pos, box, dims, None, 1.0), tol=1e-6)
+
+
 def test_window_and_sorted_engines_agree(gp):
     """Same particles, both engines, accumulate semantics across passes."""
     from genpk_gb300 import synth
