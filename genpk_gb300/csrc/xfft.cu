@@ -234,11 +234,30 @@ __device__ __forceinline__ void stage_read(const float2 *tile, const float2 *tw,
     for (int m = 0; m < PER; m++) {
         const int j = g + m * (N / 8);
         const int k = j & (NS - 1);
+        float2 w[R];  // w[r] = tw[k * TSTEP * r]
+        if (NS > 1) {
+            if (R == 8) {
+                // three table reads, the other four by products (a few ulp)
+                const float2 w1 = tw[k * TSTEP], w2 = tw[2 * k * TSTEP], w4 = tw[4 * k * TSTEP];
+                const float2 w3 = cmul(w1, w2);
+                w[1] = w1;
+                w[2] = w2;
+                w[3] = w3;
+                w[4] = w4;
+                w[5] = cmul(w1, w4);
+                w[6] = cmul(w2, w4);
+                w[7] = cmul(w3, w4);
+            } else {
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    w[r] = tw[k * TSTEP * r];
+            }
+        }
 #pragma unroll
         for (int r = 0; r < R; r++) {
             float2 x = tile[(j + r * NB) * TZ + c];
             if (NS > 1 && r > 0)
-                x = cmul(x, tw[k * TSTEP * r]);
+                x = cmul(x, w[r]);
             v[m * R + r] = x;
         }
         dft<R>(&v[m * R]);
