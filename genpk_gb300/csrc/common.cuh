@@ -109,88 +109,114 @@ __device__ __forceinline__ f2sum f2_mul(f2sum a, f2sum b)
     return renorm(p, e);
 }
 
-// 1 - 2d for one axis of a particle, d = x - floor(x), x = p*units, as a float
-// pair good to ~2^-44.  The carry decisions repeat split_cell's exactly, so the
-// value belongs to the same cell split_cell returns.
-__device__ __forceinline__ f2sum one_minus_2frac(float p, float uh, float ul)
-{
-    const float xh = __fmul_rn(p, uh);
-    const float xe = fmaf(p, uh, -xh);
-    const float xl = fmaf(p, ul, xe);
-    const float f = floorf(xh);
-    f2sum d = two_sum(__fsub_rn(xh, f), xl);
-    if (d.hi < 0.f)
-        d = f2_add(d, 1.f);
-    if (d.hi >= 1.f)
-        d = f2_add(d, -1.f);
-    const f2sum u = two_sum(1.f, -2.f * d.hi);
-    return renorm(u.hi, __fsub_rn(u.lo, 2.f * d.lo));
-}
-
-// One axis of a particle in full: the wrapped cell and FP32 fraction exactly as
-// split_cell computes them, plus what the exact corner-mode term needs:
-// u = 1 - 2*(xh - floor) for the final cell (exact in FP32 for xh >= 1; one
-// rounding below) and xl, the low part of x = xh + xl, so that
-// 1 - 2d = u - 2*xl exactly.
-struct AxisSplit {
+// One axis split to a 28-bit fixed-point fraction, from the exact two-product
+// x = xh + xl (no FP32 rounding of the fraction): q = round((xh - floor(xh) +
+// xl) * 2^28) with at most 2^-28 error, the cell moved when the carry leaves
+// [0, 1).  u = 1 - 2*(xh - floor) (moved with the cell) and xl feed the exact
+// corner-mode term (1 - 2d = u - 2 xl exactly).  FP32 fractions are not enough: a smooth
+// lattice's faintest high-k bins moved by 2.5e-5 with FP32 fractions and by
+// 2.5e-7 with 32-bit ones in an emulation at 128^3.
+struct AxisQ {
     int cell;
-    float frac;
+    uint32_t q;  // fraction * 2^28, in [0, 2^28)
     float u;
     float xl;
 };
 
-__device__ __forceinline__ AxisSplit split_axis(float p, float uh, float ul, int dims)
+constexpr int kFracBits = 28;
+constexpr uint32_t kFracOne = 1u << kFracBits;
+
+__device__ __forceinline__ AxisQ split_q28(float p, float uh, float ul, int dims)
 {
     const float xh = __fmul_rn(p, uh);
     const float xe = fmaf(p, uh, -xh);
     const float xl = fmaf(p, ul, xe);
     const float f = floorf(xh);
     const float a = __fsub_rn(xh, f);
-    float d = __fadd_rn(a, xl);
-    float u = fmaf(-2.f, a, 1.f);
+    // a * 2^28 is exact (and an integer when xh >= 1); xl * 2^28 is small
+    int q = __float2int_rn(a * 268435456.f) + __float2int_rn(xl * 268435456.f);
+    // 1 - 2a is exact in FP32 for |xh| >= 1 (a is then a multiple of 2^-23);
+    // below, its rounding error is folded into xl so that u - 2 xl stays exact
+    float u = __fsub_rn(1.f, __fmul_rn(2.f, a));
+    float xlu = xl;
+    if (fabsf(xh) < 1.f) {
+        const f2sum t = two_sum(1.f, -2.f * a);
+        u = t.hi;
+        xlu = __fsub_rn(xl, 0.5f * t.lo);
+    }
     int fi = (int)f;
-    if (d < 0.f) {
-        d = __fadd_rn(d, 1.f);
+    if (q < 0) {
+        q += (int)kFracOne;
         fi -= 1;
         u = __fsub_rn(u, 2.f);
     }
-    if (d >= 1.f) {
-        d = __fsub_rn(d, 1.f);
+    if (q >= (int)kFracOne) {
+        q -= (int)kFracOne;
         fi += 1;
         u = __fadd_rn(u, 2.f);
     }
+    q = min(max(q, 0), (int)kFracOne - 1);  // far positions (|x| > 2^22 cells) only
     if ((unsigned)fi >= (unsigned)dims) {
         fi %= dims;
         if (fi < 0)
             fi += dims;
     }
-    return {fi, d, u, xl};
+    return {fi, (uint32_t)q, u, xlu};
+}
+
+// The CIC weights of one particle in 2^-s mass units, shared by both deposit
+// engines so that they produce identical integer cell sums.  Factors per axis:
+// 2^28 - q (lower cell) and q (upper), so f / 2^28 is the CIC factor; the
+// particle's mass is mant * 2^(e - 150) (mant with its implicit bit) and
+// dsh = emax - e for the pass's largest exponent emax, with s = 154 - emax.
+//   pair (x, y):  P = rnd(fx fy / 2^26)                 <= 2^30
+//   z with mass:  Z = rnd(rnd(fz mant / 2^23) / 2^dsh)  <= 2^29
+//   corner:       W = rnd(P Z / 2^31)                   <= 2^28
+// so W = prod(f / 2^28) * m * 2^s to within ~2 units.  rnd is to nearest: a
+// truncation bias depends on the fraction, and on a lattice that follows the
+// displacement field.  Each rnd(a b / 2^32) is one 32x32->64 multiply plus a
+// 64-bit add; the operands are pre-scaled so the binary point sits at bit 32.
+__device__ __forceinline__ uint32_t mul_rnd_hi(uint32_t a, uint32_t b)
+{
+    return (uint32_t)(((unsigned long long)a * b + 0x80000000ull) >> 32);
+}
+
+__device__ __forceinline__ uint32_t pair_w(uint32_t fx, uint32_t fy)
+{
+    return mul_rnd_hi(fx << 3, fy << 3);  // fx, fy <= 2^28: fx fy 2^6 / 2^32
+}
+
+__device__ __forceinline__ uint32_t z_mass(uint32_t fz, uint32_t mant, int dsh)
+{
+    const uint32_t z = mul_rnd_hi(fz << 3, mant << 6);  // fz mant 2^9 / 2^32
+    if (dsh == 0)
+        return z;
+    if (dsh > 31)
+        return 0u;
+    return (uint32_t)(((unsigned long long)z + (1ull << (dsh - 1))) >> dsh);
+}
+
+__device__ __forceinline__ uint32_t corner_w(uint32_t p, uint32_t z)
+{
+    return mul_rnd_hi(p, z << 1);  // p z 2 / 2^32 = p z / 2^31
 }
 
 // prod_a (1 - 2 d_a) = prod_a (u_a - 2 xl_a) as a float pair: the product of
-// the u's with two-product steps (error ~2^-47) plus the first-order xl terms
-// in FP32 (second-order terms are ~2^-48 and dropped).
-__device__ __forceinline__ f2sum corner_factor(const AxisSplit &x, const AxisSplit &y,
-                                               const AxisSplit &z)
+// the u's with two-product steps (relative error ~2^-47), then the first-,
+// second- and third-order xl terms in FP32.  All orders are kept: xl holds
+// p * (units - fl(units)), up to x * 2^-24, and dropping the second order left
+// a coherent error of ~1e-4 in the single-mode last bin of a 128^3 lattice.
+__device__ __forceinline__ f2sum corner_factor_q(const AxisQ &x, const AxisQ &y, const AxisQ &z)
 {
     const float p = __fmul_rn(x.u, y.u);
     const float pl = fmaf(x.u, y.u, -p);
     const float q = __fmul_rn(p, z.u);
     const float ql = fmaf(p, z.u, -q) + pl * z.u;
-    const float corr = -2.f * (x.xl * (y.u * z.u) + y.xl * (x.u * z.u) + z.xl * (x.u * y.u));
-    return {q, ql + corr};
-}
-
-// 24-bit fixed point of a fraction in [0,1); exact in FP32 on the way back.
-__device__ __forceinline__ uint32_t frac_to_q24(float d)
-{
-    uint32_t q = (uint32_t)(d * 16777216.f);
-    return q > 0xFFFFFFu ? 0xFFFFFFu : q;
-}
-
-__device__ __forceinline__ float q24_to_frac(uint32_t w)
-{
-    return (float)(w & 0xFFFFFFu) * (1.f / 16777216.f);
+    const float yz = y.u * z.u, xz = x.u * z.u, xy = x.u * y.u;
+    const float t1 = x.xl * yz + y.xl * xz + z.xl * xy;
+    const float t2 = x.xl * y.xl * z.u + x.xl * z.xl * y.u + y.xl * z.xl * x.u;
+    const float t3 = x.xl * y.xl * z.xl;
+    return {q, ql + ((-2.f * t1 + 4.f * t2) - 8.f * t3)};
 }
 
 __device__ __forceinline__ bool finite3(float a, float b, float c)

@@ -4,7 +4,7 @@
 // by one CTA per tile accumulating in shared memory:
 //
 //   k_sort_hist       each CTA owns a contiguous particle range; it computes
-//                     every particle's cell (two-product split, split_cell),
+//                     every particle's cell (two-product split, split_q28),
 //                     counts particles per tile in a shared histogram and
 //                     writes the histogram row to scratch; it also sums the
 //                     masses (Kahan, FP32 -> FP64) and takes their maximum.
@@ -14,7 +14,7 @@
 //                     mean in fixed point.
 //   k_sort_offsets    per tile: histogram rows -> each CTA's first slot.
 //   k_sort_scatter    re-reads the range and writes every particle, packed as
-//                     tile-local cell + 24-bit fraction per axis (+ mass bits),
+//                     tile-local cell + 28-bit fraction per axis (+ mass bits),
 //                     to its slot.
 //   (grids with more tiles than a shared histogram holds run both kernels with
 //    global counters instead.)
@@ -74,21 +74,22 @@ constexpr int kSortThreads = 512;
 constexpr int kSortUnroll = 4;
 constexpr uint32_t kNoTile = 0xffffffffu;
 
-// Cell and tile of one particle; false for a particle that must be skipped.
+// Cell, 28-bit fraction and tile of one particle (split_q28, as the window
+// engine splits it); false for a particle that must be skipped.
 __device__ __forceinline__ bool particle_cell(const SortParams &p, float x, float y, float z,
-                                              float m, int c[3], float d[3], uint32_t &tile)
+                                              float m, AxisQ a[3], uint32_t &tile)
 {
     if (!finite3(x, y, z) || !isfinite(m))
         return false;
     const float lim = 1.0e9f;
     if (fabsf(x * p.uh) > lim || fabsf(y * p.uh) > lim || fabsf(z * p.uh) > lim)
         return false;
-    split_cell(x, p.uh, p.ul, p.dims, c[0], d[0]);
-    split_cell(y, p.uh, p.ul, p.dims, c[1], d[1]);
-    split_cell(z, p.uh, p.ul, p.dims, c[2], d[2]);
-    tile = ((uint32_t)(c[0] >> p.lx) * (uint32_t)p.nty + (uint32_t)(c[1] >> p.ly)) *
+    a[0] = split_q28(x, p.uh, p.ul, p.dims);
+    a[1] = split_q28(y, p.uh, p.ul, p.dims);
+    a[2] = split_q28(z, p.uh, p.ul, p.dims);
+    tile = ((uint32_t)(a[0].cell >> p.lx) * (uint32_t)p.nty + (uint32_t)(a[1].cell >> p.ly)) *
                (uint32_t)p.ntz +
-           (uint32_t)(c[2] >> p.lz);
+           (uint32_t)(a[2].cell >> p.lz);
     return true;
 }
 
@@ -174,9 +175,8 @@ __global__ void __launch_bounds__(kSortThreads)
     for_each_warp_batch(p, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
         if (in) {
-            int c[3];
-            float d[3];
-            if (particle_cell(p, v[0], v[1], v[2], m, c, d, t)) {
+            AxisQ a[3];
+            if (particle_cell(p, v[0], v[1], v[2], m, a, t)) {
                 const float y = m - mc;  // Kahan-compensated FP32 sum of masses
                 const float s = msum + y;
                 mc = (s - msum) - y;
@@ -330,13 +330,15 @@ __global__ void k_sort_offsets(uint32_t *__restrict__ hist, int nsort, int ntile
     }
 }
 
-__device__ __forceinline__ uint4 pack_particle(const int c[3], const float d[3], float m,
-                                               uint32_t mx, uint32_t my, uint32_t mz)
+// Packed particle: per axis (tile-local cell << 28) | 28-bit fraction (tiles
+// of at most 16 cells per edge), then the mass bits.
+__device__ __forceinline__ uint4 pack_particle(const AxisQ a[3], float m, uint32_t mx, uint32_t my,
+                                               uint32_t mz)
 {
     uint4 w;
-    w.x = (((uint32_t)c[0] & mx) << 24) | frac_to_q24(d[0]);
-    w.y = (((uint32_t)c[1] & my) << 24) | frac_to_q24(d[1]);
-    w.z = (((uint32_t)c[2] & mz) << 24) | frac_to_q24(d[2]);
+    w.x = (((uint32_t)a[0].cell & mx) << kFracBits) | a[0].q;
+    w.y = (((uint32_t)a[1].cell & my) << kFracBits) | a[1].q;
+    w.z = (((uint32_t)a[2].cell & mz) << kFracBits) | a[2].q;
     w.w = __float_as_uint(m);
     return w;
 }
@@ -344,7 +346,7 @@ __device__ __forceinline__ uint4 pack_particle(const int c[3], const float d[3],
 // Writes every particle of the CTA's range to its slot in tile order.  Shared
 // cursors start at this CTA's offsets (GLOBAL = false) or global cursors are
 // used directly (GLOBAL = true).  Lanes in the same tile take consecutive slots
-// from one atomic.  Packed particle: per axis (tile-local cell << 24) | 24-bit
+// from one atomic.  Packed particle: per axis (tile-local cell << 28) | 28-bit
 // fraction; w = mass bits.
 //
 // On even grids it also sums the corner mode k = (N/2, N/2, N/2) of the CIC
@@ -376,9 +378,9 @@ __global__ void __launch_bounds__(kSortThreads)
     f2sum alt = {0.f, 0.f};
     for_each_warp_batch(p, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
-        int c[3] = {0, 0, 0};
-        float d[3] = {0.f, 0.f, 0.f};
-        if (in && !particle_cell(p, v[0], v[1], v[2], m, c, d, t))
+        AxisQ a[3];
+        a[0] = a[1] = a[2] = AxisQ{0, 0u, 1.f, 0.f};
+        if (in && !particle_cell(p, v[0], v[1], v[2], m, a, t))
             t = kNoTile;
         const unsigned peers = __match_any_sync(0xffffffffu, t);
         const int leader = __ffs(peers) - 1;
@@ -387,13 +389,13 @@ __global__ void __launch_bounds__(kSortThreads)
             slot0 = atomicAdd(&cur[t], (uint32_t)__popc(peers));
         slot0 = __shfl_sync(0xffffffffu, slot0, leader);
         if (t != kNoTile) {
-            sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = pack_particle(c, d, m, mx, my, mz);
+            sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = pack_particle(a, m, mx, my, mz);
             if (p.corner) {
                 const float mm = (p.masses ? m : p.umass) * mscale;
-                f2sum u = f2_mul(one_minus_2frac(v[0], p.uh, p.ul), one_minus_2frac(v[1], p.uh, p.ul));
-                u = f2_mul(u, one_minus_2frac(v[2], p.uh, p.ul));
-                u = f2_mul(u, f2sum{mm, 0.f});
-                if ((c[0] + c[1] + c[2]) & 1)
+                f2sum u = corner_factor_q(a[0], a[1], a[2]);
+                const float h = __fmul_rn(u.hi, mm);
+                u = f2sum{h, fmaf(u.hi, mm, -h) + u.lo * mm};
+                if ((a[0].cell + a[1].cell + a[2].cell) & 1)
                     u = f2sum{-u.hi, -u.lo};
                 alt = f2_add2(alt, u);
             }
@@ -540,22 +542,6 @@ __device__ __forceinline__ long long acc_get(const unsigned *lo, const unsigned 
     return (long long)(((unsigned long long)hi[idx] << 32) | lo[idx]);
 }
 
-// CIC corner weight in 2^-s mass units from the 24-bit fractions, integer
-// instructions only.  a, b, c are the per-axis factors (2^24 - q or q, so
-// a*b*c / 2^72 is the product of the CIC factors); the particle's mass is
-// mant * 2^(e - 23) and sh = 54 - s - e.  Intermediate truncations keep
-// ~31 bits; the result is rounded to nearest.
-__device__ __forceinline__ unsigned corner_weight(unsigned long long ab, unsigned c, unsigned mant,
-                                                  int sh)
-{
-    const unsigned p2 = (unsigned)(ab >> 17);
-    const unsigned y = (unsigned)(((unsigned long long)p2 * c) >> 24);
-    const unsigned long long z = (unsigned long long)y * mant;
-    if (sh >= 64)
-        return 0u;
-    return (unsigned)((z + (1ull << (sh - 1))) >> sh);
-}
-
 template <int TX, int TY, int TZ, bool VARMASS, bool CLEAN>
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_deposit(TileParams p, const uint4 *__restrict__ sorted,
@@ -577,45 +563,45 @@ __global__ void __launch_bounds__(kTileThreads)
 
     const int s = st->fx_shift;
     const float inv_scale = ldexpf(1.f, -s);
-    // Uniform mass as mantissa and exponent.
+    // Weights in 2^-s mass units with s = 154 - emax (common.cuh pair_w / z_mass /
+    // corner_w, as the window engine computes them).
+    const int emax = 154 - s;
     const unsigned ubits = __float_as_uint(p.mass);
     const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
-    const int ush = 54 - s - (int)((ubits >> 23) & 0xffu) + 127;
+    const int uef = (int)((ubits >> 23) & 0xffu);
     const bool uneg = (ubits >> 31) != 0u;
-    const bool uzero = ((ubits >> 23) & 0xffu) == 0u;
     const uint32_t s0 = tile_start[t], s1 = tile_start[t + 1];
     for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         const uint4 w = sorted[i];
         unsigned mant = umant;
-        int sh = ush;
-        bool neg = uneg, zero = uzero;
+        int ef = uef;
+        bool neg = uneg;
         if (VARMASS) {
             const unsigned mb = w.w;
-            const unsigned ef = (mb >> 23) & 0xffu;
+            ef = (int)((mb >> 23) & 0xffu);
             mant = (mb & 0x7fffffu) | 0x800000u;
-            sh = 54 - s - (int)ef + 127;
             neg = (mb >> 31) != 0u;
-            zero = ef == 0u;  // zero or subnormal mass deposits nothing
         }
-        if (zero)
+        if (ef == 0)  // zero or subnormal mass deposits nothing
             continue;
-        sh = max(sh, 1);
-        const unsigned qx = w.x & 0xffffffu, qy = w.y & 0xffffffu, qz = w.z & 0xffffffu;
-        const unsigned rx = 0x1000000u - qx, ry = 0x1000000u - qy, rz = 0x1000000u - qz;
-        const int base = L::acc_index((int)(w.x >> 24), (int)(w.y >> 24), (int)(w.z >> 24));
+        const int dsh = max(emax - ef, 0);
+        const uint32_t qx = w.x & (kFracOne - 1u), qy = w.y & (kFracOne - 1u),
+                       qz = w.z & (kFracOne - 1u);
+        const uint32_t rx = kFracOne - qx, ry = kFracOne - qy, rz = kFracOne - qz;
+        const int base = L::acc_index((int)(w.x >> kFracBits), (int)(w.y >> kFracBits),
+                                      (int)(w.z >> kFracBits));
         constexpr int DX = L::SY * L::SZ, DY = L::SZ;
-        const unsigned long long a00 = (unsigned long long)rx * ry;  // (x, y) lower corners
-        const unsigned long long a10 = (unsigned long long)qx * ry;
-        const unsigned long long a01 = (unsigned long long)rx * qy;
-        const unsigned long long a11 = (unsigned long long)qx * qy;
-        acc_add(lo, hi, base, corner_weight(a00, rz, mant, sh), neg);
-        acc_add(lo, hi, base + DX, corner_weight(a10, rz, mant, sh), neg);
-        acc_add(lo, hi, base + DY, corner_weight(a01, rz, mant, sh), neg);
-        acc_add(lo, hi, base + DX + DY, corner_weight(a11, rz, mant, sh), neg);
-        acc_add(lo, hi, base + 1, corner_weight(a00, qz, mant, sh), neg);
-        acc_add(lo, hi, base + DX + 1, corner_weight(a10, qz, mant, sh), neg);
-        acc_add(lo, hi, base + DY + 1, corner_weight(a01, qz, mant, sh), neg);
-        acc_add(lo, hi, base + DX + DY + 1, corner_weight(a11, qz, mant, sh), neg);
+        const uint32_t p00 = pair_w(rx, ry), p10 = pair_w(qx, ry), p01 = pair_w(rx, qy),
+                       p11 = pair_w(qx, qy);
+        const uint32_t z0 = z_mass(rz, mant, dsh), z1 = z_mass(qz, mant, dsh);
+        acc_add(lo, hi, base, corner_w(p00, z0), neg);
+        acc_add(lo, hi, base + DX, corner_w(p10, z0), neg);
+        acc_add(lo, hi, base + DY, corner_w(p01, z0), neg);
+        acc_add(lo, hi, base + DX + DY, corner_w(p11, z0), neg);
+        acc_add(lo, hi, base + 1, corner_w(p00, z1), neg);
+        acc_add(lo, hi, base + DX + 1, corner_w(p10, z1), neg);
+        acc_add(lo, hi, base + DY + 1, corner_w(p01, z1), neg);
+        acc_add(lo, hi, base + DX + DY + 1, corner_w(p11, z1), neg);
     }
     __syncthreads();
 
@@ -780,10 +766,11 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
 
 }  // namespace
 
+// Tile edges of at most 16 cells: the packed record keeps 4 bits of tile-local
+// cell beside each 28-bit fraction.
 bool deposit_tile_supported(int tx, int ty, int tz)
 {
-    return (tx == 8 && ty == 8 && tz == 8) || (tx == 16 && ty == 16 && tz == 16) ||
-           (tx == 16 && ty == 16 && tz == 32);
+    return (tx == 8 && ty == 8 && tz == 8) || (tx == 16 && ty == 16 && tz == 16);
 }
 
 TileShape deposit_default_tile(int dims, int64_t n)
@@ -901,9 +888,7 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         return err;
     if (g.tx == 8)
         return launch_tile_kernels<8, 8, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
-    if (g.tz == 16)
-        return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook, hook_user);
-    return launch_tile_kernels<16, 16, 32>(g, a, s, dstat, stream, launches, hook, hook_user);
+    return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook, hook_user);
 }
 
 }  // namespace genpk

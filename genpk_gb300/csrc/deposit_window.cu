@@ -18,20 +18,21 @@
 //             down the global path); an axis the chunk spans completely is
 //             taken whole, with one extra layer for the wrapped CIC corner.
 //             Invalid particles are counted and marked (x := NaN).
-//     pass B  splits every position exactly (split_axis) and adds the eight
-//             CIC weights to the shared window as 28-bit fixed-point integers
-//             (native shared integer atomics; a signed overflow of a window
-//             cell is carried straight to the grid as +-2^32 units).  Pass B
-//             also sums the chunk's share of the exact corner mode.
-//     flush   every non-zero window cell is added to the FP32 grid (16-byte
-//             vector atomics along whole rows) and cleared, so the window is
-//             zero again for the next chunk.
+//     pass B  splits every position exactly (split_q28) and adds the eight
+//             CIC weights (at most 2^28 units each) to the shared window with
+//             native shared integer atomics; a signed overflow of a window
+//             cell becomes a +-1 carry of its grid cell.  Pass B also sums the
+//             chunk's share of the exact corner mode.
+//     flush   every non-zero window cell is added to the pass accumulator
+//             (global integer atomics) and cleared, so the window is zero
+//             again for the next chunk.
 //
-// The grid is first filled with -mean (k_grid_fill / k_grid_add), the pass mean
-// computed in k_window_prep, so the result is mean-subtracted like the sorted
-// engine's.  FP32 atomics into the grid make its low bits depend on summation
-// order; the sorted engine (deposit.cu) is the exact, bit-reproducible
-// alternative.
+// Sums are exact: the window cells and the pass accumulator are integers of
+// 2^-s mass units (the sorted engine's weights, common.cuh pair_w / z_mass /
+// corner_w), the accumulator 32-bit with signed overflows counted in a 16-bit
+// carry per cell; k_window_convert subtracts the fixed-point pass mean and
+// rounds each cell once to FP32.  The grid is therefore bit-identical to the
+// sorted engine's and independent of summation order.
 #include "common.cuh"
 #include "internal.h"
 
@@ -144,12 +145,6 @@ __device__ __forceinline__ float ref_cell(const WinParams &p, float v)
     float r = floorf(v * p.uh);
     r = fmaf(-p.fdims, floorf(r * p.inv_dims), r);
     return (r >= 0.f && r < p.fdims) ? r : 0.f;
-}
-
-// 23-bit fixed point of a fraction d in [0,1): round(d * 2^23), in [0, 2^23].
-__device__ __forceinline__ unsigned frac_q23(float d)
-{
-    return (unsigned)(__float_as_int(fmaf(d, 8388608.f, 8388608.f)) - 0x4B000000);
 }
 
 struct WinBox {
@@ -269,38 +264,58 @@ __device__ __forceinline__ void copy_chunk(const WinParams &p, int64_t c, int cn
         copy_floats(M, p.masses + chunk_first(p, c), cnt);
 }
 
-// Global-path adds of one particle's eight corners (cells c, weights w[k] for
-// corner k = dx | dy << 1 | dz << 2).
-__device__ __noinline__ void global_corners(const WinParams &p, float *grid, const int c[3],
-                                            const float w[8])
+// The pass accumulates exact integers: acc[gi] (32-bit, wrapping) plus 2^32
+// times the signed count in carry[gi >> 1] (16-bit half gi & 1, biased by
+// kCarryBias), for every padded grid index gi.
+constexpr int kCarryBias = 0x8080;  // carry words start as bytes of 0x80
+constexpr int kFlushBatch = 8;      // cells per lane in flight per round trip
+
+// Adds v to one accumulator cell; a signed overflow moves +-1 into its carry.
+__device__ __forceinline__ void acc_add_global(int *acc, unsigned *carry, size_t gi, int v)
 {
-    const int h0 = c[0] + 1 == p.dims ? 0 : c[0] + 1;
-    const int h1 = c[1] + 1 == p.dims ? 0 : c[1] + 1;
-    const int h2 = c[2] + 1 == p.dims ? 0 : c[2] + 1;
+    const int old = atomicAdd(acc + gi, v);
+    const int nw = (int)((unsigned)old + (unsigned)v);
+    if (v > 0 ? nw < old : nw > old)
+        atomicAdd(carry + (gi >> 1), (unsigned)((v > 0 ? 1 : -1) * (1 << (16 * (int)(gi & 1)))));
+}
+
+__device__ __forceinline__ size_t corner_index(const WinParams &p, const int c[3], int k)
+{
+    const int x = (k & 1) ? (c[0] + 1 == p.dims ? 0 : c[0] + 1) : c[0];
+    const int y = (k & 2) ? (c[1] + 1 == p.dims ? 0 : c[1] + 1) : c[1];
+    const int z = (k & 4) ? (c[2] + 1 == p.dims ? 0 : c[2] + 1) : c[2];
+    return cell_index(p.plane, p.row, x, y, z);
+}
+
+// Global-path adds of one particle's eight corners (cells c, signed weights
+// w[k] for corner k = dx | dy << 1 | dz << 2).
+__device__ __noinline__ void global_corners(const WinParams &p, int *acc, unsigned *carry,
+                                            const int c[3], const int w[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        if (w[k] != 0)
+            acc_add_global(acc, carry, corner_index(p, c, k), w[k]);
+}
+
+// Window cells of the corners in `mask` overflowed by `sign`: carry +-1 into
+// their grid cells' carry counts.
+__device__ __noinline__ void carry_corners(const WinParams &p, unsigned *carry, const int c[3],
+                                           unsigned mask, int sign)
+{
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        if (w[k] != 0.f) {
-            const int x = (k & 1) ? h0 : c[0], y = (k & 2) ? h1 : c[1], z = (k & 4) ? h2 : c[2];
-            atomicAdd(grid + cell_index(p.plane, p.row, x, y, z), w[k]);
+        if ((mask >> k) & 1u) {
+            const size_t gi = corner_index(p, c, k);
+            atomicAdd(carry + (gi >> 1), (unsigned)(sign * (1 << (16 * (int)(gi & 1)))));
         }
     }
 }
 
-// Window cells of corners in `mask` overflowed: carry `carry` (+-2^32 window
-// units, as grid units) to their grid cells.
-__device__ __noinline__ void carry_corners(const WinParams &p, float *grid, const int c[3],
-                                           unsigned mask, float carry)
-{
-    float w[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-        w[k] = ((mask >> k) & 1u) ? carry : 0.f;
-    global_corners(p, grid, c, w);
-}
-
 template <bool VARMASS, bool CORNER>
 __global__ void __launch_bounds__(kWinThreads, 1)
-    k_window_deposit(WinParams p, DeviceStatus *st, float *__restrict__ grid)
+    k_window_deposit(WinParams p, DeviceStatus *st, int *__restrict__ acc,
+                     unsigned *__restrict__ carry)
 {
     extern __shared__ __align__(128) unsigned char win_smem[];
     float *pbuf = reinterpret_cast<float *>(win_smem);              // [2][chunk * 3]
@@ -322,13 +337,14 @@ __global__ void __launch_bounds__(kWinThreads, 1)
     }
     __syncthreads();
 
-    // Window units: uniform mass -> 2^-28 * mass; variable -> 2^-s with
-    // s = 154 - (exponent field of the largest |mass|).
-    const unsigned mbits_max = st->max_mass_bits;
-    const int emax = VARMASS ? (int)((mbits_max >> 23) & 0xffu) : 0;
-    const float unit = VARMASS ? ldexpf(1.f, emax - 154) : p.umass * (1.f / 268435456.f);
+    // Weights in 2^-s mass units, s = 154 - emax (common.cuh pair_w / z_mass /
+    // corner_w, as the sorted engine computes them).
+    const int emax = 154 - st->fx_shift;
+    const unsigned ubits = __float_as_uint(p.umass);
+    const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
+    const int uef = (int)((ubits >> 23) & 0xffu);
+    const bool uneg = (ubits >> 31) != 0u;
     const float mscale = ldexpf(1.f, st->fx_shift + 4);
-    const float carry_val = 4294967296.f * unit;
 
     f2sum alt = {0.f, 0.f};
     unsigned bad = 0, timeouts = 0;
@@ -393,24 +409,24 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             if (isnan(x))
                 continue;
             float m = p.umass;
-            unsigned mant7 = 0u;
-            int dsh = 0;
-            bool neg = false;
+            unsigned mant = umant;
+            int ef = uef;
+            bool neg = uneg;
             if (VARMASS) {
                 m = M[j];
                 const unsigned mb = __float_as_uint(m);
-                const int ef = (int)((mb >> 23) & 0xffu);
-                dsh = emax - ef;
-                if (ef == 0 || dsh > 30)  // zero, subnormal or below 2^-30 of the largest
-                    continue;
-                mant7 = ((mb & 0x7fffffu) | 0x800000u) << 7;
+                ef = (int)((mb >> 23) & 0xffu);
+                mant = (mb & 0x7fffffu) | 0x800000u;
                 neg = (mb >> 31) != 0u;
             }
-            const AxisSplit ax = split_axis(x, p.uh, p.ul, p.dims);
-            const AxisSplit ay = split_axis(y, p.uh, p.ul, p.dims);
-            const AxisSplit az = split_axis(z, p.uh, p.ul, p.dims);
+            if (ef == 0)  // zero or subnormal mass deposits nothing
+                continue;
+            const int dsh = max(emax - ef, 0);
+            const AxisQ ax = split_q28(x, p.uh, p.ul, p.dims);
+            const AxisQ ay = split_q28(y, p.uh, p.ul, p.dims);
+            const AxisQ az = split_q28(z, p.uh, p.ul, p.dims);
             if (CORNER) {
-                f2sum v = corner_factor(ax, ay, az);
+                f2sum v = corner_factor_q(ax, ay, az);
                 if (VARMASS) {
                     const float mm = m * mscale;
                     const float h = __fmul_rn(v.hi, mm);
@@ -420,24 +436,15 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                     v = f2sum{-v.hi, -v.lo};
                 alt = f2_add2(alt, v);
             }
-            // Weights: per-axis factors r = 2^23 - q (lower cell) and q (upper)
-            // from 23-bit fractions; pair products a = rx*ry / 2^16 (<= 2^30,
-            // times mant / 2^24 >> dsh for variable masses); corner weight
-            // a * rz / 2^25 (<= 2^28).
-            const unsigned qx = frac_q23(ax.frac), qy = frac_q23(ay.frac), qz = frac_q23(az.frac);
-            const unsigned rx = 0x800000u - qx, ry = 0x800000u - qy, rz = 0x800000u - qz;
-            unsigned a00 = __umulhi(rx << 8, ry << 8), a10 = __umulhi(qx << 8, ry << 8);
-            unsigned a01 = __umulhi(rx << 8, qy << 8), a11 = __umulhi(qx << 8, qy << 8);
-            if (VARMASS) {
-                a00 = __umulhi(a00 << 1, mant7) >> dsh;
-                a10 = __umulhi(a10 << 1, mant7) >> dsh;
-                a01 = __umulhi(a01 << 1, mant7) >> dsh;
-                a11 = __umulhi(a11 << 1, mant7) >> dsh;
-            }
-            const unsigned cz0 = rz << 7, cz1 = qz << 7;
-            unsigned w[8] = {__umulhi(a00, cz0), __umulhi(a10, cz0), __umulhi(a01, cz0),
-                             __umulhi(a11, cz0), __umulhi(a00, cz1), __umulhi(a10, cz1),
-                             __umulhi(a01, cz1), __umulhi(a11, cz1)};
+            // Weights (common.cuh): factors 2^28 - q (lower cell) and q (upper).
+            const uint32_t rx = kFracOne - ax.q, ry = kFracOne - ay.q, rz = kFracOne - az.q;
+            const uint32_t p00 = pair_w(rx, ry), p10 = pair_w(ax.q, ry), p01 = pair_w(rx, ay.q),
+                           p11 = pair_w(ax.q, ay.q);
+            const uint32_t z0 = z_mass(rz, mant, VARMASS ? dsh : 0);
+            const uint32_t z1 = z_mass(az.q, mant, VARMASS ? dsh : 0);
+            const uint32_t w[8] = {corner_w(p00, z0), corner_w(p10, z0), corner_w(p01, z0),
+                                   corner_w(p11, z0), corner_w(p00, z1), corner_w(p10, z1),
+                                   corner_w(p01, z1), corner_w(p11, z1)};
             const int cell[3] = {ax.cell, ay.cell, az.cell};
             int o0 = ax.cell - box.org[0], o1 = ay.cell - box.org[1], o2 = az.cell - box.org[2];
             o0 += o0 < 0 ? p.dims : 0;
@@ -464,74 +471,65 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                         ovf |= (unsigned)(neg ? nw > old[q] : nw < old[q]) << q;
                     }
                     if (ovf)
-                        carry_corners(p, grid, cell, ovf, neg ? -carry_val : carry_val);
+                        carry_corners(p, carry, cell, ovf, neg ? -1 : 1);
                 }
             } else {
-                float wf[8];
+                int wi[8];
 #pragma unroll
                 for (int q = 0; q < 8; q++)
-                    wf[q] = (neg ? -(float)w[q] : (float)w[q]) * unit;
-                global_corners(p, grid, cell, wf);
+                    wi[q] = neg ? -(int)w[q] : (int)w[q];
+                global_corners(p, acc, carry, cell, wi);
             }
         }
         __syncthreads();
 
-        // Flush and clear: one warp per window row, lanes along z.
+        // Flush and clear: one warp per window row, lanes along z; every
+        // non-zero cell is added exactly to the pass accumulator.  A lane
+        // issues the atomics of up to kFlushBatch of its cells before it looks
+        // at any returned value, so the round trips overlap.
         if (box.use) {
             const int nrows = box.ext[0] * box.ext[1];
-            const bool whole_z = box.ext[2] == p.dims + 1 && p.dims >= 8;
             for (int r = wid; r < nrows; r += nwarps) {
                 const int wx = r / box.ext[1];
                 const int wy = r - wx * box.ext[1];
                 const int gx = wrap_once(box.org[0] + wx, p.dims);
                 const int gy = wrap_once(box.org[1] + wy, p.dims);
-                float *grow = grid + (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
+                const size_t rowbase = (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
                 int *wrow = win + (size_t)r * DY;
-                if (whole_z) {
-                    // [zv, zend) as float4; the (at most 3 + 3) cells either
-                    // side and the wrapped layer z = N (-> 0) one by one.
-                    const int zv = (int)(((16u - ((unsigned)(uintptr_t)grow & 15u)) & 15u) >> 2);
-                    const int zend = zv + ((p.dims - zv) & ~3);
-                    for (int z = zv + 4 * lane; z < zend; z += 128) {
-                        const int v0 = wrow[z], v1 = wrow[z + 1], v2 = wrow[z + 2],
-                                  v3 = wrow[z + 3];
-                        if ((v0 | v1 | v2 | v3) != 0) {
+                int *arow = acc + rowbase;
+                for (int z0 = 0; z0 < box.ext[2]; z0 += 32 * kFlushBatch) {
+                    int vv[kFlushBatch], old[kFlushBatch];
+                    int ovf = 0;  // sign bit: some add overflowed
+#pragma unroll
+                    for (int k = 0; k < kFlushBatch; k++) {
+                        const int z = z0 + lane + 32 * k;
+                        vv[k] = z < box.ext[2] ? wrow[z] : 0;
+                        old[k] = 0;
+                        if (vv[k] != 0) {
                             wrow[z] = 0;
-                            wrow[z + 1] = 0;
-                            wrow[z + 2] = 0;
-                            wrow[z + 3] = 0;
-                            atomicAdd((float4 *)(grow + z),
-                                      make_float4((float)v0 * unit, (float)v1 * unit,
-                                                  (float)v2 * unit, (float)v3 * unit));
+                            int gz = box.org[2] + z;
+                            gz -= gz >= p.dims ? p.dims : 0;
+                            old[k] = atomicAdd(arow + gz, vv[k]);
                         }
                     }
-                    int ze = -1, zg = 0;
-                    if (lane < zv) {
-                        ze = lane;
-                        zg = lane;
-                    } else if (lane - zv < p.dims - zend) {
-                        ze = zend + lane - zv;
-                        zg = ze;
-                    } else if (lane == 31) {
-                        ze = p.dims;
-                        zg = 0;
+#pragma unroll
+                    for (int k = 0; k < kFlushBatch; k++) {
+                        const int nw = (int)((unsigned)old[k] + (unsigned)vv[k]);
+                        ovf |= (old[k] ^ nw) & (vv[k] ^ nw);
                     }
-                    if (ze >= 0) {
-                        const int v = wrow[ze];
-                        if (v != 0) {
-                            wrow[ze] = 0;
-                            atomicAdd(grow + zg, (float)v * unit);
+                    if (ovf < 0) {
+#pragma unroll
+                        for (int k = 0; k < kFlushBatch; k++) {
+                            const int v = vv[k];
+                            const int nw = (int)((unsigned)old[k] + (unsigned)v);
+                            if (((old[k] ^ nw) & (v ^ nw)) < 0) {
+                                int gz = box.org[2] + z0 + lane + 32 * k;
+                                gz -= gz >= p.dims ? p.dims : 0;
+                                const size_t gi = rowbase + gz;
+                                atomicAdd(carry + (gi >> 1), (unsigned)((v > 0 ? 1 : -1) *
+                                                                        (1 << (16 * (int)(gi & 1)))));
+                            }
                         }
-                    }
-                    continue;
-                }
-                for (int z = lane; z < box.ext[2]; z += 32) {
-                    const int v = wrow[z];
-                    if (v != 0) {
-                        wrow[z] = 0;
-                        int gz = box.org[2] + z;
-                        gz -= gz >= p.dims ? p.dims : 0;
-                        atomicAdd(grow + gz, (float)v * unit);
                     }
                 }
             }
@@ -607,19 +605,20 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Pass constants for the window engine (one thread): pass mass, fixed-point
-// shift (used by the corner sum), the mean as a float (so -mean is exact in
-// FP32 and read-back adds back exactly what was subtracted), and the running
-// totals of the grid.
+// Pass constants for the window engine (one thread), as k_sort_scan forms
+// them for the sorted engine: pass mass, fixed-point shift s (the largest |mass|
+// maps into [2^27, 2^28) units of 2^-s) and the pass mean in fixed point,
+// rounded to 24 significant bits (an empty cell then reads back exactly 0).
+// nparts = 0: uniform mass umass; else the sum of nparts partial sums.
 __global__ void k_window_prep(const double *__restrict__ mass_part, int nparts, double umass,
                               int64_t n, double inv_cells, double *field_mass, double *field_sub,
                               DeviceStatus *st)
 {
     double m = 0.0;
     float mref;
-    if (umass >= 0.0) {
+    if (nparts == 0) {
         m = (double)n * umass;
-        mref = (float)umass;
+        mref = (float)fabs(umass);
     } else {
         for (int c = 0; c < nparts; c++)
             m += mass_part[c];
@@ -629,38 +628,67 @@ __global__ void k_window_prep(const double *__restrict__ mass_part, int nparts, 
     if (mref > 0.f && isfinite(mref))
         s = 27 - ilogbf(mref);
     s = max(-100, min(100, s));
-    const float mean32 = (float)(m * inv_cells);
+    const double mf = m * inv_cells * ldexp(1.0, s);
+    long long mean_fixed;
+    const double amf = fabs(mf);
+    if (amf >= 16777216.0) {
+        const double q = ldexp(1.0, ilogb(amf) - 23);
+        mean_fixed = (long long)(rint(mf / q) * q);
+    } else {
+        mean_fixed = llrint(mf);
+    }
     st->pass_mass = m;
     st->fx_shift = s;
-    st->win_mean = mean32;
+    st->mean_fixed = mean_fixed;
     *field_mass += m;
-    *field_sub += (double)mean32;
+    *field_sub += ldexp((double)mean_fixed, -s);
 }
 
-// grid[i] = -mean for every float (padding included: it is overwritten later).
-__global__ void k_grid_fill(float *__restrict__ grid, int64_t nfloat, const DeviceStatus *st)
+// Accumulator (+ 2^32 carries) minus the mean, rounded once to FP32 and
+// stored (clean grid) or added to the grid, for every real cell: the same
+// conversion as the sorted engine's.  Two cells per thread (the row length is
+// even, so an aligned cell pair shares one carry word); grid-stride loop.
+__global__ void __launch_bounds__(256)
+    k_window_convert(const int *__restrict__ acc, const unsigned *__restrict__ carry,
+                     float *__restrict__ grid, int dims, int row, int64_t npairs, int clean,
+                     const DeviceStatus *__restrict__ st)
 {
-    const float v = -st->win_mean;
-    float4 *g4 = (float4 *)grid;
-    const int64_t n4 = nfloat >> 2;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
-         i += (int64_t)gridDim.x * blockDim.x)
-        g4[i] = make_float4(v, v, v, v);
-    for (int64_t i = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nfloat;
-         i += (int64_t)gridDim.x * blockDim.x)
-        grid[i] = v;
-}
-
-// grid[real cells] += -mean (accumulating passes).
-__global__ void k_grid_add(float *__restrict__ grid, int dims, int row, int64_t ncells_rows,
-                           const DeviceStatus *st)
-{
-    const float v = -st->win_mean;
-    const int64_t total = ncells_rows * row;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        if ((int)(i % row) < dims)
-            grid[i] += v;
+    constexpr int U = 4;  // pairs in flight per thread
+    const long long mean = st->mean_fixed;
+    const float inv_scale = ldexpf(1.f, -st->fx_shift);
+    const int half_row = row >> 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < npairs;
+         k0 += U * stride) {
+        int2 a[U];
+        unsigned cw[U];
+        float2 o[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t k = k0 + u * stride;
+            if (k < npairs) {
+                a[u] = reinterpret_cast<const int2 *>(acc)[k];
+                cw[u] = carry[k];
+                o[u] = clean ? make_float2(0.f, 0.f) : reinterpret_cast<const float2 *>(grid)[k];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t k = k0 + u * stride;
+            if (k >= npairs)
+                continue;
+            const int z = 2 * (int)(k % half_row);
+            const long long v0 =
+                (long long)a[u].x + ((long long)((int)(cw[u] & 0xffffu) - kCarryBias) << 32);
+            const long long v1 =
+                (long long)a[u].y + ((long long)((int)(cw[u] >> 16) - kCarryBias) << 32);
+            const float2 f = make_float2(o[u].x + i64_to_f32_rn(v0 - mean) * inv_scale,
+                                         o[u].y + i64_to_f32_rn(v1 - mean) * inv_scale);
+            if (z + 1 < dims)
+                reinterpret_cast<float2 *>(grid)[k] = f;
+            else if (z < dims)
+                grid[2 * k] = f.x;
+        }
     }
 }
 
@@ -750,9 +778,9 @@ cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
 }
 
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, int num_sms, DeviceStatus *dstat,
-                                cudaStream_t stream, int64_t *launches, StageHook hook,
-                                void *hook_user)
+                                double *mass_part, int mass_ctas, int *acc, unsigned *carry,
+                                int num_sms, DeviceStatus *dstat, cudaStream_t stream,
+                                int64_t *launches, StageHook hook, void *hook_user)
 {
     auto mark = [&](const char *name) {
         (*launches)++;
@@ -769,18 +797,17 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         k_mass_reduce<<<mass_ctas, 256, 0, stream>>>(a.masses, a.n, mass_part, dstat);
         mark("win_mass");
     }
-    k_window_prep<<<1, 1, 0, stream>>>(mass_part, mass_ctas, a.masses ? -1.0 : (double)a.mass,
-                                       a.n, 1.0 / n3, a.field_mass, a.field_sub, dstat);
+    k_window_prep<<<1, 1, 0, stream>>>(mass_part, a.masses ? mass_ctas : 0, (double)a.mass, a.n,
+                                       1.0 / n3, a.field_mass, a.field_sub, dstat);
     mark("win_prep");
-    const int fill_blocks = 152 * 8;
-    if (a.clean)
-        k_grid_fill<<<fill_blocks, 256, 0, stream>>>(a.grid, g.grid.nfloat, dstat);
-    else
-        k_grid_add<<<fill_blocks, 256, 0, stream>>>(a.grid, g.grid.dims, g.grid.row,
-                                                     (int64_t)g.grid.dims * g.grid.dims, dstat);
-    mark("win_fill");
-    if ((err = cudaGetLastError()) != cudaSuccess)
+    // Exact accumulator: zero, and carry counts at their bias (bytes of 0x80).
+    if ((err = cudaMemsetAsync(acc, 0, sizeof(int) * (size_t)g.grid.nfloat, stream)) !=
+        cudaSuccess)
         return err;
+    if ((err = cudaMemsetAsync(carry, 0x80, sizeof(unsigned) * window_carry_words(g.grid),
+                               stream)) != cudaSuccess)
+        return err;
+    mark("win_clear");
     const WinParams p = make_win_params(g, a, chunk);
     if (p.nchunks > 0) {
         const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
@@ -790,14 +817,24 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem)) != cudaSuccess)
             return err;
-        kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, a.grid);
+        kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, acc, carry);
         mark("win_deposit");
         if ((err = cudaGetLastError()) != cudaSuccess)
             return err;
     }
+    k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, carry, a.grid, g.grid.dims, g.grid.row,
+                                                      g.grid.nfloat / 2, a.clean ? 1 : 0, dstat);
+    mark("win_convert");
+    if ((err = cudaGetLastError()) != cudaSuccess)
+        return err;
     k_window_finish<<<1, 1, 0, stream>>>(dstat, a.field_corner);
     (*launches)++;
     return cudaGetLastError();
+}
+
+size_t window_carry_words(const GridGeom &g)
+{
+    return (size_t)(g.nfloat + 1) / 2;
 }
 
 }  // namespace genpk

@@ -56,6 +56,8 @@ struct DepositScratch {
     size_t halo_cap = 0;
     double *mass_part = nullptr;     // [sort_ctas]
     int mass_part_cap = 0;
+    int *win_acc = nullptr;          // [nfloat] window engine's exact accumulator
+    unsigned *win_carry = nullptr;   // [window_carry_words] its 16-bit carry counts
 };
 
 // Device words a deposit pass reports through (zero-initialised).
@@ -67,7 +69,6 @@ struct DeviceStatus {
     long long alt_sum;                 // sum over cells of (-1)^(x+y+z) * cell, fixed point
     int fx_shift;                      // weights are accumulated as round(w * 2^fx_shift)
     unsigned max_mass_bits;            // max |mass| of the pass, as float bits
-    float win_mean;                    // window engine: mean subtracted from every cell
 };
 
 struct DepositArgs {
@@ -114,9 +115,12 @@ int window_cap_cells(int chunk, bool variable_masses);
 // Window volume (cells) of `samples` evenly spread chunks, written to vol_dev.
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
                          long long *vol_dev, int samples, cudaStream_t stream, int64_t *launches);
-// One window-engine pass; mass_part needs mass_ctas doubles (variable masses).
+// One window-engine pass; mass_part needs mass_ctas doubles (variable masses);
+// acc (nfloat ints) and carry (window_carry_words) are the exact accumulator.
+size_t window_carry_words(const GridGeom &g);
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, int num_sms, DeviceStatus *dstat,
+                                double *mass_part, int mass_ctas, int *acc, unsigned *carry,
+                                int num_sms, DeviceStatus *dstat,
                                 cudaStream_t stream, int64_t *launches, StageHook hook,
                                 void *hook_user);
 

@@ -168,7 +168,7 @@ int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *ti
                          int *sort_ctas);
 
 /* Choose the deposit tile of the sorted engine (cells per edge; supported:
- * 8^3, 16^3, 16x16x32).  The sorted engine's grid does not depend on it. */
+ * 8^3 and 16^3).  The sorted engine's grid does not depend on it. */
 int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z);
 
 /* Deposit engines.

@@ -186,7 +186,7 @@ def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
     masses = np.linspace(0.2, 3.0, len(pos)).astype(np.float32)
     ref = O.deposit(pos, box, dims, masses, 0.0)
     grids = []
-    for tile in [(8, 8, 8), (16, 16, 16), (16, 16, 32)]:
+    for tile in [(8, 8, 8), (16, 16, 16)]:
         with gp.Context(dims, 16) as ctx:
             ctx.set_engine(gp.api.ENGINE_SORTED)
             ctx.set_tile(*tile)
@@ -368,20 +368,51 @@ def test_sparse_lattice_picks_a_shorter_window_chunk(gp):
         grid_close(ctx.read_field(0), O.deposit(pos, box, dims, None, 1.0), tol=1e-6)
 
 
-def test_window_and_sorted_engines_agree(gp):
-    """Same particles, both engines, accumulate semantics across passes."""
+@pytest.mark.parametrize("var", [False, True])
+def test_window_and_sorted_engines_agree_bit_for_bit(gp, var):
+    """Both engines add the same integer CIC weights (28-bit fractions from the
+    exact split) exactly and round each cell once: identical grids, also when
+    a grid accumulates two passes."""
+    import torch
     from genpk_gb300 import synth
     dims, box = 96, 1000.0
-    pos = synth.zeldovich(96, box, seed=7)
+    pos = torch.from_numpy(synth.zeldovich(96, box, seed=7)).cuda()
+    masses = (torch.linspace(0.3, 2.0, len(pos)) if var else torch.ones(len(pos))).cuda()
     with gp.Context(dims, 16) as ctx:
         grids = []
         for eng in (gp.api.ENGINE_SORTED, gp.api.ENGINE_WINDOW):
             ctx.set_engine(eng)
             ctx.zero(0)
-            ctx.deposit(0, box, pos[:400000], None, 1.0)
-            ctx.deposit(0, box, pos[400000:], None, 1.0)
+            if var:
+                ctx.deposit(0, box, pos[:400000], masses[:400000])
+                ctx.deposit(0, box, pos[400000:], masses[400000:])
+            else:
+                ctx.deposit(0, box, pos[:400000], None, 1.0)
+                ctx.deposit(0, box, pos[400000:], None, 1.0)
+            ctx.sync()
+            assert ctx.last_engine == eng
             grids.append(ctx.read_field(0))
-    grid_close(grids[1], grids[0], tol=1e-6)
+    assert np.array_equal(grids[0], grids[1])
+
+
+@pytest.mark.parametrize("engine", ["sorted", "window"])
+def test_faint_high_k_bins_of_a_smooth_lattice(gp, engine):
+    """128^3 Zel'dovich lattice (the GPU generator, L = 25000, 64 bins): the
+    highest-k bins hold ~1e-10 of the peak power and are sensitive to the
+    fraction precision (28-bit fractions from the exact split) and to any
+    rounding of partial cell sums; every bin within 1e-5 of the FP64 oracle."""
+    from genpk_gb300 import synth
+    n, box, nrb = 128, 25000.0, 64
+    dpos = synth.zeldovich(n, box, seed=1, device="cuda")
+    pos = dpos.cpu().numpy()
+    m = O.total_mass(len(pos), None, 1.0)
+    pr, cr, _ = O.pk(pos, box, n, nrb, None, 1.0, m_norm=m)
+    with gp.Context(n, nrb) as ctx:
+        ctx.set_engine(gp.api.ENGINE_SORTED if engine == "sorted" else gp.api.ENGINE_WINDOW)
+        ctx.deposit(0, box, dpos, None, 1.0)
+        p, c, _ = ctx.power(0, 0, m, m)
+    assert np.array_equal(c, cr)
+    bins_close(p, pr, c)
 
 
 def test_global_counter_sort_mode(gp):
