@@ -21,17 +21,17 @@
 //     pass B  splits every position exactly (split_q28) and adds the eight
 //             CIC weights (at most 2^28 units each) to the shared window with
 //             native shared integer atomics; a signed overflow of a window
-//             cell becomes a +-1 carry of its grid cell.  Pass B also sums the
-//             chunk's share of the exact corner mode.
-//     flush   every non-zero window cell is added to the pass accumulator
-//             (global integer atomics) and cleared, so the window is zero
-//             again for the next chunk.
+//             cell adds +-2^32 to its grid cell.  Pass B also sums the chunk's
+//             share of the exact corner mode.
+//     flush   every non-zero window cell is added to the 64-bit pass
+//             accumulator (global RED, no return) and cleared, so the window
+//             is zero again for the next chunk.
 //
-// Sums are exact: the window cells and the pass accumulator are integers of
-// 2^-s mass units (the sorted engine's weights, common.cuh pair_w / z_mass /
-// corner_w), the accumulator 32-bit with signed overflows counted in a 16-bit
-// carry per cell; k_window_convert subtracts the fixed-point pass mean and
-// rounds each cell once to FP32.  The grid is therefore bit-identical to the
+// Sums are exact: the window cells (32-bit, overflows moved on as 2^32 units)
+// and the pass accumulator (64-bit) are integers of 2^-s mass units (the
+// sorted engine's weights, common.cuh pair_w / z_mass / corner_w);
+// k_window_convert subtracts the fixed-point pass mean and rounds each cell
+// once to FP32.  The grid is therefore bit-identical to the
 // sorted engine's and independent of summation order.
 #include "common.cuh"
 #include "internal.h"
@@ -264,19 +264,13 @@ __device__ __forceinline__ void copy_chunk(const WinParams &p, int64_t c, int cn
         copy_floats(M, p.masses + chunk_first(p, c), cnt);
 }
 
-// The pass accumulates exact integers: acc[gi] (32-bit, wrapping) plus 2^32
-// times the signed count in carry[gi >> 1] (16-bit half gi & 1, biased by
-// kCarryBias), for every padded grid index gi.
-constexpr int kCarryBias = 0x8080;  // carry words start as bytes of 0x80
-constexpr int kFlushBatch = 8;      // cells per lane in flight per round trip
+// The pass accumulates exact 64-bit integers acc[gi] for every padded grid
+// index gi; adds return nothing (RED), so they never wait.
+typedef unsigned long long acc_t;
 
-// Adds v to one accumulator cell; a signed overflow moves +-1 into its carry.
-__device__ __forceinline__ void acc_add_global(int *acc, unsigned *carry, size_t gi, int v)
+__device__ __forceinline__ void acc_add_global(acc_t *acc, size_t gi, long long v)
 {
-    const int old = atomicAdd(acc + gi, v);
-    const int nw = (int)((unsigned)old + (unsigned)v);
-    if (v > 0 ? nw < old : nw > old)
-        atomicAdd(carry + (gi >> 1), (unsigned)((v > 0 ? 1 : -1) * (1 << (16 * (int)(gi & 1)))));
+    atomicAdd(acc + gi, (acc_t)v);
 }
 
 __device__ __forceinline__ size_t corner_index(const WinParams &p, const int c[3], int k)
@@ -289,33 +283,29 @@ __device__ __forceinline__ size_t corner_index(const WinParams &p, const int c[3
 
 // Global-path adds of one particle's eight corners (cells c, signed weights
 // w[k] for corner k = dx | dy << 1 | dz << 2).
-__device__ __noinline__ void global_corners(const WinParams &p, int *acc, unsigned *carry,
-                                            const int c[3], const int w[8])
+__device__ __noinline__ void global_corners(const WinParams &p, acc_t *acc, const int c[3],
+                                            const int w[8])
 {
 #pragma unroll
     for (int k = 0; k < 8; k++)
         if (w[k] != 0)
-            acc_add_global(acc, carry, corner_index(p, c, k), w[k]);
+            acc_add_global(acc, corner_index(p, c, k), w[k]);
 }
 
-// Window cells of the corners in `mask` overflowed by `sign`: carry +-1 into
-// their grid cells' carry counts.
-__device__ __noinline__ void carry_corners(const WinParams &p, unsigned *carry, const int c[3],
+// Window cells of the corners in `mask` overflowed by `sign`: move +-2^32
+// into their grid cells.
+__device__ __noinline__ void carry_corners(const WinParams &p, acc_t *acc, const int c[3],
                                            unsigned mask, int sign)
 {
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        if ((mask >> k) & 1u) {
-            const size_t gi = corner_index(p, c, k);
-            atomicAdd(carry + (gi >> 1), (unsigned)(sign * (1 << (16 * (int)(gi & 1)))));
-        }
-    }
+    for (int k = 0; k < 8; k++)
+        if ((mask >> k) & 1u)
+            acc_add_global(acc, corner_index(p, c, k), (long long)sign << 32);
 }
 
 template <bool VARMASS, bool CORNER>
 __global__ void __launch_bounds__(kWinThreads, 1)
-    k_window_deposit(WinParams p, DeviceStatus *st, int *__restrict__ acc,
-                     unsigned *__restrict__ carry)
+    k_window_deposit(WinParams p, DeviceStatus *st, acc_t *__restrict__ acc)
 {
     extern __shared__ __align__(128) unsigned char win_smem[];
     float *pbuf = reinterpret_cast<float *>(win_smem);              // [2][chunk * 3]
@@ -471,22 +461,20 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                         ovf |= (unsigned)(neg ? nw > old[q] : nw < old[q]) << q;
                     }
                     if (ovf)
-                        carry_corners(p, carry, cell, ovf, neg ? -1 : 1);
+                        carry_corners(p, acc, cell, ovf, neg ? -1 : 1);
                 }
             } else {
                 int wi[8];
 #pragma unroll
                 for (int q = 0; q < 8; q++)
                     wi[q] = neg ? -(int)w[q] : (int)w[q];
-                global_corners(p, acc, carry, cell, wi);
+                global_corners(p, acc, cell, wi);
             }
         }
         __syncthreads();
 
         // Flush and clear: one warp per window row, lanes along z; every
-        // non-zero cell is added exactly to the pass accumulator.  A lane
-        // issues the atomics of up to kFlushBatch of its cells before it looks
-        // at any returned value, so the round trips overlap.
+        // non-zero cell is added exactly to the pass accumulator.
         if (box.use) {
             const int nrows = box.ext[0] * box.ext[1];
             for (int r = wid; r < nrows; r += nwarps) {
@@ -494,42 +482,15 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                 const int wy = r - wx * box.ext[1];
                 const int gx = wrap_once(box.org[0] + wx, p.dims);
                 const int gy = wrap_once(box.org[1] + wy, p.dims);
-                const size_t rowbase = (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
+                acc_t *arow = acc + (size_t)gx * (size_t)p.plane + (size_t)gy * (size_t)p.row;
                 int *wrow = win + (size_t)r * DY;
-                int *arow = acc + rowbase;
-                for (int z0 = 0; z0 < box.ext[2]; z0 += 32 * kFlushBatch) {
-                    int vv[kFlushBatch], old[kFlushBatch];
-                    int ovf = 0;  // sign bit: some add overflowed
-#pragma unroll
-                    for (int k = 0; k < kFlushBatch; k++) {
-                        const int z = z0 + lane + 32 * k;
-                        vv[k] = z < box.ext[2] ? wrow[z] : 0;
-                        old[k] = 0;
-                        if (vv[k] != 0) {
-                            wrow[z] = 0;
-                            int gz = box.org[2] + z;
-                            gz -= gz >= p.dims ? p.dims : 0;
-                            old[k] = atomicAdd(arow + gz, vv[k]);
-                        }
-                    }
-#pragma unroll
-                    for (int k = 0; k < kFlushBatch; k++) {
-                        const int nw = (int)((unsigned)old[k] + (unsigned)vv[k]);
-                        ovf |= (old[k] ^ nw) & (vv[k] ^ nw);
-                    }
-                    if (ovf < 0) {
-#pragma unroll
-                        for (int k = 0; k < kFlushBatch; k++) {
-                            const int v = vv[k];
-                            const int nw = (int)((unsigned)old[k] + (unsigned)v);
-                            if (((old[k] ^ nw) & (v ^ nw)) < 0) {
-                                int gz = box.org[2] + z0 + lane + 32 * k;
-                                gz -= gz >= p.dims ? p.dims : 0;
-                                const size_t gi = rowbase + gz;
-                                atomicAdd(carry + (gi >> 1), (unsigned)((v > 0 ? 1 : -1) *
-                                                                        (1 << (16 * (int)(gi & 1)))));
-                            }
-                        }
+                for (int z = lane; z < box.ext[2]; z += 32) {
+                    const int v = wrow[z];
+                    if (v != 0) {
+                        wrow[z] = 0;
+                        int gz = box.org[2] + z;
+                        gz -= gz >= p.dims ? p.dims : 0;
+                        atomicAdd(arow + gz, (acc_t)(long long)v);
                     }
                 }
             }
@@ -644,31 +605,28 @@ __global__ void k_window_prep(const double *__restrict__ mass_part, int nparts, 
     *field_sub += ldexp((double)mean_fixed, -s);
 }
 
-// Accumulator (+ 2^32 carries) minus the mean, rounded once to FP32 and
-// stored (clean grid) or added to the grid, for every real cell: the same
-// conversion as the sorted engine's.  Two cells per thread (the row length is
-// even, so an aligned cell pair shares one carry word); grid-stride loop.
+// Accumulator minus the mean, rounded once to FP32 and stored (clean grid) or
+// added to the grid, for every real cell: the same conversion as the sorted
+// engine's.  Two cells per thread (rows have even length), four pairs in
+// flight; grid-stride loop.
 __global__ void __launch_bounds__(256)
-    k_window_convert(const int *__restrict__ acc, const unsigned *__restrict__ carry,
-                     float *__restrict__ grid, int dims, int row, int64_t npairs, int clean,
-                     const DeviceStatus *__restrict__ st)
+    k_window_convert(const acc_t *__restrict__ acc, float *__restrict__ grid, int dims, int row,
+                     int64_t npairs, int clean, const DeviceStatus *__restrict__ st)
 {
-    constexpr int U = 4;  // pairs in flight per thread
+    constexpr int U = 4;
     const long long mean = st->mean_fixed;
     const float inv_scale = ldexpf(1.f, -st->fx_shift);
     const int half_row = row >> 1;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < npairs;
          k0 += U * stride) {
-        int2 a[U];
-        unsigned cw[U];
+        longlong2 a[U];
         float2 o[U];
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const int64_t k = k0 + u * stride;
             if (k < npairs) {
-                a[u] = reinterpret_cast<const int2 *>(acc)[k];
-                cw[u] = carry[k];
+                a[u] = reinterpret_cast<const longlong2 *>(acc)[k];
                 o[u] = clean ? make_float2(0.f, 0.f) : reinterpret_cast<const float2 *>(grid)[k];
             }
         }
@@ -678,12 +636,8 @@ __global__ void __launch_bounds__(256)
             if (k >= npairs)
                 continue;
             const int z = 2 * (int)(k % half_row);
-            const long long v0 =
-                (long long)a[u].x + ((long long)((int)(cw[u] & 0xffffu) - kCarryBias) << 32);
-            const long long v1 =
-                (long long)a[u].y + ((long long)((int)(cw[u] >> 16) - kCarryBias) << 32);
-            const float2 f = make_float2(o[u].x + i64_to_f32_rn(v0 - mean) * inv_scale,
-                                         o[u].y + i64_to_f32_rn(v1 - mean) * inv_scale);
+            const float2 f = make_float2(o[u].x + i64_to_f32_rn(a[u].x - mean) * inv_scale,
+                                         o[u].y + i64_to_f32_rn(a[u].y - mean) * inv_scale);
             if (z + 1 < dims)
                 reinterpret_cast<float2 *>(grid)[k] = f;
             else if (z < dims)
@@ -778,7 +732,7 @@ cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
 }
 
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, int *acc, unsigned *carry,
+                                double *mass_part, int mass_ctas, unsigned long long *acc,
                                 int num_sms, DeviceStatus *dstat, cudaStream_t stream,
                                 int64_t *launches, StageHook hook, void *hook_user)
 {
@@ -800,12 +754,8 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
     k_window_prep<<<1, 1, 0, stream>>>(mass_part, a.masses ? mass_ctas : 0, (double)a.mass, a.n,
                                        1.0 / n3, a.field_mass, a.field_sub, dstat);
     mark("win_prep");
-    // Exact accumulator: zero, and carry counts at their bias (bytes of 0x80).
-    if ((err = cudaMemsetAsync(acc, 0, sizeof(int) * (size_t)g.grid.nfloat, stream)) !=
+    if ((err = cudaMemsetAsync(acc, 0, sizeof(acc_t) * (size_t)g.grid.nfloat, stream)) !=
         cudaSuccess)
-        return err;
-    if ((err = cudaMemsetAsync(carry, 0x80, sizeof(unsigned) * window_carry_words(g.grid),
-                               stream)) != cudaSuccess)
         return err;
     mark("win_clear");
     const WinParams p = make_win_params(g, a, chunk);
@@ -817,12 +767,12 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem)) != cudaSuccess)
             return err;
-        kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, acc, carry);
+        kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, acc);
         mark("win_deposit");
         if ((err = cudaGetLastError()) != cudaSuccess)
             return err;
     }
-    k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, carry, a.grid, g.grid.dims, g.grid.row,
+    k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, a.grid, g.grid.dims, g.grid.row,
                                                       g.grid.nfloat / 2, a.clean ? 1 : 0, dstat);
     mark("win_convert");
     if ((err = cudaGetLastError()) != cudaSuccess)
@@ -832,9 +782,5 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
     return cudaGetLastError();
 }
 
-size_t window_carry_words(const GridGeom &g)
-{
-    return (size_t)(g.nfloat + 1) / 2;
-}
 
 }  // namespace genpk

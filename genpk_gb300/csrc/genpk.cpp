@@ -349,18 +349,11 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         s.mass_part_cap = (int)mp;
         if (!s.win_acc) {
             GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-            GENPK_CUDA(cudaMalloc(&s.win_acc, sizeof(int) * (size_t)g.grid.nfloat));
-            if (cudaMalloc(&s.win_carry, sizeof(unsigned) * window_carry_words(g.grid)) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                cudaFree(s.win_acc);
-                s.win_acc = nullptr;
-                return fail(ctx, GENPK_ERR_NOMEM, "window accumulator allocation failed");
-            }
+            GENPK_CUDA(cudaMalloc(&s.win_acc, sizeof(unsigned long long) * (size_t)g.grid.nfloat));
         }
         GENPK_CUDA(deposit_window_pass(g, a, chunk, s.mass_part, mass_ctas, s.win_acc,
-                                       s.win_carry, ctx->num_sms, ctx->d_status, ctx->stream,
-                                       &ctx->launches, hook, ctx));
+                                       ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches,
+                                       hook, ctx));
     } else {
         const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
         if (deposit_shared_hist(g)) {
@@ -747,7 +740,6 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->dscr.cursor);
     cudaFree(ctx->dscr.mass_part);
     cudaFree(ctx->dscr.win_acc);
-    cudaFree(ctx->dscr.win_carry);
     cudaFree(ctx->stage_pos);
     cudaFree(ctx->stage_mass);
     cudaFree(ctx->d_partial);

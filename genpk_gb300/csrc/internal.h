@@ -56,8 +56,7 @@ struct DepositScratch {
     size_t halo_cap = 0;
     double *mass_part = nullptr;     // [sort_ctas]
     int mass_part_cap = 0;
-    int *win_acc = nullptr;          // [nfloat] window engine's exact accumulator
-    unsigned *win_carry = nullptr;   // [window_carry_words] its 16-bit carry counts
+    unsigned long long *win_acc = nullptr;  // [nfloat] window engine's exact accumulator
 };
 
 // Device words a deposit pass reports through (zero-initialised).
@@ -116,10 +115,9 @@ int window_cap_cells(int chunk, bool variable_masses);
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
                          long long *vol_dev, int samples, cudaStream_t stream, int64_t *launches);
 // One window-engine pass; mass_part needs mass_ctas doubles (variable masses);
-// acc (nfloat ints) and carry (window_carry_words) are the exact accumulator.
-size_t window_carry_words(const GridGeom &g);
+// acc (nfloat 64-bit integers) is the exact accumulator.
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, int *acc, unsigned *carry,
+                                double *mass_part, int mass_ctas, unsigned long long *acc,
                                 int num_sms, DeviceStatus *dstat,
                                 cudaStream_t stream, int64_t *launches, StageHook hook,
                                 void *hook_user);
