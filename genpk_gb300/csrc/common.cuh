@@ -40,33 +40,26 @@ __device__ __forceinline__ void split_cell(float p, float uh, float ul, int dims
     frac = d;
 }
 
-// Nearest float to a 64-bit integer (ties to even), with integer instructions
-// only: the hardware int64 -> float conversion runs on the FP64 pipe, which
-// GB300 has little of.
+// Nearest float to a 64-bit integer (ties to even) from 32-bit operations:
+// the hardware int64 -> float conversion runs on the FP64 pipe, which GB300
+// has little of.  |v| < 2^32 converts directly (32-bit conversion, nearest
+// even); above, the top 32 bits of |v| from its leading one, with every lower
+// bit ORed into bit 0 (a sticky bit below the rounding position, bit 7), round
+// the same way and are scaled back by an exact power of two.
 __device__ __forceinline__ float i64_to_f32_rn(long long v)
 {
-    const unsigned neg = (unsigned)((unsigned long long)v >> 63);
-    unsigned long long a = neg ? 0ull - (unsigned long long)v : (unsigned long long)v;
-    if (a == 0ull)
-        return 0.f;
-    int e = 63 - __clzll((long long)a);  // position of the leading one
-    unsigned m;
-    if (e <= 23) {
-        m = (unsigned)a << (23 - e);
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    const unsigned hi = (unsigned)(a >> 32), lo = (unsigned)a;
+    float r;
+    if (hi == 0u) {
+        r = __uint2float_rn(lo);
     } else {
-        const int sh = e - 23;
-        unsigned long long q = a >> sh;
-        const unsigned long long rem = a & ((1ull << sh) - 1ull);
-        const unsigned long long half = 1ull << (sh - 1);
-        if (rem > half || (rem == half && (q & 1ull)))
-            q++;
-        if (q == (1ull << 24)) {
-            q >>= 1;
-            e++;
-        }
-        m = (unsigned)q;
+        const int k = __clz((int)hi);                      // hi << k has bit 31 set
+        const unsigned top = __funnelshift_l(lo, hi, k);   // bits 63-k .. 32-k of |v|
+        const unsigned sticky = (lo << k) != 0u ? 1u : 0u;  // the 32-k bits below
+        r = __uint2float_rn(top | sticky) * __uint_as_float((unsigned)(159 - k) << 23);  // 2^(32-k)
     }
-    return __uint_as_float((neg << 31) | ((unsigned)(e + 127) << 23) | (m & 0x7fffffu));
+    return v < 0 ? -r : r;
 }
 
 // Unevaluated sum hi + lo of two floats (double-float arithmetic, Dekker/Knuth).
@@ -130,38 +123,37 @@ __device__ __forceinline__ AxisQ split_q28(float p, float uh, float ul, int dims
 {
     const float xh = __fmul_rn(p, uh);
     const float xe = fmaf(p, uh, -xh);
-    const float xl = fmaf(p, ul, xe);
+    float xl = fmaf(p, ul, xe);
     const float f = floorf(xh);
-    const float a = __fsub_rn(xh, f);
-    // a * 2^28 is exact (and an integer when xh >= 1); xl * 2^28 is small
-    int q = __float2int_rn(a * 268435456.f) + __float2int_rn(xl * 268435456.f);
-    // 1 - 2a is exact in FP32 for |xh| >= 1 (a is then a multiple of 2^-23);
-    // below, its rounding error is folded into xl so that u - 2 xl stays exact
-    float u = __fsub_rn(1.f, __fmul_rn(2.f, a));
+    float a = __fsub_rn(xh, f);
+    // For |xh| >= 1, a is exact and a multiple of 2^-23, so 1 - 2a is exact.
+    // Within one cell of the origin both may round (a = xh + 1 for
+    // -1 < xh < 0; 1 - 2a for a < 1/4): the errors move into xl, so that the
+    // fraction a + xl and u - 2 xl (the corner factor) stay exact.
+    float u = fmaf(-2.f, a, 1.f);
     float xlu = xl;
     if (fabsf(xh) < 1.f) {
+        const f2sum s = two_sum(xh, -f);
+        a = s.hi;
+        xl = __fadd_rn(xl, s.lo);
         const f2sum t = two_sum(1.f, -2.f * a);
         u = t.hi;
         xlu = __fsub_rn(xl, 0.5f * t.lo);
     }
-    int fi = (int)f;
-    if (q < 0) {
-        q += (int)kFracOne;
-        fi -= 1;
-        u = __fsub_rn(u, 2.f);
-    }
-    if (q >= (int)kFracOne) {
-        q -= (int)kFracOne;
-        fi += 1;
-        u = __fadd_rn(u, 2.f);
-    }
-    q = min(max(q, 0), (int)kFracOne - 1);  // far positions (|x| > 2^22 cells) only
+    // a * 2^28 is exact (an integer when xh >= 1); xl * 2^28 is at most
+    // ~|x| 2^5, clamped so that the sum cannot overflow (exact up to 2^25 cells)
+    const int qa = __float2int_rn(a * 268435456.f);
+    const int qb = min(max(__float2int_rn(xl * 268435456.f), -(1 << 30)), 1 << 30);
+    const int q = qa + qb;
+    const int carry = q >> kFracBits;  // floor(q / 2^28): the cell moves by carry
+    int fi = (int)f + carry;
+    u = fmaf(2.f, (float)carry, u);    // 1 - 2 (a - carry)
     if ((unsigned)fi >= (unsigned)dims) {
         fi %= dims;
         if (fi < 0)
             fi += dims;
     }
-    return {fi, (uint32_t)q, u, xlu};
+    return {fi, (uint32_t)q & (kFracOne - 1u), u, xlu};
 }
 
 // The CIC weights of one particle in 2^-s mass units, shared by both deposit

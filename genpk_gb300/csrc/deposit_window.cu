@@ -473,8 +473,9 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         }
         __syncthreads();
 
-        // Flush and clear: one warp per window row, lanes along z; every
-        // non-zero cell is added exactly to the pass accumulator.
+        // Flush and clear: one warp per window row, lanes along z (each
+        // reduction instruction then covers consecutive cells); every non-zero
+        // cell is added exactly to the pass accumulator.
         if (box.use) {
             const int nrows = box.ext[0] * box.ext[1];
             for (int r = wid; r < nrows; r += nwarps) {
@@ -608,7 +609,9 @@ __global__ void k_window_prep(const double *__restrict__ mass_part, int nparts, 
 // Accumulator minus the mean, rounded once to FP32 and stored (clean grid) or
 // added to the grid, for every real cell: the same conversion as the sorted
 // engine's.  Two cells per thread (rows have even length), four pairs in
-// flight; grid-stride loop.
+// flight; grid-stride loop.  The pair's place in its row is tracked
+// incrementally (no 64-bit division): the row's last pair is padding for even
+// dims and half padding for odd dims, and padding is never written.
 __global__ void __launch_bounds__(256)
     k_window_convert(const acc_t *__restrict__ acc, float *__restrict__ grid, int dims, int row,
                      int64_t npairs, int clean, const DeviceStatus *__restrict__ st)
@@ -617,9 +620,13 @@ __global__ void __launch_bounds__(256)
     const long long mean = st->mean_fixed;
     const float inv_scale = ldexpf(1.f, -st->fx_shift);
     const int half_row = row >> 1;
+    const int last = (dims - 1) >> 1;  // the pair holding z = dims - 1
+    const bool odd = (dims & 1) != 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < npairs;
-         k0 += U * stride) {
+    const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int dz = (int)(stride % half_row);
+    int zp = (int)(first % half_row);
+    for (int64_t k0 = first; k0 < npairs; k0 += U * stride) {
         longlong2 a[U];
         float2 o[U];
 #pragma unroll
@@ -633,14 +640,16 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const int64_t k = k0 + u * stride;
-            if (k >= npairs)
+            const int zu = zp;
+            zp += dz;
+            zp -= zp >= half_row ? half_row : 0;
+            if (k >= npairs || zu > last)
                 continue;
-            const int z = 2 * (int)(k % half_row);
             const float2 f = make_float2(o[u].x + i64_to_f32_rn(a[u].x - mean) * inv_scale,
                                          o[u].y + i64_to_f32_rn(a[u].y - mean) * inv_scale);
-            if (z + 1 < dims)
+            if (zu < last || !odd)
                 reinterpret_cast<float2 *>(grid)[k] = f;
-            else if (z < dims)
+            else
                 grid[2 * k] = f.x;
         }
     }

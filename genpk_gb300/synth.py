@@ -57,7 +57,7 @@ def zeldovich(nside: int, box: float, seed: int = 1, rms: float = 0.3, kc_frac: 
         dk = wk * amp
         # psi_k = i k / k^2 delta_k
         inv = np.where(k2 > 0, 1.0 / k2, 0.0)
-    psi = [np.fft.irfftn(1j * kk * inv * dk, s=(n, n, n)) for kk in (kx, ky, kzz)]
+    psi = [np.fft.irfftn(1j * kk * inv * dk, s=(n, n, n), axes=(0, 1, 2)) for kk in (kx, ky, kzz)]
     cur = np.sqrt(np.mean(psi[0] ** 2 + psi[1] ** 2 + psi[2] ** 2))
     spacing = box / n
     scale = amplitude * rms * spacing / cur
@@ -121,7 +121,7 @@ def lognormal(n_mean: int, box: float, ngrid: int, sigma: float = 1.5, seed: int
     k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
     kc = 0.25 * ngrid
     gk *= np.exp(-0.5 * k2 / kc ** 2)
-    g = np.fft.irfftn(gk, s=(ngrid,) * 3)
+    g = np.fft.irfftn(gk, s=(ngrid,) * 3, axes=(0, 1, 2))
     g /= g.std()
     rho = np.exp(sigma * g - 0.5 * sigma ** 2)
     lam = rho * (n_mean / rho.sum())
