@@ -41,11 +41,12 @@ if ROOT not in sys.path:
 METRIC = ("particles/s + ms/spectrum at 512^3 grid vs FP64 oracle; "
           "fwd+adjoint/fwd time ratio")
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_window_deposit launch,
-# from an ncu capture of the default workload (512^3 Zel'dovich particles onto
-# a 512^3 grid, uniform mass): 2.151 GB read + 0.530 GB written.  Reported only
-# for that workload.
-NCU_WINDOW_TRAFFIC = {"nside": 512, "grid": 512, "bytes": 2.151e9 + 0.530e9}
+# dram__bytes_read.sum + dram__bytes_write.sum of one deposit-kernel launch,
+# from ncu captures of the default workload (512^3 Zel'dovich particles onto a
+# 512^3 grid, uniform mass), keyed by (kernel, particles per side, grid).
+# k_window_deposit: 2.692 GB read (positions 1.61 GB + the 64-bit accumulator's
+# lines) + 1.052 GB written (the accumulator).  Reported only for that workload.
+NCU_TRAFFIC = {("k_window_deposit", 512, 512): 2.692e9 + 1.052e9}
 
 
 def parse():
@@ -61,7 +62,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--engine", choices=["auto", "sorted", "window"], default="auto",
+    ap.add_argument("--engine", choices=["auto", "sorted", "window", "stream"], default="auto",
                     help="deposit engine (default: the library's automatic choice)")
     ap.add_argument("--fft", choices=["auto", "cufft3d"], default="auto",
                     help="forward FFT path (default: the library's choice)")
@@ -309,7 +310,7 @@ def main():
     dpos = synth.zeldovich(nside, box, seed=1 + rank, device="cuda")
     torch.cuda.synchronize()
     ctx = gp.Context(n, nrbins, timing=True)
-    ctx.set_engine({"auto": 0, "sorted": 1, "window": 2}[args.engine])
+    ctx.set_engine({"auto": 0, "sorted": 1, "window": 2, "stream": 3}[args.engine])
     ctx.set_fft_mode({"auto": 0, "cufft3d": 1}[args.fft])
 
     def step(src):
@@ -351,22 +352,22 @@ def main():
     stages = {k: v / args.steps for k, v in stages.items()}
     value = npart * world / (ms_step * 1e-3)
 
-    # roofline: the dominant kernel (k_window_deposit, or the sorted engine's
-    # whole pass), the deposit pass, and deposit + binning (SURVEY-style)
+    # roofline: the dominant kernel (k_stream_deposit / k_window_deposit, or
+    # the sorted engine's whole pass), the deposit pass, and deposit + binning
     pk_, pk_src = peaks()
     peak = float(pk_["hbm_gbs"])
     b_dep, b_bin = algorithmic_bytes(npart, n)
-    engine = {1: "sorted", 2: "window"}.get(ctx.last_engine, "?")
-    t_pass = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_"))) * 1e-3
+    engine = {1: "sorted", 2: "window", 3: "stream"}.get(ctx.last_engine, "?")
+    t_pass = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_", "stream_"))) * 1e-3
     # binning time: the fused x-axis FFT + binning kernel when it ran (it also
     # does the last FFT pass, so this overstates the binning time), else k_bin
     t_bin = (stages.get("xfft_bin", 0.0) + stages.get("bin", 0.0)) * 1e-3
-    if engine == "window":
-        t_k = stages.get("win_deposit", 0.0) * 1e-3
-        kname = "k_window_deposit"
-        traffic = (NCU_WINDOW_TRAFFIC["bytes"] if (nside, n) == (NCU_WINDOW_TRAFFIC["nside"],
-                                                                  NCU_WINDOW_TRAFFIC["grid"])
-                   else None)
+    if engine in ("window", "stream"):
+        stage = "win_deposit" if engine == "window" else "stream_deposit"
+        t_k = stages.get(stage, 0.0) * 1e-3
+        kname = "k_" + stage
+        ncu = NCU_TRAFFIC.get((kname, nside, n))
+        traffic = ncu
     else:
         t_k = t_pass
         kname = "deposit pass (sorted engine: all its kernels)"

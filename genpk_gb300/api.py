@@ -20,7 +20,7 @@ import numpy as np
 from . import native
 
 GENPK_FLAG_TIMING = 0x1
-ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW = 0, 1, 2
+ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW, ENGINE_STREAM = 0, 1, 2, 3
 FFT_AUTO, FFT_CUFFT3D = 0, 1
 
 
@@ -202,7 +202,9 @@ class Context:
         return {"tile": (v[0].value, v[1].value, v[2].value), "sort_ctas": v[3].value}
 
     def set_engine(self, engine: int):
-        """Deposit engine: ENGINE_AUTO, ENGINE_SORTED (exact) or ENGINE_WINDOW."""
+        """Deposit engine: ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW or
+        ENGINE_STREAM (identical grids; they differ in speed by particle order
+        and density)."""
         self._chk(self.lib.genpk_set_deposit_engine(self.h, int(engine)))
 
     def set_fft_mode(self, mode: int):

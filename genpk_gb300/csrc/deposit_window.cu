@@ -303,6 +303,40 @@ __device__ __noinline__ void carry_corners(const WinParams &p, acc_t *acc, const
             acc_add_global(acc, corner_index(p, c, k), (long long)sign << 32);
 }
 
+// Block epilogue of both deposit kernels: the warps' shares of the exact
+// corner mode (fixed point, 2^-(s+4) units) and the invalid-particle and
+// wait-timeout counts.
+template <bool VARMASS, bool CORNER>
+__device__ __forceinline__ void report_block(const WinParams &p, DeviceStatus *st, f2sum alt,
+                                             unsigned bad, unsigned timeouts, float mscale)
+{
+    const int lane = threadIdx.x & 31;
+    if (CORNER) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const f2sum other = {__shfl_xor_sync(0xffffffffu, alt.hi, o),
+                                 __shfl_xor_sync(0xffffffffu, alt.lo, o)};
+            alt = f2_add2(alt, other);
+        }
+        if (lane == 0) {
+            if (!VARMASS) {  // the uniform mass was factored out of the sum
+                const float mm = p.umass * mscale;
+                const float h = __fmul_rn(alt.hi, mm);
+                alt = f2sum{h, fmaf(alt.hi, mm, -h) + alt.lo * mm};
+            }
+            const long long v = __float2ll_rn(alt.hi) + __float2ll_rn(alt.lo);
+            if (v != 0)
+                atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
+        }
+    }
+    bad = __reduce_add_sync(0xffffffffu, bad);
+    timeouts = __reduce_add_sync(0xffffffffu, timeouts);
+    if (lane == 0 && bad)
+        atomicAdd(&st->bad_particles, (unsigned long long)bad);
+    if (lane == 0 && timeouts)
+        atomicAdd(&st->timeouts, (unsigned long long)timeouts);
+}
+
 template <bool VARMASS, bool CORNER>
 __global__ void __launch_bounds__(kWinThreads, 1)
     k_window_deposit(WinParams p, DeviceStatus *st, acc_t *__restrict__ acc)
@@ -500,30 +534,162 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         // window_box, so the flush needs no barrier of its own.
     }
 
-    if (CORNER) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const f2sum other = {__shfl_xor_sync(0xffffffffu, alt.hi, o),
-                                 __shfl_xor_sync(0xffffffffu, alt.lo, o)};
-            alt = f2_add2(alt, other);
+    report_block<VARMASS, CORNER>(p, st, alt, bad, timeouts, mscale);
+}
+
+// Stream mode: the window kernel's chunk pipeline without the window.  Every
+// particle's eight weights go straight to the 64-bit accumulator as L2
+// reductions (no return).  Lanes hold consecutive particles; where lane l + 1's
+// particle lies in the next z cell of lane l's (x, y) cell column (consecutive
+// particles of a lattice, or of any order that runs along z), lane l + 1 adds
+// lane l's four upper-z weights to its own four lower-z weights (one shuffle
+// each) and lane l skips those four reductions, so each such cell takes one
+// reduction for both.  The lower-z reductions of a warp cover consecutive
+// cells.  One barrier per chunk; the L2 holds the few x-planes that the
+// resident chunks touch.
+template <bool VARMASS, bool CORNER>
+__global__ void __launch_bounds__(kWinThreads, 1)
+    k_stream_deposit(WinParams p, DeviceStatus *st, acc_t *__restrict__ acc)
+{
+    extern __shared__ __align__(128) unsigned char win_smem[];
+    float *pbuf = reinterpret_cast<float *>(win_smem);  // [2][chunk * 3]
+    float *mbuf = pbuf + 6 * p.chunk;                   // [2][chunk] (VARMASS)
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    __syncthreads();
+
+    const int emax = 154 - st->fx_shift;
+    const unsigned ubits = __float_as_uint(p.umass);
+    const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
+    const int uef = (int)((ubits >> 23) & 0xffu);
+    const bool uneg = (ubits >> 31) != 0u;
+    const float mscale = ldexpf(1.f, st->fx_shift + 4);
+
+    f2sum alt = {0.f, 0.f};
+    unsigned bad = 0, timeouts = 0;
+    const int64_t c0 = blockIdx.x;
+    if (threadIdx.x == 0 && c0 < p.nchunks && chunk_by_bulk(p, c0))
+        issue_chunk<VARMASS>(p, c0, pbuf, mbuf, &bar[0]);
+
+    int k = 0;
+    for (int64_t c = c0; c < p.nchunks; c += gridDim.x, k++) {
+        const int buf = k & 1;
+        float *P = pbuf + buf * 3 * p.chunk;
+        float *M = mbuf + buf * p.chunk;
+        const int cnt = (int)min((int64_t)p.chunk, p.n - chunk_first(p, c));
+        if (chunk_by_bulk(p, c)) {
+            if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
+                timeouts++;
+        } else {
+            copy_chunk<VARMASS>(p, c, cnt, P, M);
         }
-        if (lane == 0) {
-            if (!VARMASS) {  // the uniform mass was factored out of the sum
-                const float mm = p.umass * mscale;
-                const float h = __fmul_rn(alt.hi, mm);
-                alt = f2sum{h, fmaf(alt.hi, mm, -h) + alt.lo * mm};
+        // The chunk is in place, and every thread is done with the other buffer.
+        __syncthreads();
+        if (threadIdx.x == 0 && c + gridDim.x < p.nchunks && chunk_by_bulk(p, c + gridDim.x))
+            issue_chunk<VARMASS>(p, c + gridDim.x, pbuf + (buf ^ 1) * 3 * p.chunk,
+                                 mbuf + (buf ^ 1) * p.chunk, &bar[buf ^ 1]);
+
+        // Same trip count for every lane: the merge shuffles need full warps.
+        for (int j0 = 0; j0 < cnt; j0 += blockDim.x) {
+            const int j = j0 + threadIdx.x;
+            float x = 0.f, y = 0.f, z = 0.f, m = p.umass;
+            bool valid = j < cnt;
+            if (valid) {
+                x = P[3 * j];
+                y = P[3 * j + 1];
+                z = P[3 * j + 2];
+                bool ok = fabsf(x * p.uh) <= kPosLimit && fabsf(y * p.uh) <= kPosLimit &&
+                          fabsf(z * p.uh) <= kPosLimit;
+                if (VARMASS) {
+                    m = M[j];
+                    ok = ok && fabsf(m) <= 3.4028235e38f;
+                }
+                if (!ok) {
+                    bad++;
+                    valid = false;
+                    x = y = z = 0.f;
+                }
             }
-            const long long v = __float2ll_rn(alt.hi) + __float2ll_rn(alt.lo);
-            if (v != 0)
-                atomicAdd((unsigned long long *)&st->alt_sum, (unsigned long long)v);
+            unsigned mant = umant;
+            int ef = uef;
+            bool neg = uneg;
+            if (VARMASS) {
+                const unsigned mb = __float_as_uint(m);
+                ef = (int)((mb >> 23) & 0xffu);
+                mant = (mb & 0x7fffffu) | 0x800000u;
+                neg = (mb >> 31) != 0u;
+            }
+            valid = valid && ef != 0;  // zero or subnormal mass deposits nothing
+            const int dsh = max(emax - ef, 0);
+            const AxisQ ax = split_q28(x, p.uh, p.ul, p.dims);
+            const AxisQ ay = split_q28(y, p.uh, p.ul, p.dims);
+            const AxisQ az = split_q28(z, p.uh, p.ul, p.dims);
+            if (CORNER && valid) {
+                f2sum v = corner_factor_q(ax, ay, az);
+                if (VARMASS) {
+                    const float mm = m * mscale;
+                    const float h = __fmul_rn(v.hi, mm);
+                    v = f2sum{h, fmaf(v.hi, mm, -h) + v.lo * mm};
+                }
+                if ((ax.cell + ay.cell + az.cell) & 1)
+                    v = f2sum{-v.hi, -v.lo};
+                alt = f2_add2(alt, v);
+            }
+            const uint32_t rx = kFracOne - ax.q, ry = kFracOne - ay.q, rz = kFracOne - az.q;
+            const uint32_t p00 = pair_w(rx, ry), p10 = pair_w(ax.q, ry), p01 = pair_w(rx, ay.q),
+                           p11 = pair_w(ax.q, ay.q);
+            const uint32_t zl = z_mass(rz, mant, VARMASS ? dsh : 0);
+            const uint32_t zu = z_mass(az.q, mant, VARMASS ? dsh : 0);
+            const uint32_t wu[8] = {corner_w(p00, zl), corner_w(p10, zl), corner_w(p01, zl),
+                                    corner_w(p11, zl), corner_w(p00, zu), corner_w(p10, zu),
+                                    corner_w(p01, zu), corner_w(p11, zu)};
+            int w[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                w[q] = neg ? -(int)wu[q] : (int)wu[q];
+            const int x1 = ax.cell + 1 == p.dims ? 0 : ax.cell + 1;
+            const int y1 = ay.cell + 1 == p.dims ? 0 : ay.cell + 1;
+            const int z1 = az.cell + 1 == p.dims ? 0 : az.cell + 1;
+
+            // Neighbour merge: equal keys mean both lanes valid in one (x, y)
+            // cell column (an invalid lane's key is unique and negative).
+            const int key = valid ? ax.cell * p.dims + ay.cell : -1 - lane;
+            const int key_prev = __shfl_up_sync(0xffffffffu, key, 1);
+            const int z1_prev = __shfl_up_sync(0xffffffffu, z1, 1);
+            const int key_next = __shfl_down_sync(0xffffffffu, key, 1);
+            const int z_next = __shfl_down_sync(0xffffffffu, az.cell, 1);
+            const bool take = lane > 0 && key_prev == key && z1_prev == az.cell;
+            const bool give = lane < 31 && key_next == key && z_next == z1;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int up = __shfl_up_sync(0xffffffffu, w[4 + q], 1);
+                w[q] += take ? up : 0;
+            }
+            if (valid) {
+                acc_t *r00 = acc + (size_t)ax.cell * (size_t)p.plane + (size_t)ay.cell * (size_t)p.row;
+                acc_t *r10 = acc + (size_t)x1 * (size_t)p.plane + (size_t)ay.cell * (size_t)p.row;
+                acc_t *r01 = acc + (size_t)ax.cell * (size_t)p.plane + (size_t)y1 * (size_t)p.row;
+                acc_t *r11 = acc + (size_t)x1 * (size_t)p.plane + (size_t)y1 * (size_t)p.row;
+                atomicAdd(r00 + az.cell, (acc_t)(long long)w[0]);
+                atomicAdd(r10 + az.cell, (acc_t)(long long)w[1]);
+                atomicAdd(r01 + az.cell, (acc_t)(long long)w[2]);
+                atomicAdd(r11 + az.cell, (acc_t)(long long)w[3]);
+                if (!give) {
+                    atomicAdd(r00 + z1, (acc_t)(long long)w[4]);
+                    atomicAdd(r10 + z1, (acc_t)(long long)w[5]);
+                    atomicAdd(r01 + z1, (acc_t)(long long)w[6]);
+                    atomicAdd(r11 + z1, (acc_t)(long long)w[7]);
+                }
+            }
         }
     }
-    bad = __reduce_add_sync(0xffffffffu, bad);
-    timeouts = __reduce_add_sync(0xffffffffu, timeouts);
-    if (lane == 0 && bad)
-        atomicAdd(&st->bad_particles, (unsigned long long)bad);
-    if (lane == 0 && timeouts)
-        atomicAdd(&st->timeouts, (unsigned long long)timeouts);
+    report_block<VARMASS, CORNER>(p, st, alt, bad, timeouts, mscale);
 }
 
 // Per-CTA FP64 mass partials (Kahan in FP32 first) and the max |mass|.
@@ -694,6 +860,42 @@ __global__ void __launch_bounds__(256)
         vol_out[blockIdx.x] = (long long)box.ext[0] * box.ext[1] * box.ext[2];
 }
 
+// Probe of the stream mode: over `samples` evenly spread runs of 256
+// consecutive particles, how many neighbour pairs within a warp meet the
+// stream kernel's merge condition (out[0]) out of all such pairs (out[1]).
+__global__ void __launch_bounds__(256)
+    k_stream_probe(WinParams p, int samples, unsigned long long *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t j = (((int64_t)blockIdx.x * (p.n - 256) / max(samples - 1, 1)) & ~(int64_t)31) +
+                      threadIdx.x;  // warp-aligned like the kernel's lanes
+    bool valid = j < p.n;
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (valid) {
+        x = p.pos[3 * j];
+        y = p.pos[3 * j + 1];
+        z = p.pos[3 * j + 2];
+        valid = fabsf(x * p.uh) <= kPosLimit && fabsf(y * p.uh) <= kPosLimit &&
+                fabsf(z * p.uh) <= kPosLimit;
+        if (!valid)
+            x = y = z = 0.f;
+    }
+    const AxisQ ax = split_q28(x, p.uh, p.ul, p.dims);
+    const AxisQ ay = split_q28(y, p.uh, p.ul, p.dims);
+    const AxisQ az = split_q28(z, p.uh, p.ul, p.dims);
+    const int z1 = az.cell + 1 == p.dims ? 0 : az.cell + 1;
+    const int key = valid ? ax.cell * p.dims + ay.cell : -1 - lane;
+    const int key_next = __shfl_down_sync(0xffffffffu, key, 1);
+    const int z_next = __shfl_down_sync(0xffffffffu, az.cell, 1);
+    const bool pair = lane < 31 && j + 1 < p.n;
+    const unsigned merged = __popc(__ballot_sync(0xffffffffu, pair && key_next == key && z_next == z1));
+    const unsigned pairs = __popc(__ballot_sync(0xffffffffu, pair));
+    if (lane == 0) {
+        atomicAdd(out, (unsigned long long)merged);
+        atomicAdd(out + 1, (unsigned long long)pairs);
+    }
+}
+
 WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk)
 {
     WinParams p;
@@ -740,10 +942,26 @@ cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
     return cudaGetLastError();
 }
 
+cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
+                         unsigned long long *out_dev, int samples, cudaStream_t stream,
+                         int64_t *launches)
+{
+    const WinParams p = make_win_params(g, a, kStreamChunk);
+    cudaError_t err = cudaMemsetAsync(out_dev, 0, 2 * sizeof(unsigned long long), stream);
+    if (err != cudaSuccess)
+        return err;
+    if (a.n >= 256) {
+        k_stream_probe<<<samples, 256, 0, stream>>>(p, samples, out_dev);
+        (*launches)++;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, unsigned long long *acc,
-                                int num_sms, DeviceStatus *dstat, cudaStream_t stream,
-                                int64_t *launches, StageHook hook, void *hook_user)
+                                bool stream_mode, double *mass_part, int mass_ctas,
+                                unsigned long long *acc, int num_sms, DeviceStatus *dstat,
+                                cudaStream_t stream, int64_t *launches, StageHook hook,
+                                void *hook_user)
 {
     auto mark = [&](const char *name) {
         (*launches)++;
@@ -770,14 +988,18 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
     const WinParams p = make_win_params(g, a, chunk);
     if (p.nchunks > 0) {
         const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
-        const int smem = p.win_off + 4 * p.cap;
+        // stream mode: the two chunk buffers only
+        const int smem = stream_mode ? p.win_off : p.win_off + 4 * p.cap;
         auto kern = a.masses ? (p.corner ? k_window_deposit<true, true> : k_window_deposit<true, false>)
                              : (p.corner ? k_window_deposit<false, true> : k_window_deposit<false, false>);
+        if (stream_mode)
+            kern = a.masses ? (p.corner ? k_stream_deposit<true, true> : k_stream_deposit<true, false>)
+                            : (p.corner ? k_stream_deposit<false, true> : k_stream_deposit<false, false>);
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem)) != cudaSuccess)
             return err;
         kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, acc);
-        mark("win_deposit");
+        mark(stream_mode ? "stream_deposit" : "win_deposit");
         if ((err = cudaGetLastError()) != cudaSuccess)
             return err;
     }

@@ -114,11 +114,19 @@ int window_cap_cells(int chunk, bool variable_masses);
 // Window volume (cells) of `samples` evenly spread chunks, written to vol_dev.
 cudaError_t window_probe(const DepositGeom &g, const DepositArgs &a, int chunk,
                          long long *vol_dev, int samples, cudaStream_t stream, int64_t *launches);
+// Chunk length of the stream mode (no window: the chunk buffers only).
+constexpr int kStreamChunk = 4096;
+// Stream-mode merge count (out_dev[0]) out of neighbour pairs (out_dev[1]) over
+// `samples` runs of 256 consecutive particles (none when fewer than 256).
+cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
+                         unsigned long long *out_dev, int samples, cudaStream_t stream,
+                         int64_t *launches);
 // One window-engine pass; mass_part needs mass_ctas doubles (variable masses);
-// acc (nfloat 64-bit integers) is the exact accumulator.
+// acc (nfloat 64-bit integers) is the exact accumulator.  stream_mode: the
+// stream mode (reductions straight to acc, neighbour-merged), no windows.
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
-                                double *mass_part, int mass_ctas, unsigned long long *acc,
-                                int num_sms, DeviceStatus *dstat,
+                                bool stream_mode, double *mass_part, int mass_ctas,
+                                unsigned long long *acc, int num_sms, DeviceStatus *dstat,
                                 cudaStream_t stream, int64_t *launches, StageHook hook,
                                 void *hook_user);
 

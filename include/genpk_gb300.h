@@ -171,20 +171,26 @@ int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *ti
  * 8^3 and 16^3).  The sorted engine's grid does not depend on it. */
 int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z);
 
-/* Deposit engines.
- *  SORTED: counting sort into cell tiles, exact 64-bit fixed-point shared
- *          accumulation; bit-reproducible whatever the particle order.
+/* Deposit engines.  All three add the same integer CIC weights exactly (64-bit
+ * fixed point) and round each cell once: their grids are bit-identical and do
+ * not depend on particle order.
+ *  SORTED: counting sort into cell tiles, shared-memory tile sums; any order.
  *  WINDOW: for spatially coherent particle order (lattice or Peano-Hilbert
- *          order of most snapshots): per-chunk shared windows flushed with
- *          FP32 atomics, no sort; the last bits depend on summation order.
- *  AUTO (default): WINDOW when a sample of particle chunks is coherent, else
- *          SORTED. */
+ *          order of most snapshots): per-chunk shared windows, no sort.
+ *  STREAM: the window engine's chunk pipeline without windows: reductions
+ *          straight to the accumulator, merged between neighbouring particles
+ *          of one z cell column; for coherent order at about one particle per
+ *          cell, where windows merge few adds.
+ *  AUTO (default): from a sample of particle chunks, STREAM or WINDOW when the
+ *          order is coherent (by window cells per particle), else SORTED. */
 #define GENPK_ENGINE_AUTO 0
 #define GENPK_ENGINE_SORTED 1
 #define GENPK_ENGINE_WINDOW 2
+#define GENPK_ENGINE_STREAM 3
 int genpk_set_deposit_engine(genpk_ctx *ctx, int engine);
 
-/* Engine the most recent deposit pass used (GENPK_ENGINE_SORTED or _WINDOW). */
+/* Engine the most recent deposit pass used (GENPK_ENGINE_SORTED, _WINDOW or
+ * _STREAM). */
 int genpk_last_deposit_engine(const genpk_ctx *ctx);
 
 /* Forward-FFT path (replaces the driver-owned FFTW plan, gen-pk.cpp:186-193,233).

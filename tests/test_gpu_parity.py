@@ -200,10 +200,14 @@ def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
         assert np.array_equal(g, grids[0])
 
 
+CHUNKED = {"window": 2, "stream": 3}  # api.ENGINE_WINDOW, api.ENGINE_STREAM
+
+
+@pytest.mark.parametrize("engine", ["window", "stream"])
 @pytest.mark.parametrize("var", [False, True])
-def test_window_engine_matches_oracle(gp, var):
+def test_window_engine_matches_oracle(gp, var, engine):
     """Lattice-ordered particles through the window engine (shared windows
-    per chunk, no sort)."""
+    per chunk, no sort) and its stream mode (neighbour-merged reductions)."""
     from genpk_gb300 import synth
     dims, box, nrbins = 128, 25000.0, 64
     pos = synth.zeldovich(128, box, seed=3)
@@ -213,19 +217,20 @@ def test_window_engine_matches_oracle(gp, var):
     ref = O.deposit(pos, box, dims, masses, mass)
     pr, cr, _ = O.pk(pos, box, dims, nrbins, masses, mass, m_norm=m)
     with gp.Context(dims, nrbins) as ctx:
-        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.set_engine(CHUNKED[engine])
         ctx.deposit(0, box, pos, masses, mass)
         ctx.sync()
-        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        assert ctx.last_engine == CHUNKED[engine]
         grid_close(ctx.read_field(0), ref, tol=1e-6)
         p, c, _ = ctx.power(0, 0, m, m)
     assert np.array_equal(c, cr)
     bins_close(p, pr, c)
 
 
+@pytest.mark.parametrize("engine", ["window", "stream"])
 @pytest.mark.parametrize("case", ["unaligned_tail", "dense_carry", "negative_mass_carry",
                                   "tiny_grid", "grid_8"])
-def test_window_engine_edge_cases(gp, case):
+def test_window_engine_edge_cases(gp, case, engine):
     """Window-engine paths the lattice case does not reach: an input pointer
     that is not 16-byte aligned (chunks copied by threads, not bulk copies) with
     a partial last chunk; window cells whose 32-bit fixed-point sum overflows
@@ -259,10 +264,10 @@ def test_window_engine_edge_cases(gp, case):
         dev = torch.from_numpy(pos).cuda()
     ref = O.deposit(pos, box, dims, masses, mass)
     with gp.Context(dims, 8) as ctx:
-        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.set_engine(CHUNKED[engine])
         ctx.deposit(0, box, dev, None if masses is None else torch.from_numpy(masses).cuda(), mass)
         ctx.sync()
-        assert ctx.last_engine == gp.api.ENGINE_WINDOW
+        assert ctx.last_engine == CHUNKED[engine]
         grid_close(ctx.read_field(0), ref, tol=1e-6)
 
 
@@ -286,7 +291,7 @@ def test_pinned_host_input_read_in_place(gp, var):
     dmass = hmass.cuda() if var else None
     with gp.Context(dims, 16) as ctx:
         out = {}
-        for eng in (gp.api.ENGINE_WINDOW, gp.api.ENGINE_SORTED):
+        for eng in (gp.api.ENGINE_WINDOW, gp.api.ENGINE_STREAM, gp.api.ENGINE_SORTED):
             ctx.set_engine(eng)
             for name, p_, m_ in (("dev", dpos, dmass), ("pinned", hpos, hmass)):
                 ctx.zero(0)
@@ -294,13 +299,15 @@ def test_pinned_host_input_read_in_place(gp, var):
                 ctx.sync()
                 assert ctx.last_engine == eng
                 out[(eng, name)] = ctx.read_field(0)
-    grid_close(out[(gp.api.ENGINE_WINDOW, "pinned")], out[(gp.api.ENGINE_WINDOW, "dev")], tol=1e-6)
-    assert np.array_equal(out[(gp.api.ENGINE_SORTED, "pinned")], out[(gp.api.ENGINE_SORTED, "dev")])
+    for eng in (gp.api.ENGINE_WINDOW, gp.api.ENGINE_STREAM, gp.api.ENGINE_SORTED):
+        assert np.array_equal(out[(eng, "pinned")], out[(eng, "dev")])
+        assert np.array_equal(out[(eng, "pinned")], out[(gp.api.ENGINE_SORTED, "dev")])
     grid_close(out[(gp.api.ENGINE_WINDOW, "pinned")], O.deposit(pos, box, dims, masses, mass),
                tol=1e-6)
 
 
-def test_window_engine_reports_non_finite(gp):
+@pytest.mark.parametrize("engine", ["window", "stream"])
+def test_window_engine_reports_non_finite(gp, engine):
     from genpk_gb300 import synth
     dims, box = 32, 100.0
     pos = synth.zeldovich(32, box, seed=14)
@@ -310,7 +317,7 @@ def test_window_engine_reports_non_finite(gp):
     keep = np.ones(len(pos), bool)
     keep[[5, 9000]] = False
     with gp.Context(dims, 8) as ctx:
-        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.set_engine(CHUNKED[engine])
         ctx.deposit(0, box, bad, None, 1.0)
         with pytest.raises(gp.GenPKError) as e:
             ctx.sync()
@@ -319,16 +326,17 @@ def test_window_engine_reports_non_finite(gp):
     grid_close(g, O.deposit(pos[keep], box, dims, None, 1.0), tol=1e-6)
 
 
-def test_window_engine_direct_fallback_on_random_order(gp):
-    """Randomly ordered particles: no chunk fits a window, every corner takes a
-    global atomic.  Still correct."""
+@pytest.mark.parametrize("engine", ["window", "stream"])
+def test_window_engine_direct_fallback_on_random_order(gp, engine):
+    """Randomly ordered particles: no chunk fits a window (every corner takes a
+    global reduction), no neighbours merge.  Still correct."""
     from genpk_gb300 import synth
     dims, box, nrbins = 64, 1000.0, 32
     pos = synth.uniform(300000, box, seed=4)
     m = O.total_mass(len(pos), None, 1.0)
     pr, cr, _ = O.pk(pos, box, dims, nrbins, None, 1.0, m_norm=m)
     with gp.Context(dims, nrbins) as ctx:
-        ctx.set_engine(gp.api.ENGINE_WINDOW)
+        ctx.set_engine(CHUNKED[engine])
         ctx.deposit(0, box, pos, None, 1.0)
         grid_close(ctx.read_field(0), O.deposit(pos, box, dims, None, 1.0), tol=1e-6)
         p, c, _ = ctx.power(0, 0, m, m)
@@ -336,6 +344,8 @@ def test_window_engine_direct_fallback_on_random_order(gp):
 
 
 def test_auto_engine_choice(gp):
+    """A lattice at one particle per cell (consecutive particles one z cell
+    apart): stream mode; at eight per cell: windows; random order: sorted."""
     from genpk_gb300 import synth
     box = 1000.0
     lattice = synth.zeldovich(128, box, seed=5)              # 2^21 particles, coherent
@@ -343,7 +353,12 @@ def test_auto_engine_choice(gp):
     with gp.Context(128, 16) as ctx:
         ctx.deposit(0, box, lattice, None, 1.0)
         ctx.sync()
+        assert ctx.last_engine == gp.api.ENGINE_STREAM
+    with gp.Context(64, 16) as ctx:
+        ctx.deposit(0, box, lattice, None, 1.0)
+        ctx.sync()
         assert ctx.last_engine == gp.api.ENGINE_WINDOW
+    with gp.Context(128, 16) as ctx:
         ctx.zero(0)
         ctx.deposit(0, box, rand, None, 1.0)
         ctx.sync()
@@ -370,7 +385,7 @@ def test_sparse_lattice_picks_a_shorter_window_chunk(gp):
 
 @pytest.mark.parametrize("var", [False, True])
 def test_window_and_sorted_engines_agree_bit_for_bit(gp, var):
-    """Both engines add the same integer CIC weights (28-bit fractions from the
+    """All engines add the same integer CIC weights (28-bit fractions from the
     exact split) exactly and round each cell once: identical grids, also when
     a grid accumulates two passes."""
     import torch
@@ -380,7 +395,7 @@ def test_window_and_sorted_engines_agree_bit_for_bit(gp, var):
     masses = (torch.linspace(0.3, 2.0, len(pos)) if var else torch.ones(len(pos))).cuda()
     with gp.Context(dims, 16) as ctx:
         grids = []
-        for eng in (gp.api.ENGINE_SORTED, gp.api.ENGINE_WINDOW):
+        for eng in (gp.api.ENGINE_SORTED, gp.api.ENGINE_WINDOW, gp.api.ENGINE_STREAM):
             ctx.set_engine(eng)
             ctx.zero(0)
             if var:
@@ -393,9 +408,10 @@ def test_window_and_sorted_engines_agree_bit_for_bit(gp, var):
             assert ctx.last_engine == eng
             grids.append(ctx.read_field(0))
     assert np.array_equal(grids[0], grids[1])
+    assert np.array_equal(grids[0], grids[2])
 
 
-@pytest.mark.parametrize("engine", ["sorted", "window"])
+@pytest.mark.parametrize("engine", ["sorted", "window", "stream"])
 def test_faint_high_k_bins_of_a_smooth_lattice(gp, engine):
     """128^3 Zel'dovich lattice (the GPU generator, L = 25000, 64 bins): the
     highest-k bins hold ~1e-10 of the peak power and are sensitive to the
@@ -408,7 +424,7 @@ def test_faint_high_k_bins_of_a_smooth_lattice(gp, engine):
     m = O.total_mass(len(pos), None, 1.0)
     pr, cr, _ = O.pk(pos, box, n, nrb, None, 1.0, m_norm=m)
     with gp.Context(n, nrb) as ctx:
-        ctx.set_engine(gp.api.ENGINE_SORTED if engine == "sorted" else gp.api.ENGINE_WINDOW)
+        ctx.set_engine({"sorted": 1, "window": 2, "stream": 3}[engine])
         ctx.deposit(0, box, dpos, None, 1.0)
         p, c, _ = ctx.power(0, 0, m, m)
     assert np.array_equal(c, cr)
