@@ -200,15 +200,22 @@ __device__ __forceinline__ uint32_t corner_w(uint32_t p, uint32_t z)
 // a coherent error of ~1e-4 in the single-mode last bin of a 128^3 lattice.
 __device__ __forceinline__ f2sum corner_factor_q(const AxisQ &x, const AxisQ &y, const AxisQ &z)
 {
+    // (u_x + l_x)(u_y + l_y) with l = -2 xl: P exact to ~2^-47 relative plus
+    // E = its rounding error + u_x l_y + l_x u_y + l_x l_y; then times
+    // (u_z + l_z) the same way, so the first-, second- and third-order l
+    // terms all enter E3 (each in FP32).
+    const float lx = -2.f * x.xl, ly = -2.f * y.xl, lz = -2.f * z.xl;
     const float p = __fmul_rn(x.u, y.u);
-    const float pl = fmaf(x.u, y.u, -p);
-    const float q = __fmul_rn(p, z.u);
-    const float ql = fmaf(p, z.u, -q) + pl * z.u;
-    const float yz = y.u * z.u, xz = x.u * z.u, xy = x.u * y.u;
-    const float t1 = x.xl * yz + y.xl * xz + z.xl * xy;
-    const float t2 = x.xl * y.xl * z.u + x.xl * z.xl * y.u + y.xl * z.xl * x.u;
-    const float t3 = x.xl * y.xl * z.xl;
-    return {q, ql + ((-2.f * t1 + 4.f * t2) - 8.f * t3)};
+    float e = fmaf(x.u, y.u, -p);
+    e = fmaf(x.u, ly, e);
+    e = fmaf(lx, y.u, e);
+    e = fmaf(lx, ly, e);
+    const float p3 = __fmul_rn(p, z.u);
+    float e3 = fmaf(p, z.u, -p3);
+    e3 = fmaf(p, lz, e3);
+    e3 = fmaf(e, z.u, e3);
+    e3 = fmaf(e, lz, e3);
+    return {p3, e3};
 }
 
 __device__ __forceinline__ bool finite3(float a, float b, float c)

@@ -37,6 +37,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace genpk {
 namespace {
@@ -547,7 +548,14 @@ __global__ void __launch_bounds__(kWinThreads, 1)
 // reduction for both.  The lower-z reductions of a warp cover consecutive
 // cells.  One barrier per chunk; the L2 holds the few x-planes that the
 // resident chunks touch.
-template <bool VARMASS, bool CORNER>
+// Accumulator element of cell (x, y, z): 32-bit arithmetic where the grid has
+// fewer than 2^32 elements (WIDE = false), else 64-bit.
+template <bool WIDE>
+struct CellIndex {
+    typedef typename std::conditional<WIDE, int64_t, uint32_t>::type T;
+};
+
+template <bool VARMASS, bool CORNER, bool WIDE>
 __global__ void __launch_bounds__(kWinThreads, 1)
     k_stream_deposit(WinParams p, DeviceStatus *st, acc_t *__restrict__ acc)
 {
@@ -604,8 +612,10 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                 x = P[3 * j];
                 y = P[3 * j + 1];
                 z = P[3 * j + 2];
-                bool ok = fabsf(x * p.uh) <= kPosLimit && fabsf(y * p.uh) <= kPosLimit &&
-                          fabsf(z * p.uh) <= kPosLimit;
+                // the products split_q28 forms first
+                bool ok = fabsf(__fmul_rn(x, p.uh)) <= kPosLimit &&
+                          fabsf(__fmul_rn(y, p.uh)) <= kPosLimit &&
+                          fabsf(__fmul_rn(z, p.uh)) <= kPosLimit;
                 if (VARMASS) {
                     m = M[j];
                     ok = ok && fabsf(m) <= 3.4028235e38f;
@@ -649,42 +659,61 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             const uint32_t wu[8] = {corner_w(p00, zl), corner_w(p10, zl), corner_w(p01, zl),
                                     corner_w(p11, zl), corner_w(p00, zu), corner_w(p10, zu),
                                     corner_w(p01, zu), corner_w(p11, zu)};
+            // Variable masses carry their sign into the merge; a uniform mass's
+            // sign is applied at the reductions.
             int w[8];
 #pragma unroll
             for (int q = 0; q < 8; q++)
-                w[q] = neg ? -(int)wu[q] : (int)wu[q];
-            const int x1 = ax.cell + 1 == p.dims ? 0 : ax.cell + 1;
-            const int y1 = ay.cell + 1 == p.dims ? 0 : ay.cell + 1;
-            const int z1 = az.cell + 1 == p.dims ? 0 : az.cell + 1;
+                w[q] = (VARMASS && neg) ? -(int)wu[q] : (int)wu[q];
 
-            // Neighbour merge: equal keys mean both lanes valid in one (x, y)
-            // cell column (an invalid lane's key is unique and negative).
-            const int key = valid ? ax.cell * p.dims + ay.cell : -1 - lane;
-            const int key_prev = __shfl_up_sync(0xffffffffu, key, 1);
-            const int z1_prev = __shfl_up_sync(0xffffffffu, z1, 1);
-            const int key_next = __shfl_down_sync(0xffffffffu, key, 1);
-            const int z_next = __shfl_down_sync(0xffffffffu, az.cell, 1);
-            const bool take = lane > 0 && key_prev == key && z1_prev == az.cell;
-            const bool give = lane < 31 && key_next == key && z_next == z1;
+            // Accumulator elements of the lower-z corner cells (x, y, z) and the
+            // +1 steps, wrapped periodically.
+            typedef typename CellIndex<WIDE>::T I;
+            const I i000 = (I)ax.cell * (I)p.plane + (I)(ay.cell * p.row + az.cell);
+            const I dx = ax.cell + 1 == p.dims ? -(I)(p.dims - 1) * (I)p.plane : (I)p.plane;
+            const I dy = (I)(ay.cell + 1 == p.dims ? -(p.dims - 1) * p.row : p.row);
+            const I dz = (I)(az.cell + 1 == p.dims ? -(p.dims - 1) : 1);
+
+            // Neighbour merge: lane l + 1 takes lane l's upper-z weights when its
+            // lower-z cell is lane l's upper-z cell (same x, y cells: the element
+            // index fixes all three).  Invalid lanes hold two distinct
+            // sentinels that no element index equals.
+            const I lower = valid ? i000 : ~(I)0;
+            const I upper = valid ? i000 + dz : ~(I)0 - 1;
+            const I upper_prev = __shfl_up_sync(0xffffffffu, upper, 1);
+            const I lower_next = __shfl_down_sync(0xffffffffu, lower, 1);
+            const bool take = lane > 0 && upper_prev == lower;
+            const bool give = lane < 31 && lower_next == upper;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int up = __shfl_up_sync(0xffffffffu, w[4 + q], 1);
                 w[q] += take ? up : 0;
             }
             if (valid) {
-                acc_t *r00 = acc + (size_t)ax.cell * (size_t)p.plane + (size_t)ay.cell * (size_t)p.row;
-                acc_t *r10 = acc + (size_t)x1 * (size_t)p.plane + (size_t)ay.cell * (size_t)p.row;
-                acc_t *r01 = acc + (size_t)ax.cell * (size_t)p.plane + (size_t)y1 * (size_t)p.row;
-                acc_t *r11 = acc + (size_t)x1 * (size_t)p.plane + (size_t)y1 * (size_t)p.row;
-                atomicAdd(r00 + az.cell, (acc_t)(long long)w[0]);
-                atomicAdd(r10 + az.cell, (acc_t)(long long)w[1]);
-                atomicAdd(r01 + az.cell, (acc_t)(long long)w[2]);
-                atomicAdd(r11 + az.cell, (acc_t)(long long)w[3]);
-                if (!give) {
-                    atomicAdd(r00 + z1, (acc_t)(long long)w[4]);
-                    atomicAdd(r10 + z1, (acc_t)(long long)w[5]);
-                    atomicAdd(r01 + z1, (acc_t)(long long)w[6]);
-                    atomicAdd(r11 + z1, (acc_t)(long long)w[7]);
+                const I i100 = i000 + dx, i010 = i000 + dy, i110 = i100 + dy;
+                if (!VARMASS && !uneg) {  // positive uniform mass: no sign extension
+                    atomicAdd(acc + i000, (acc_t)(unsigned)w[0]);
+                    atomicAdd(acc + i100, (acc_t)(unsigned)w[1]);
+                    atomicAdd(acc + i010, (acc_t)(unsigned)w[2]);
+                    atomicAdd(acc + i110, (acc_t)(unsigned)w[3]);
+                    if (!give) {
+                        atomicAdd(acc + (i000 + dz), (acc_t)(unsigned)w[4]);
+                        atomicAdd(acc + (i100 + dz), (acc_t)(unsigned)w[5]);
+                        atomicAdd(acc + (i010 + dz), (acc_t)(unsigned)w[6]);
+                        atomicAdd(acc + (i110 + dz), (acc_t)(unsigned)w[7]);
+                    }
+                } else {
+                    const long long sg = (!VARMASS && uneg) ? -1 : 1;
+                    atomicAdd(acc + i000, (acc_t)(sg * w[0]));
+                    atomicAdd(acc + i100, (acc_t)(sg * w[1]));
+                    atomicAdd(acc + i010, (acc_t)(sg * w[2]));
+                    atomicAdd(acc + i110, (acc_t)(sg * w[3]));
+                    if (!give) {
+                        atomicAdd(acc + (i000 + dz), (acc_t)(sg * w[4]));
+                        atomicAdd(acc + (i100 + dz), (acc_t)(sg * w[5]));
+                        atomicAdd(acc + (i010 + dz), (acc_t)(sg * w[6]));
+                        atomicAdd(acc + (i110 + dz), (acc_t)(sg * w[7]));
+                    }
                 }
             }
         }
@@ -992,9 +1021,17 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         const int smem = stream_mode ? p.win_off : p.win_off + 4 * p.cap;
         auto kern = a.masses ? (p.corner ? k_window_deposit<true, true> : k_window_deposit<true, false>)
                              : (p.corner ? k_window_deposit<false, true> : k_window_deposit<false, false>);
-        if (stream_mode)
-            kern = a.masses ? (p.corner ? k_stream_deposit<true, true> : k_stream_deposit<true, false>)
-                            : (p.corner ? k_stream_deposit<false, true> : k_stream_deposit<false, false>);
+        // 32-bit element indices: every index and both sentinels fit
+        if (stream_mode && g.grid.nfloat < ((int64_t)1 << 32) - 2)
+            kern = a.masses ? (p.corner ? k_stream_deposit<true, true, false>
+                                        : k_stream_deposit<true, false, false>)
+                            : (p.corner ? k_stream_deposit<false, true, false>
+                                        : k_stream_deposit<false, false, false>);
+        else if (stream_mode)
+            kern = a.masses ? (p.corner ? k_stream_deposit<true, true, true>
+                                        : k_stream_deposit<true, false, true>)
+                            : (p.corner ? k_stream_deposit<false, true, true>
+                                        : k_stream_deposit<false, false, true>);
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         smem)) != cudaSuccess)
             return err;
