@@ -306,32 +306,39 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         // stay small per particle (the flush visits every window cell).
         const int samples = 64, nq = (int)(sizeof(kWindowChunks) / sizeof(kWindowChunks[0]));
         GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)samples * nq + 2));
-        for (int q = 0; q < nq; q++)
-            GENPK_CUDA(window_probe(g, a, kWindowChunks[q], ctx->d_probe + (size_t)q * samples,
-                                    samples, ctx->stream, &ctx->launches));
-        unsigned long long *merge_dev =
-            reinterpret_cast<unsigned long long *>(ctx->d_probe + (size_t)samples * nq);
-        GENPK_CUDA(stream_probe(g, a, merge_dev, samples, ctx->stream, &ctx->launches));
         long long vol[4 * 64 + 2];
-        GENPK_CUDA(cudaMemcpyAsync(vol, ctx->d_probe, sizeof(long long) * (samples * nq + 2),
-                                   cudaMemcpyDeviceToHost, ctx->stream));
-        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-        const long long merges = vol[samples * nq], pairs = vol[samples * nq + 1];
-        const bool stream_order = pairs > 0 && (double)merges >= kStreamMergeRate * (double)pairs;
+        bool stream_order = false;
+        if (engine == GENPK_ENGINE_AUTO) {  // the stream probe first: it may settle it
+            unsigned long long *merge_dev =
+                reinterpret_cast<unsigned long long *>(ctx->d_probe + (size_t)samples * nq);
+            GENPK_CUDA(stream_probe(g, a, merge_dev, samples, ctx->stream, &ctx->launches));
+            GENPK_CUDA(cudaMemcpyAsync(vol, merge_dev, 2 * sizeof(long long),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            stream_order = vol[1] > 0 && (double)vol[0] >= kStreamMergeRate * (double)vol[1];
+        }
         int best = -1;
-        for (int q = 0; q < nq && best < 0; q++) {
-            const int c = kWindowChunks[q];
-            const int got = (int)std::min<int64_t>(samples, (n + c - 1) / c);
-            const long long cap = window_cap_cells(c, masses != nullptr);
-            int fit = 0;
-            double cells = 0.0;
-            for (int i = 0; i < got; i++) {
-                fit += vol[q * samples + i] <= (long long)(0.9 * cap) ? 1 : 0;
-                cells += (double)vol[q * samples + i];
+        if (!stream_order) {
+            for (int q = 0; q < nq; q++)
+                GENPK_CUDA(window_probe(g, a, kWindowChunks[q], ctx->d_probe + (size_t)q * samples,
+                                        samples, ctx->stream, &ctx->launches));
+            GENPK_CUDA(cudaMemcpyAsync(vol, ctx->d_probe, sizeof(long long) * samples * nq,
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            for (int q = 0; q < nq && best < 0; q++) {
+                const int c = kWindowChunks[q];
+                const int got = (int)std::min<int64_t>(samples, (n + c - 1) / c);
+                const long long cap = window_cap_cells(c, masses != nullptr);
+                int fit = 0;
+                double cells = 0.0;
+                for (int i = 0; i < got; i++) {
+                    fit += vol[q * samples + i] <= (long long)(0.9 * cap) ? 1 : 0;
+                    cells += (double)vol[q * samples + i];
+                }
+                if (got > 0 && fit * 10 >= got * 9 &&
+                    cells / ((double)got * c) <= kWindowMaxCellsPerParticle)
+                    best = q;
             }
-            if (got > 0 && fit * 10 >= got * 9 &&
-                cells / ((double)got * c) <= kWindowMaxCellsPerParticle)
-                best = q;
         }
         if (engine == GENPK_ENGINE_AUTO)
             engine = stream_order ? GENPK_ENGINE_STREAM
