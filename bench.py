@@ -43,10 +43,11 @@ METRIC = ("particles/s + ms/spectrum at 512^3 grid vs FP64 oracle; "
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # dram__bytes_read.sum + dram__bytes_write.sum of one deposit-kernel launch,
 # from ncu captures of the default workload (512^3 Zel'dovich particles onto a
-# 512^3 grid, uniform mass), keyed by (kernel, particles per side, grid).
-# k_window_deposit: 2.692 GB read (positions 1.61 GB + the 64-bit accumulator's
-# lines) + 1.052 GB written (the accumulator).  Reported only for that workload.
-NCU_TRAFFIC = {("k_window_deposit", 512, 512): 2.692e9 + 1.052e9}
+# 512^3 grid, uniform mass), keyed by (kernel, particles per side, grid): the
+# positions (1.61 GB) and the 64-bit accumulator's lines read, the accumulator
+# written.  Reported only for that workload.
+NCU_TRAFFIC = {("k_stream_deposit", 512, 512): 2.691e9 + 1.036e9,
+               ("k_window_deposit", 512, 512): 2.692e9 + 1.052e9}
 
 
 def parse():
@@ -66,7 +67,8 @@ def parse():
                     help="deposit engine (default: the library's automatic choice)")
     ap.add_argument("--fft", choices=["auto", "cufft3d"], default="auto",
                     help="forward FFT path (default: the library's choice)")
-    ap.add_argument("--workload", choices=["zeldovich", "multispecies"], default="zeldovich",
+    ap.add_argument("--workload", choices=["zeldovich", "uniform", "multispecies"],
+                    default="zeldovich",
                     help="zeldovich: one species (sizes from --nside/--grid/--box); "
                          "multispecies: DM 256^3 + gas 256^3 + 1.2e7 lognormal stars on a "
                          "512^3 grid, 3 auto + 3 cross spectra per step")
@@ -181,15 +183,15 @@ def reference_arm(args):
     world, rank, _ = dist_setup("gloo")
     if rank != 0:
         return
-    from genpk_gb300 import synth
     n, nside = args.grid, args.nside
     npart = nside ** 3
-    pos = synth.zeldovich(nside, args.box, seed=1)
+    pos = positions(args, seed=1)
     sample = min(npart, 1 << 24)
     times = []
     cores = 1
     for it in range(args.warmup + args.steps):
-        _, _, t, ndep = cpu_pipeline(pos, args.box, n, args.nrbins, 1.0, sample=sample)
+        _, _, t, ndep = cpu_pipeline(pos, args.box, n, args.nrbins, particle_mass(args),
+                                     sample=sample)
         cores = t["cores"]
         full = t["deposit"] * npart / ndep + t["fft"] + t["bin"]
         if it >= args.warmup:
@@ -200,7 +202,8 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particles/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tstep * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice)",
+        "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic (seeded, {'uniform random' if args.workload == 'uniform' else 'Zeldovich lattice'})",
         "config": config_dict(args, npart),
         "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
                          "sample": f"each step: deposit of the first {sample} particles "
@@ -211,8 +214,23 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def positions(args, seed, device="cpu"):
+    """nside^3 particles: a Zel'dovich lattice (lattice order), or i.i.d.
+    uniform positions in [0, box) (the 128^3 Gadget-snapshot configuration)."""
+    from genpk_gb300 import synth
+    if args.workload == "uniform":
+        return synth.uniform(args.nside ** 3, args.box, seed=seed, device=device)
+    return synth.zeldovich(args.nside, args.box, seed=seed, device=device)
+
+
+def particle_mass(args):
+    return 1.0e-2 if args.workload == "uniform" else 1.0
+
+
 def config_dict(args, npart):
-    return {"workload": (f"Zel'dovich lattice {args.nside}^3 particles, L={args.box:g} kpc/h, "
+    kind = ("uniform random particles (mass 1e-2)" if args.workload == "uniform"
+            else "Zel'dovich lattice particles")
+    return {"workload": (f"{kind}, {args.nside}^3 particles, L={args.box:g} kpc/h, "
                          f"FP32 {args.grid}^3 grid, {args.nrbins} log-k bins, auto spectrum"),
             "particles": npart, "grid": args.grid, "nrbins": args.nrbins, "boxsize": args.box,
             "l2": f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions per step)",
@@ -300,14 +318,13 @@ def main():
     world, rank, local = dist_setup("nccl")
     torch.cuda.set_device(local)
     import genpk_gb300 as gp
-    from genpk_gb300 import synth
     from oracle import oracle as O
 
     n, nrbins, box, nside = args.grid, args.nrbins, args.box, args.nside
     npart = nside ** 3
-    mass = 1.0
+    mass = particle_mass(args)
     m_norm = O.total_mass(npart, None, mass)
-    dpos = synth.zeldovich(nside, box, seed=1 + rank, device="cuda")
+    dpos = positions(args, seed=1 + rank, device="cuda")
     torch.cuda.synchronize()
     ctx = gp.Context(n, nrbins, timing=True)
     ctx.set_engine({"auto": 0, "sorted": 1, "window": 2, "stream": 3}[args.engine])
@@ -388,7 +405,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded Zel'dovich lattice generated on the GPU",
+            "data": ("synthetic: seeded uniform random positions generated on the GPU"
+                     if args.workload == "uniform"
+                     else "synthetic: seeded Zel'dovich lattice generated on the GPU"),
             "config": config_dict(args, npart), "ms_per_spectrum": ms_step,
             "wall_ms_per_step": wall / args.steps * 1e3,
             "stages_ms": {k: round(v, 5) for k, v in stages.items()},
