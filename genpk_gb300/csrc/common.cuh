@@ -93,6 +93,24 @@ __device__ __forceinline__ f2sum f2_add2(f2sum a, f2sum b)
     return renorm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
+// acc += v for a running sum kept as an unnormalised pair: hi is the rounded
+// sum of the high parts, lo collects their exact rounding errors and the low
+// parts (the pair is renormalised only when sums are combined at the end).
+__device__ __forceinline__ void f2_accumulate(f2sum &acc, f2sum v)
+{
+    const f2sum s = two_sum(acc.hi, v.hi);
+    acc.hi = s.hi;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, v.lo));
+}
+
+// v * (-1)^parity (sign flips of both parts; parity in bit 0).
+__device__ __forceinline__ f2sum f2_signed(f2sum v, int parity)
+{
+    const unsigned flip = (unsigned)parity << 31;
+    return {__uint_as_float(__float_as_uint(v.hi) ^ flip),
+            __uint_as_float(__float_as_uint(v.lo) ^ flip)};
+}
+
 __device__ __forceinline__ f2sum f2_mul(f2sum a, f2sum b)
 {
     const float p = __fmul_rn(a.hi, b.hi);
@@ -156,8 +174,8 @@ __device__ __forceinline__ AxisQ split_q28(float p, float uh, float ul, int dims
     return {fi, (uint32_t)q & (kFracOne - 1u), u, xlu};
 }
 
-// The CIC weights of one particle in 2^-s mass units, shared by both deposit
-// engines so that they produce identical integer cell sums.  Factors per axis:
+// The CIC weights of one particle in 2^-s mass units, shared by every deposit
+// path so that they produce identical integer cell sums.  Factors per axis:
 // 2^28 - q (lower cell) and q (upper), so f / 2^28 is the CIC factor; the
 // particle's mass is mant * 2^(e - 150) (mant with its implicit bit) and
 // dsh = emax - e for the pass's largest exponent emax, with s = 154 - emax.

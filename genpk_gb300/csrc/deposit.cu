@@ -395,9 +395,7 @@ __global__ void __launch_bounds__(kSortThreads)
                 f2sum u = corner_factor_q(a[0], a[1], a[2]);
                 const float h = __fmul_rn(u.hi, mm);
                 u = f2sum{h, fmaf(u.hi, mm, -h) + u.lo * mm};
-                if ((a[0].cell + a[1].cell + a[2].cell) & 1)
-                    u = f2sum{-u.hi, -u.lo};
-                alt = f2_add2(alt, u);
+                f2_accumulate(alt, f2_signed(u, a[0].cell ^ a[1].cell ^ a[2].cell));
             }
         }
     });

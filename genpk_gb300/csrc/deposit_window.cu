@@ -37,6 +37,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 namespace genpk {
@@ -457,9 +458,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                     const float h = __fmul_rn(v.hi, mm);
                     v = f2sum{h, fmaf(v.hi, mm, -h) + v.lo * mm};
                 }
-                if ((ax.cell + ay.cell + az.cell) & 1)
-                    v = f2sum{-v.hi, -v.lo};
-                alt = f2_add2(alt, v);
+                f2_accumulate(alt, f2_signed(v, ax.cell ^ ay.cell ^ az.cell));
             }
             // Weights (common.cuh): factors 2^28 - q (lower cell) and q (upper).
             const uint32_t rx = kFracOne - ax.q, ry = kFracOne - ay.q, rz = kFracOne - az.q;
@@ -647,9 +646,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
                     const float h = __fmul_rn(v.hi, mm);
                     v = f2sum{h, fmaf(v.hi, mm, -h) + v.lo * mm};
                 }
-                if ((ax.cell + ay.cell + az.cell) & 1)
-                    v = f2sum{-v.hi, -v.lo};
-                alt = f2_add2(alt, v);
+                f2_accumulate(alt, f2_signed(v, ax.cell ^ ay.cell ^ az.cell));
             }
             const uint32_t rx = kFracOne - ax.q, ry = kFracOne - ay.q, rz = kFracOne - az.q;
             const uint32_t p00 = pair_w(rx, ry), p10 = pair_w(ax.q, ry), p01 = pair_w(rx, ay.q),
@@ -1021,8 +1018,14 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         const int smem = stream_mode ? p.win_off : p.win_off + 4 * p.cap;
         auto kern = a.masses ? (p.corner ? k_window_deposit<true, true> : k_window_deposit<true, false>)
                              : (p.corner ? k_window_deposit<false, true> : k_window_deposit<false, false>);
-        // 32-bit element indices: every index and both sentinels fit
-        if (stream_mode && g.grid.nfloat < ((int64_t)1 << 32) - 2)
+        // 32-bit element indices where every index and both sentinels fit.  The
+        // environment variable GENPK_WIDE_INDEX=1 forces the 64-bit variant on any grid
+        // (a test hook: that variant otherwise runs only from N = 1626 up).
+        static const bool force_wide = [] {
+            const char *e = std::getenv("GENPK_WIDE_INDEX");
+            return e && e[0] == '1';
+        }();
+        if (stream_mode && !force_wide && g.grid.nfloat < ((int64_t)1 << 32) - 2)
             kern = a.masses ? (p.corner ? k_stream_deposit<true, true, false>
                                         : k_stream_deposit<true, false, false>)
                             : (p.corner ? k_stream_deposit<false, true, false>

@@ -348,6 +348,21 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     }
     if (engine == GENPK_ENGINE_AUTO)  // too few particles to judge the order
         engine = GENPK_ENGINE_SORTED;
+    if ((engine == GENPK_ENGINE_WINDOW || engine == GENPK_ENGINE_STREAM) && !s.win_acc) {
+        // The window engine's accumulator (8 bytes per grid element) is allocated on first
+        // use; where it does not fit (the largest grids) an automatic pass takes the sorted
+        // engine, which needs no grid-sized scratch.
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (cudaMalloc(&s.win_acc, sizeof(unsigned long long) * (size_t)g.grid.nfloat) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            s.win_acc = nullptr;
+            if (ctx->engine != GENPK_ENGINE_AUTO)
+                return fail(ctx, GENPK_ERR_NOMEM,
+                            "window engine: the 64-bit accumulator does not fit in device memory");
+            engine = GENPK_ENGINE_SORTED;
+        }
+    }
     const bool chunked = engine == GENPK_ENGINE_WINDOW || engine == GENPK_ENGINE_STREAM;
     if (engine == GENPK_ENGINE_STREAM)
         chunk = kStreamChunk;
@@ -372,10 +387,6 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         size_t mp = (size_t)s.mass_part_cap;
         GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)mass_ctas));
         s.mass_part_cap = (int)mp;
-        if (!s.win_acc) {
-            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-            GENPK_CUDA(cudaMalloc(&s.win_acc, sizeof(unsigned long long) * (size_t)g.grid.nfloat));
-        }
         GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
                                        mass_ctas, s.win_acc,
                                        ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches,

@@ -411,6 +411,43 @@ def test_window_and_sorted_engines_agree_bit_for_bit(gp, var):
     assert np.array_equal(grids[0], grids[2])
 
 
+_WIDE_CHECK = """
+import sys, numpy as np, torch
+sys.path.insert(0, {root!r})
+import genpk_gb300 as gp
+from genpk_gb300 import synth
+box = 1000.0
+pos = torch.from_numpy(synth.zeldovich(64, box, seed=21)).cuda()
+masses = torch.linspace(-0.5, 1.5, len(pos)).cuda()
+grids = []
+with gp.Context(64, 8) as ctx:
+    for eng, m in ((gp.api.ENGINE_SORTED, None), (gp.api.ENGINE_STREAM, None),
+                   (gp.api.ENGINE_SORTED, masses), (gp.api.ENGINE_STREAM, masses)):
+        ctx.set_engine(eng)
+        ctx.zero(0)
+        ctx.deposit(0, box, pos, m, 1.0)
+        ctx.sync()
+        grids.append(ctx.read_field(0))
+assert np.array_equal(grids[0], grids[1]) and np.array_equal(grids[2], grids[3])
+print("wide ok")
+"""
+
+
+def test_stream_mode_64bit_indices(gp):
+    """The stream kernel's 64-bit element-index variant (chosen for grids of 2^32 or more
+    elements, N >= 1626) forced on a 64^3 grid through the GENPK_WIDE_INDEX=1 hook, in a
+    child process (the hook is read once): the same grids as the sorted engine, uniform and
+    signed variable masses."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _WIDE_CHECK.format(root=root)],
+                       env={**os.environ, "GENPK_WIDE_INDEX": "1"}, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "wide ok" in r.stdout, r.stdout + r.stderr
+
+
 @pytest.mark.parametrize("engine", ["sorted", "window", "stream"])
 def test_faint_high_k_bins_of_a_smooth_lattice(gp, engine):
     """128^3 Zel'dovich lattice (the GPU generator, L = 25000, 64 bins): the
