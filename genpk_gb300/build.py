@@ -20,6 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libgenpk_gb300.so")
 COMPAT_LIB = os.path.join(LIBDIR, "libgenpk_compat.so")
+CLI = os.path.join(LIBDIR, "gen-pk-gb300")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -29,6 +30,8 @@ CU_SOURCES = ["deposit.cu", "deposit_window.cu", "spectrum.cu", "xfft.cu", "adjo
               "noalloc.cu"]
 CXX_SOURCES = {"genpk.cpp": ["-O2"], "tables.cpp": ["-O2", "-ffast-math"]}
 COMPAT_SOURCE = "compat.cpp"
+# The gen-pk command line (format-II reader + driver) over the C ABI.
+CLI_SOURCES = ["gadget2.cpp", "gen_pk_gb300.cpp"]
 
 
 def _run(cmd):
@@ -75,6 +78,16 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     if force or _stale(cobj, [csrc] + headers):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", f"-I{CUDA_HOME}/include",
                      "-c", csrc, "-o", cobj])
+    cli_dir = os.path.join(PKG, "cli")
+    cli_objs = []
+    for src in CLI_SOURCES:
+        s = os.path.join(cli_dir, src)
+        o = os.path.join(BUILD, "cli_" + src + ".o")
+        cli_objs.append(o)
+        if force or _stale(o, [s, os.path.join(cli_dir, "gadget2.h"),
+                               os.path.join(ROOT, "include", "genpk_gb300.h")]):
+            jobs.append(["g++", "-O2", "-std=c++17", "-Wall", f"-I{ROOT}/include", "-c", s,
+                         "-o", o])
     out = []
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for text in ex.map(_run, jobs):
@@ -84,6 +97,9 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
                          f"-L{CUDA_HOME}/lib64", "-Xlinker", f"-rpath,{CUDA_HOME}/lib64"]))
     if jobs or not os.path.exists(COMPAT_LIB):
         out.append(_run(["g++", "-shared", "-o", COMPAT_LIB, cobj, f"-L{LIBDIR}", "-lgenpk_gb300",
+                         "-Wl,-rpath,$ORIGIN"]))
+    if jobs or not os.path.exists(CLI):
+        out.append(_run(["g++", "-o", CLI, *cli_objs, f"-L{LIBDIR}", "-lgenpk_gb300",
                          "-Wl,-rpath,$ORIGIN"]))
     text = "".join(out)
     if verbose and text:

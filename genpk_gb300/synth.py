@@ -136,3 +136,60 @@ def lognormal(n_mean: int, box: float, ngrid: int, sigma: float = 1.5, seed: int
     if mass_mu is not None:
         masses = rng.lognormal(mass_mu, mass_sigma, cells.size).astype(np.float32)
     return pos, masses
+
+
+def write_gadget2(base: str, pos_by_type: dict, masses_by_type: dict, box: float,
+                  nfiles: int = 1, time: float = 1.0, redshift: float = 0.0,
+                  hubble: float = 0.7, omega0: float = 0.3, extra_blocks: bool = True):
+    """Write a Gadget-2 format-II snapshot: `base` (nfiles = 1) or base.0 ...
+    base.(nfiles-1), each type's particles split into contiguous parts.
+
+    pos_by_type: {type: float32 [n, 3]}.  masses_by_type: {type: float (the
+    header mass table) or float32 [n] (the MASS block; header mass 0)}.
+    Each block is a label record (int32 8, name, int32 size + 8, int32 8) and
+    a data record (int32 size, data, int32 size); HEAD is the 256-byte
+    io_header.  extra_blocks adds VEL and ID blocks, which readers skip."""
+    import struct
+
+    ntypes = 6
+    counts = [len(pos_by_type.get(t, ())) for t in range(ntypes)]
+    table = [0.0 if not np.isscalar(masses_by_type.get(t, 0.0)) else float(masses_by_type.get(t, 0.0))
+             for t in range(ntypes)]
+    paths = [base] if nfiles == 1 else [f"{base}.{i}" for i in range(nfiles)]
+
+    def split(n, i):
+        edges = [n * k // nfiles for k in range(nfiles + 1)]
+        return edges[i], edges[i + 1]
+
+    def block(f, name, data: bytes):
+        f.write(struct.pack("<i4sii", 8, name.encode(), len(data) + 8, 8))
+        f.write(struct.pack("<i", len(data)))
+        f.write(data)
+        f.write(struct.pack("<i", len(data)))
+
+    for i, path in enumerate(paths):
+        npart = []
+        pos_parts, mass_parts, vel_parts = [], [], []
+        for t in range(ntypes):
+            lo, hi = split(counts[t], i)
+            npart.append(hi - lo)
+            if hi > lo:
+                p = np.ascontiguousarray(pos_by_type[t][lo:hi], dtype=np.float32)
+                pos_parts.append(p)
+                vel_parts.append(np.zeros_like(p))
+                if table[t] == 0.0:
+                    mass_parts.append(np.asarray(masses_by_type[t][lo:hi], dtype=np.float32))
+        head = struct.pack("<6I6dddii6Iiiddddii6I", *npart, *table, time, redshift, 0, 0,
+                           *[c & 0xFFFFFFFF for c in counts], 0, nfiles, box, omega0,
+                           1.0 - omega0, hubble, 0, 0, *[c >> 32 for c in counts])
+        head = head + b"\0" * (256 - len(head))
+        with open(path, "wb") as f:
+            block(f, "HEAD", head)
+            block(f, "POS ", b"".join(p.tobytes() for p in pos_parts))
+            if extra_blocks:
+                block(f, "VEL ", b"".join(v.tobytes() for v in vel_parts))
+                ids = np.arange(sum(npart), dtype=np.uint32)
+                block(f, "ID  ", ids.tobytes())
+            if mass_parts:
+                block(f, "MASS", b"".join(m.tobytes() for m in mass_parts))
+    return paths
