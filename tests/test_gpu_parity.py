@@ -369,6 +369,26 @@ def test_auto_engine_choice(gp):
         assert ctx.last_engine == gp.api.ENGINE_SORTED
 
 
+def test_engine_choice_is_kept_for_the_same_arrays(gp):
+    """Device arrays deposited again take the previous automatic choice (no
+    probe, no host round trip); other arrays are probed afresh."""
+    import torch
+    from genpk_gb300 import synth
+    box = 1000.0
+    lattice = torch.from_numpy(synth.zeldovich(128, box, seed=5)).cuda()
+    rand = torch.from_numpy(synth.uniform(len(lattice), box, seed=6)).cuda()
+    with gp.Context(128, 16, timing=True) as ctx:
+        got = []
+        for src in (lattice, rand, rand, lattice):
+            ctx.timing_reset()
+            ctx.zero(0)
+            ctx.deposit(0, box, src, None, 1.0)
+            ctx.sync()
+            got.append((ctx.last_engine, "probe" in ctx.stage_times()))
+    S, W = gp.api.ENGINE_STREAM, gp.api.ENGINE_SORTED
+    assert got == [(S, True), (W, True), (W, False), (S, True)]
+
+
 def test_sparse_lattice_picks_a_shorter_window_chunk(gp):
     """128^3 lattice particles on a 256^3 grid (two cells per lattice
     spacing): a 4096-particle chunk's window does not fit, a 1024-particle
