@@ -88,16 +88,19 @@ struct genpk_ctx {
     int engine = GENPK_ENGINE_AUTO;   // requested deposit engine
     int last_engine = GENPK_ENGINE_AUTO;  // engine the latest pass used
     long long *d_probe = nullptr;     // window-engine probe results
-    // The last automatic engine choice and the pass it was made for.  Every
-    // engine yields the same grid, so reusing a choice for the same particle
-    // arrays (a loop over one buffer, positions updated in place) can only
-    // change the speed; it saves the probes and their host round trip.
-    struct {
+    // Recent automatic engine choices and the arrays they were made for (a few:
+    // one per species of a multi-species loop).  Every engine yields the same
+    // grid, so reusing a choice for the same particle arrays (a loop over the
+    // same buffers, positions updated in place) can only change the speed; it
+    // saves the probes and their host round trip.
+    struct Choice {
         const float *pos = nullptr, *masses = nullptr;
         int64_t n = -1;
         double boxsize = 0.0;
         int engine = 0, chunk = 0;
-    } choice;
+    };
+    Choice choices[8];
+    int choice_next = 0;
     size_t probe_cap = 0;
 
     // staging of host particles
@@ -309,12 +312,15 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     int chunk = kWindowChunks[0];
     timing_touch(ctx);  // the probes belong to the pass
     // (never for the staging buffer: it holds a different caller array each time)
-    const bool reuse = engine == GENPK_ENGINE_AUTO && pos != ctx->stage_pos &&
-                       ctx->choice.pos == pos && ctx->choice.masses == masses &&
-                       ctx->choice.n == n && ctx->choice.boxsize == boxsize;
+    const genpk_ctx::Choice *hit = nullptr;
+    if (engine == GENPK_ENGINE_AUTO && pos != ctx->stage_pos)
+        for (const auto &c : ctx->choices)
+            if (c.pos == pos && c.masses == masses && c.n == n && c.boxsize == boxsize)
+                hit = &c;
+    const bool reuse = hit != nullptr;
     if (reuse) {
-        engine = ctx->choice.engine;
-        chunk = ctx->choice.chunk;
+        engine = hit->engine;
+        chunk = hit->chunk;
     } else if (engine == GENPK_ENGINE_WINDOW ||
                (engine == GENPK_ENGINE_AUTO && n >= kWindowMinParticles)) {
         // Spatially coherent order (most snapshot layouts) -> window engine
@@ -368,12 +374,16 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     if (engine == GENPK_ENGINE_AUTO)  // too few particles to judge the order
         engine = GENPK_ENGINE_SORTED;
     if (ctx->engine == GENPK_ENGINE_AUTO && !reuse) {
-        ctx->choice.pos = pos;
-        ctx->choice.masses = masses;
-        ctx->choice.n = n;
-        ctx->choice.boxsize = boxsize;
-        ctx->choice.engine = engine;
-        ctx->choice.chunk = chunk;
+        if (pos != ctx->stage_pos) {
+            genpk_ctx::Choice &c = ctx->choices[ctx->choice_next];
+            ctx->choice_next = (ctx->choice_next + 1) % 8;
+            c.pos = pos;
+            c.masses = masses;
+            c.n = n;
+            c.boxsize = boxsize;
+            c.engine = engine;
+            c.chunk = chunk;
+        }
         stage_event(ctx, "probe");
     }
     if ((engine == GENPK_ENGINE_WINDOW || engine == GENPK_ENGINE_STREAM) && !s.win_acc) {
@@ -718,7 +728,8 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         const int ctas = bin_ctas(ctx->gg, nrb, l.npairs, l.nfields, ctx->num_sms, &warps, &smem);
         if (ctas <= 0)
             return fail(ctx, GENPK_ERR_UNSUPPORTED, "nrbins too large for the binning kernel");
-        GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * l.npairs * nrb));
+        GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap,
+                       (size_t)ctas * bin_pair_slots(l.nfields, l.npairs) * nrb));
         GENPK_CUDA(bin_spectra(ctx->gg, ctx->tables, ctx->bdev, l, ctx->d_partial,
                                ctx->d_power + (size_t)q0 * nrb, ctas, warps, smem, ctx->stream,
                                &ctx->launches));

@@ -211,6 +211,9 @@ struct BinLaunch {
     int npairs;
 };
 
+// Pair sums per CTA partial for a request (the instantiation's pair count:
+// every pair of the fields, or the single pair of one or two fields).
+int bin_pair_slots(int nfields, int npairs);
 int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms, int *warps,
              size_t *smem);
 

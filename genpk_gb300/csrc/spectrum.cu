@@ -33,8 +33,7 @@ struct BinParams {
     const float2 *f[kMaxBinFields];
     const double *corner[kMaxBinFields];  // exact (N/2,N/2,N/2) value per field, or null
     int64_t corner_row;                   // row index i*N+j of that mode, -1 if none
-    int pa[kMaxBinPairs], pb[kMaxBinPairs];
-    int np;          // pairs actually reported (<= NP of the instantiation)
+    int np;          // pair sums per CTA partial: the instantiation's pair count
     int dims, hc, half;
     int nrbins;
     float bpu_half;  // 0.5 * binsperunit as float, for the first-guess bin
@@ -44,16 +43,33 @@ struct BinParams {
 
 constexpr int kPromoteRows = 16;  // rows summed in FP32 before promotion to FP64
 
-// fv[idx] for a runtime idx without spilling fv to local memory.
-template <int NF>
-__device__ __forceinline__ float2 pick(const float2 (&fv)[NF], int idx)
+// Pairs an instantiation sums, with compile-time field indices: the single
+// cross pair (0, 1) (CROSS1), or every pair a <= b of NF fields in the order
+// (0,0), (0,1), ..., (0,NF-1), (1,1), ... (Re F_a F_b* is symmetric).
+template <int NF, bool CROSS1>
+struct PairSet {
+    static constexpr int NP = CROSS1 ? 1 : NF * (NF + 1) / 2;
+};
+
+__host__ __device__ constexpr int pair_slot(int nf, int a, int b)
 {
-    float2 r = fv[0];
+    return a * nf - a * (a - 1) / 2 + (b - a);
+}
+
+template <int NF, bool CROSS1>
+__device__ __forceinline__ void add_pairs(const float2 (&fv)[NF], float w,
+                                          float (&acc)[PairSet<NF, CROSS1>::NP])
+{
+    if (CROSS1) {
+        acc[0] = fmaf(w, fmaf(fv[0].x, fv[NF - 1].x, fv[0].y * fv[NF - 1].y), acc[0]);
+    } else {
 #pragma unroll
-    for (int f = 1; f < NF; f++)
-        if (idx == f)
-            r = fv[f];
-    return r;
+        for (int a = 0; a < NF; a++)
+#pragma unroll
+            for (int b = a; b < NF; b++)
+                acc[pair_slot(NF, a, b)] =
+                    fmaf(w, fmaf(fv[a].x, fv[b].x, fv[a].y * fv[b].y), acc[pair_slot(NF, a, b)]);
+    }
 }
 
 __device__ __forceinline__ int kval_dev(int i, int dims)
@@ -163,11 +179,12 @@ __device__ __forceinline__ void stage_piece(const BinParams &p, int64_t r, int p
 // are combined by a segmented warp scan over their (non-decreasing) bins and
 // each bin's last lane adds the total without atomics.  Every kPromoteRows
 // rows the touched FP32 bins are promoted into the warp's FP64 histogram.
-template <int NF, int NP>
+template <int NF, bool CROSS1>
 __global__ void __launch_bounds__(256)
     k_bin(BinParams p, const uint32_t *__restrict__ thr_g, const float *__restrict__ iw_g,
           double *__restrict__ partial)
 {
+    constexpr int NP = PairSet<NF, CROSS1>::NP;
     extern __shared__ __align__(16) unsigned char smem[];
     const int nrb = p.nrbins;
     const int rp = p.rp, piece = 32 * rp;
@@ -247,11 +264,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                     for (int f = 0; f < NF; f++)
                         fv[f] = bl[f * piece + t];
-#pragma unroll
-                    for (int s = 0; s < NP; s++) {
-                        const float2 a = pick<NF>(fv, p.pa[s]), c = pick<NF>(fv, p.pb[s]);
-                        acc[s] = fmaf(w, fmaf(a.x, c.x, a.y * c.y), acc[s]);
-                    }
+                    add_pairs<NF, CROSS1>(fv, w, acc);
                     kk2 += (uint32_t)(2 * kz + 1);
                 }
                 bmax = max(bmax, cb);
@@ -309,6 +322,8 @@ __global__ void __launch_bounds__(256)
 
 struct NormParams {
     double ma[kMaxBinPairs], mb[kMaxBinPairs];
+    int src[kMaxBinPairs];  // the partials' pair slot of each reported pair
+    int npc;                // pair slots per CTA partial
 };
 
 // One block per (pair, bin): strided sums over the CTA partials, then a
@@ -316,15 +331,16 @@ struct NormParams {
 constexpr int kFinalizeThreads = 256;
 
 __global__ void __launch_bounds__(kFinalizeThreads)
-    k_bin_finalize(const double *__restrict__ partial, int ctas, int np, int nrbins,
+    k_bin_finalize(const double *__restrict__ partial, int ctas, int nrbins,
                    const double *__restrict__ count, NormParams mn, double *__restrict__ power)
 {
     __shared__ double sh[kFinalizeThreads];
     const int k = blockIdx.x;
     const int s = k / nrbins, b = k - s * nrbins;
+    const size_t src = (size_t)mn.src[s] * nrbins + b;
     double part = 0.0;
     for (int c = threadIdx.x; c < ctas; c += blockDim.x)
-        part += partial[(size_t)c * np * nrbins + k];
+        part += partial[(size_t)c * mn.npc * nrbins + src];
     sh[threadIdx.x] = part;
     __syncthreads();
     for (int w = kFinalizeThreads / 2; w > 0; w >>= 1) {
@@ -355,22 +371,31 @@ size_t bin_smem(int nrbins, int hc, int np, int nf, int warps)
     return L.warps + L.per_warp * warps;
 }
 
-// Instantiated (fields, pairs) shapes; a request is rounded up to the first
-// shape that holds it and padded with dummy pairs whose sums are dropped.
+// Instantiated shapes: one field (its auto pair); two fields and one pair
+// (the cross pair alone); else every pair of 2, 3 or 4 fields.  A request's
+// pairs are found among the shape's by pair_slot.
 struct Shape {
     int nf, np;
+    bool cross1;
 };
-constexpr Shape kShapes[] = {{1, 1}, {2, 1}, {2, 3}, {3, 6}, {4, 10}};
 
 Shape pick_shape(int nf, int np)
 {
-    for (const Shape &s : kShapes)
-        if (s.nf >= nf && s.np >= np)
-            return s;
-    return {0, 0};
+    if (nf == 1)
+        return {1, 1, false};
+    if (nf == 2 && np == 1)
+        return {2, 1, true};
+    if (nf >= 2 && nf <= kMaxBinFields)
+        return {nf, nf * (nf + 1) / 2, false};
+    return {0, 0, false};
 }
 
 }  // namespace
+
+int bin_pair_slots(int nfields, int npairs)
+{
+    return pick_shape(nfields, npairs).np;
+}
 
 int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms, int *warps,
              size_t *smem)
@@ -403,12 +428,7 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
         p.corner[f] = l.corner[f < l.nfields ? f : 0];
     }
     p.corner_row = (g.dims % 2 == 0) ? (int64_t)g.half * g.dims + g.half : -1;
-    for (int q = 0; q < kMaxBinPairs; q++) {
-        const int src = q < l.npairs ? q : 0;
-        p.pa[q] = l.pairs[src].a;
-        p.pb[q] = l.pairs[src].b;
-    }
-    p.np = l.npairs;
+    p.np = s.np;
     p.dims = g.dims;
     p.hc = g.hc;
     p.half = g.half;
@@ -417,36 +437,40 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
     p.rp = bin_rp(g.hc);
     p.warps = warps;
     cudaError_t err;
-#define GENPK_BIN_LAUNCH(NF, NP)                                                              \
+#define GENPK_BIN_LAUNCH(NF, CROSS1)                                                          \
     do {                                                                                      \
-        auto kern = k_bin<NF, NP>;                                                            \
+        auto kern = k_bin<NF, CROSS1>;                                                        \
         if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                         (int)smem)) != cudaSuccess)                           \
             return err;                                                                       \
         kern<<<ctas, 32 * warps, smem, stream>>>(p, d.thr, d.iw, partial);                    \
     } while (0)
     if (s.nf == 1)
-        GENPK_BIN_LAUNCH(1, 1);
-    else if (s.nf == 2 && s.np == 1)
-        GENPK_BIN_LAUNCH(2, 1);
+        GENPK_BIN_LAUNCH(1, false);
+    else if (s.nf == 2 && s.cross1)
+        GENPK_BIN_LAUNCH(2, true);
     else if (s.nf == 2)
-        GENPK_BIN_LAUNCH(2, 3);
+        GENPK_BIN_LAUNCH(2, false);
     else if (s.nf == 3)
-        GENPK_BIN_LAUNCH(3, 6);
+        GENPK_BIN_LAUNCH(3, false);
     else
-        GENPK_BIN_LAUNCH(4, 10);
+        GENPK_BIN_LAUNCH(4, false);
 #undef GENPK_BIN_LAUNCH
     (*launches)++;
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
     NormParams mn;
+    mn.npc = s.np;
     for (int q = 0; q < kMaxBinPairs; q++) {
         mn.ma[q] = q < l.npairs ? l.pairs[q].mass_a : 1.0;
         mn.mb[q] = q < l.npairs ? l.pairs[q].mass_b : 1.0;
+        const int a = q < l.npairs ? std::min(l.pairs[q].a, l.pairs[q].b) : 0;
+        const int b = q < l.npairs ? std::max(l.pairs[q].a, l.pairs[q].b) : 0;
+        mn.src[q] = s.cross1 ? 0 : pair_slot(s.nf, a, b);
     }
     const int k = l.npairs * t.nrbins;
-    k_bin_finalize<<<k, kFinalizeThreads, 0, stream>>>(partial, ctas, l.npairs, t.nrbins, d.count,
-                                                        mn, out_power);
+    k_bin_finalize<<<k, kFinalizeThreads, 0, stream>>>(partial, ctas, t.nrbins, d.count, mn,
+                                                        out_power);
     (*launches)++;
     return cudaGetLastError();
 }
@@ -456,11 +480,13 @@ cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const do
                            int64_t *launches)
 {
     NormParams mn;
+    mn.npc = 1;
     for (int q = 0; q < kMaxBinPairs; q++) {
         mn.ma[q] = q == 0 ? ma : 1.0;
         mn.mb[q] = q == 0 ? mb : 1.0;
+        mn.src[q] = 0;
     }
-    k_bin_finalize<<<nrbins, kFinalizeThreads, 0, stream>>>(partial, ctas, 1, nrbins, count, mn,
+    k_bin_finalize<<<nrbins, kFinalizeThreads, 0, stream>>>(partial, ctas, nrbins, count, mn,
                                                             out);
     (*launches)++;
     return cudaGetLastError();

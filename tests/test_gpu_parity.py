@@ -370,8 +370,9 @@ def test_auto_engine_choice(gp):
 
 
 def test_engine_choice_is_kept_for_the_same_arrays(gp):
-    """Device arrays deposited again take the previous automatic choice (no
-    probe, no host round trip); other arrays are probed afresh."""
+    """Device arrays deposited again take their previous automatic choice (no
+    probe, no host round trip; a few arrays are remembered, one per species of
+    a multi-species loop); new arrays are probed."""
     import torch
     from genpk_gb300 import synth
     box = 1000.0
@@ -386,7 +387,7 @@ def test_engine_choice_is_kept_for_the_same_arrays(gp):
             ctx.sync()
             got.append((ctx.last_engine, "probe" in ctx.stage_times()))
     S, W = gp.api.ENGINE_STREAM, gp.api.ENGINE_SORTED
-    assert got == [(S, True), (W, True), (W, False), (S, True)]
+    assert got == [(S, True), (W, True), (W, False), (S, False)]
 
 
 def test_sparse_lattice_picks_a_shorter_window_chunk(gp):
