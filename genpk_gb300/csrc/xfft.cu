@@ -24,9 +24,9 @@
 //             per-warp FP32 histogram;
 //             the lanes' open sums are combined by a segmented warp scan (rows
 //             of a warp lie in one half of the axis, so their bins are
-//             monotone); per tile the warps' histograms are summed in a fixed
-//             order into the CTA's FP64 histogram; k_bin_finalize reduces the
-//             CTA partials.
+//             monotone); every 8 tiles the warps' histograms are summed in a
+//             fixed order into the CTA's FP64 histogram; k_bin_finalize reduces
+//             the CTA partials.
 #include "common.cuh"
 #include "internal.h"
 
@@ -69,7 +69,8 @@ struct ColInfo {
     float w;     // mode weight: 1 on the kz = 0 and kz = N/2 planes, else 2
     int special; // 1: (j, kz) = (0, 0) (row 0 is the skipped k = 0 mode);
                  // 2: (j, kz) = (N/2, N/2) (row N/2 is the exact corner mode)
-    int pad[3];
+    int run;     // 1: kz = 0, a new run of consecutive kz begins (new ky)
+    int pad[2];
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -372,8 +373,10 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
     q += sizeof(float2) * N;
     float *iw_s = reinterpret_cast<float *>(q);
     q += sizeof(float) * N;
-    ColInfo *cols = reinterpret_cast<ColInfo *>(q);
-    q += sizeof(ColInfo) * TZ;
+    // [2][TZ]: by tile parity, so that the next tile's column table is written
+    // while warps may still walk this tile's (no barrier ends a tile)
+    ColInfo *cols2 = reinterpret_cast<ColInfo *>(q);
+    q += sizeof(ColInfo) * 2 * TZ;
     float *vals = reinterpret_cast<float *>(q);                  // [TZ][N + 1]
     q += BIN ? sizeof(float) * TZ * (N + 1) : 0;
     q = xs + ((q - xs + 15) & ~(size_t)15);
@@ -440,12 +443,14 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
                 ci.iwz = p.iw[kz];
                 ci.w = (kz == 0 || kz == N / 2) ? 1.f : 2.f;
                 ci.special = (j == 0 && kz == 0) ? 1 : (j == N / 2 && kz == N / 2 && p.corner) ? 2 : 0;
+                ci.run = kz == 0 ? 1 : 0;
             } else {
                 ci.r2 = -1;
+                ci.run = 0;
                 ci.iwj = ci.iwz = ci.w = 0.f;
                 ci.special = 0;
             }
-            cols[tid] = ci;
+            cols2[(k & 1) * TZ + tid] = ci;
         }
         if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
             timeouts++;
@@ -454,6 +459,7 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         float2 v[8];
         fft_to_last<N>(tile, tw_s, c, g, v);
         __syncthreads();
+        const ColInfo *cols = cols2 + (k & 1) * TZ;
         const ColInfo ci = BIN ? cols[c] : ColInfo{};
         last_write<N, BIN>(tile, vals, ci, c, g, v, iw_s);
         if (BIN && ci.special) {
@@ -477,6 +483,11 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         if (BIN) {
             // Walk columns of a row with a running bin: 8 modes per thread
             // (8 columns of one row; for N = 1024, 4 columns of two rows).
+            // The column structure is the same for every lane of a warp (lanes
+            // differ in the row): the bin is looked up where a run of
+            // consecutive kz starts (the first column, or kz = 0 of a new ky),
+            // so those lookups are warp-uniform; along a run |k|^2 grows and
+            // the bin only steps up past the next threshold.
             constexpr int ROWS_PT = N > kXThreads ? N / kXThreads : 1;
             constexpr int COLS_PT = (kXTileBytes / 8 / kXThreads) / ROWS_PT;
 #pragma unroll
@@ -486,24 +497,29 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
                 const int kx = kval_x(row, N);
                 const uint32_t kx2 = (uint32_t)(kx * kx);
                 int cb = p.nrbins;  // sentinel: no mode yet
-                uint32_t lo = 0, hi = 0;
+                uint32_t nx = 0;    // the open bin's upper threshold
                 float acc = 0.f;
 #pragma unroll
                 for (int cc = 0; cc < COLS_PT; cc++) {
                     const int r2 = cols[c0 + cc].r2;
                     if (r2 < 0)
-                        continue;
+                        break;  // padding columns: only after the field's last column
                     const uint32_t kk2 = kx2 + (uint32_t)r2;
-                    const float val = vals[(c0 + cc) * (N + 1) + row];
-                    if (kk2 >= hi || kk2 < lo) {  // also true for the first mode
+                    if (cc == 0 || cols[c0 + cc].run) {
                         if (cb < p.nrbins)
                             atomicAdd(&whist[wid * p.nrbins + cb], acc);
                         cb = bin_of(kk2, thr, p.nrbins, p.bpu_half);
-                        lo = thr[cb];
-                        hi = thr[cb + 1];
+                        nx = thr[cb + 1];
                         acc = 0.f;
+                    } else {
+                        while (kk2 >= nx) {  // thr[nrbins] = 2^32 - 1 ends it
+                            atomicAdd(&whist[wid * p.nrbins + cb], acc);
+                            acc = 0.f;
+                            cb++;
+                            nx = thr[cb + 1];
+                        }
                     }
-                    acc += val;
+                    acc += vals[(c0 + cc) * (N + 1) + row];
                 }
                 // Segmented scan over the lanes' open bins (the warp's rows lie
                 // in one half of the axis, so the bins are monotone across it).
@@ -518,14 +534,18 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
                 if (cb < p.nrbins && (lane == 31 || kd != cb))
                     atomicAdd(&whist[wid * p.nrbins + cb], acc);
             }
-            __syncthreads();
-            for (int bb = tid; bb < p.nrbins; bb += kXThreads) {
-                float s = 0.f;
-                for (int w = 0; w < kXThreads / 32; w++) {
-                    s += whist[w * p.nrbins + bb];
-                    whist[w * p.nrbins + bb] = 0.f;
+            // The warps' FP32 histograms go into the CTA's FP64 one every 8
+            // tiles and after the CTA's last tile (the condition is uniform).
+            if ((k & 7) == 7 || t + (int)gridDim.x >= p.ntiles) {
+                __syncthreads();
+                for (int bb = tid; bb < p.nrbins; bb += kXThreads) {
+                    float s = 0.f;
+                    for (int w = 0; w < kXThreads / 32; w++) {
+                        s += whist[w * p.nrbins + bb];
+                        whist[w * p.nrbins + bb] = 0.f;
+                    }
+                    chist[bb] += (double)s;
                 }
-                chist[bb] += (double)s;
             }
         }
     }
@@ -572,7 +592,7 @@ size_t xfft_smem(int dims, int nrbins)
 {
     const int tz = xfft_tz(dims);
     size_t s = 2 * (size_t)kXTileBytes + sizeof(float2) * dims + sizeof(float) * dims +
-               sizeof(ColInfo) * tz;
+               sizeof(ColInfo) * 2 * tz;
     if (nrbins > 0) {
         s += sizeof(float) * tz * (dims + 1);
         s = (s + 15) & ~(size_t)15;
