@@ -338,7 +338,7 @@ __device__ __forceinline__ int bin_of(uint32_t kk2, const uint32_t *thr, int nrb
 // the per-mode values v into vals[c * (N + 1) + row].
 template <int N, bool BIN>
 __device__ __forceinline__ void last_write(float2 *tile, float *vals, const ColInfo &ci, int c,
-                                           int g, const float2 (&v)[8], const float *iw_s)
+                                           int g, const float2 (&v)[8], const float (&iwr)[8])
 {
     using P = FftPlan<N>;
     constexpr int TZ = kXTileBytes / 8 / N;
@@ -352,7 +352,7 @@ __device__ __forceinline__ void last_write(float2 *tile, float *vals, const ColI
             const float2 f = v[m * P::RL + r];
             tile[row * TZ + c] = f;
             if (BIN) {
-                const float p1 = (iw_s[row] * ci.iwj) * ci.iwz;
+                const float p1 = (iwr[m * P::RL + r] * ci.iwj) * ci.iwz;
                 const float p2 = p1 * p1;
                 vals[c * (N + 1) + row] = cw * (p2 * p2) * fmaf(f.x, f.x, f.y * f.y);
             }
@@ -410,6 +410,16 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
     }
     __syncthreads();
     const float corner_val = (BIN && p.corner) ? (float)*p.corner : 0.f;
+    // iw(kx) of the 8 rows this thread's last stage writes: the same in every tile
+    float iwr[8];
+    {
+        using P = FftPlan<N>;
+#pragma unroll
+        for (int m = 0; m < 8 / P::RL; m++)
+#pragma unroll
+            for (int r = 0; r < P::RL; r++)
+                iwr[m * P::RL + r] = BIN ? iw_s[stage_out_row<N, P::NSL, P::RL>(g, m, r)] : 0.f;
+    }
 
     auto issue = [&](int t, int buf) {
         const int b = t / p.tiles_per_field, f0 = (t - b * p.tiles_per_field) * TZ;
@@ -461,7 +471,7 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         __syncthreads();
         const ColInfo *cols = cols2 + (k & 1) * TZ;
         const ColInfo ci = BIN ? cols[c] : ColInfo{};
-        last_write<N, BIN>(tile, vals, ci, c, g, v, iw_s);
+        last_write<N, BIN>(tile, vals, ci, c, g, v, iwr);
         if (BIN && ci.special) {
             // the skipped k = 0 mode and the exact corner mode
             const int row = ci.special == 1 ? 0 : N / 2;
