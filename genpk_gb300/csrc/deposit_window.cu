@@ -27,12 +27,18 @@
 //             accumulator (global RED, no return) and cleared, so the window
 //             is zero again for the next chunk.
 //
+//   k_stream_deposit  the stream mode: the same chunk pipeline without the
+//     window, for lattice order at about one particle per cell (where windows
+//     merge few adds); each particle's weights go to the accumulator as L2
+//     reductions, merged between neighbouring lanes of one z cell column.
+//     Chosen by the merge rate k_stream_probe measures.
+//
 // Sums are exact: the window cells (32-bit, overflows moved on as 2^32 units)
 // and the pass accumulator (64-bit) are integers of 2^-s mass units (the
 // sorted engine's weights, common.cuh pair_w / z_mass / corner_w);
 // k_window_convert subtracts the fixed-point pass mean and rounds each cell
-// once to FP32.  The grid is therefore bit-identical to the
-// sorted engine's and independent of summation order.
+// once to FP32.  The grid is therefore bit-identical to the sorted engine's,
+// in either mode, and independent of summation order.
 #include "common.cuh"
 #include "internal.h"
 
