@@ -382,7 +382,7 @@ def main():
     if engine in ("window", "stream"):
         stage = "win_deposit" if engine == "window" else "stream_deposit"
         t_k = stages.get(stage, 0.0) * 1e-3
-        kname = "k_" + stage
+        kname = "k_window_deposit" if engine == "window" else "k_stream_deposit"
         ncu = NCU_TRAFFIC.get((kname, nside, n))
         traffic = ncu
     else:
