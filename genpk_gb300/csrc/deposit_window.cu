@@ -989,11 +989,21 @@ cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
     return cudaGetLastError();
 }
 
+cudaError_t window_convert(const GridGeom &g, const unsigned long long *acc, float *grid,
+                           bool clean, const DeviceStatus *dstat, int num_sms,
+                           cudaStream_t stream, int64_t *launches)
+{
+    k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, grid, g.dims, g.row, g.nfloat / 2,
+                                                      clean ? 1 : 0, dstat);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
                                 bool stream_mode, double *mass_part, int mass_ctas,
-                                unsigned long long *acc, int num_sms, DeviceStatus *dstat,
-                                cudaStream_t stream, int64_t *launches, StageHook hook,
-                                void *hook_user)
+                                unsigned long long *acc, bool defer_convert, int num_sms,
+                                DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
+                                StageHook hook, void *hook_user)
 {
     auto mark = [&](const char *name) {
         (*launches)++;
@@ -1049,11 +1059,14 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
         if ((err = cudaGetLastError()) != cudaSuccess)
             return err;
     }
-    k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, a.grid, g.grid.dims, g.grid.row,
-                                                      g.grid.nfloat / 2, a.clean ? 1 : 0, dstat);
-    mark("win_convert");
-    if ((err = cudaGetLastError()) != cudaSuccess)
-        return err;
+    if (!defer_convert) {
+        k_window_convert<<<num_sms * 8, 256, 0, stream>>>(acc, a.grid, g.grid.dims, g.grid.row,
+                                                          g.grid.nfloat / 2, a.clean ? 1 : 0,
+                                                          dstat);
+        mark("win_convert");
+        if ((err = cudaGetLastError()) != cudaSuccess)
+            return err;
+    }
     k_window_finish<<<1, 1, 0, stream>>>(dstat, a.field_corner);
     (*launches)++;
     return cudaGetLastError();

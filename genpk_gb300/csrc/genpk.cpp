@@ -88,6 +88,10 @@ struct genpk_ctx {
     int engine = GENPK_ENGINE_AUTO;   // requested deposit engine
     int last_engine = GENPK_ENGINE_AUTO;  // engine the latest pass used
     long long *d_probe = nullptr;     // window-engine probe results
+    // A field whose latest (clean) window-engine pass is still only in the
+    // 64-bit accumulator: the forward transform reads it from there (the
+    // conversion pass is skipped); anything else converts it first.
+    int acc_pending = -1;
     // Recent automatic engine choices and the arrays they were made for (a few:
     // one per species of a multi-species loop).  Every engine yields the same
     // grid, so reusing a choice for the same particle arrays (a loop over the
@@ -289,9 +293,13 @@ int ensure_stage(genpk_ctx *ctx, int64_t need);
 
 // One deposit pass from device particle arrays, or (host_mapped) from pinned
 // host arrays read in place by the window engine.
+int flush_acc(genpk_ctx *ctx);
+bool use_xfft(const genpk_ctx *ctx);
+
 int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const float *masses,
                 float mass, int64_t n, bool host_mapped = false)
 {
+    GENPK_TRY(flush_acc(ctx));  // this pass reuses the accumulator
     if (n > 0xffffffffLL - 1)
         return fail(ctx, GENPK_ERR_UNSUPPORTED, "more than 2^32-1 particles in one pass");
     const DepositGeom g = deposit_geom(ctx, boxsize);
@@ -425,10 +433,14 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         size_t mp = (size_t)s.mass_part_cap;
         GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)mass_ctas));
         s.mass_part_cap = (int)mp;
+        // A clean grid headed for the own z/y/x transform keeps the pass in the
+        // accumulator: the z pass converts it on the fly.
+        const bool defer = a.clean && use_xfft(ctx);
         GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
-                                       mass_ctas, s.win_acc,
-                                       ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches,
-                                       hook, ctx));
+                                       mass_ctas, s.win_acc, defer, ctx->num_sms, ctx->d_status,
+                                       ctx->stream, &ctx->launches, hook, ctx));
+        if (defer)
+            ctx->acc_pending = f;
     } else {
         const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
         if (deposit_shared_hist(g)) {
@@ -454,7 +466,30 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     return GENPK_OK;
 }
 
+// The pending accumulator (if any) into its FP32 grid.
+int flush_acc(genpk_ctx *ctx)
+{
+    if (ctx->acc_pending < 0)
+        return GENPK_OK;
+    const int f = ctx->acc_pending;
+    ctx->acc_pending = -1;
+    GENPK_CUDA(window_convert(ctx->gg, ctx->dscr.win_acc, grid_of(ctx, f), true, ctx->d_status,
+                              ctx->num_sms, ctx->stream, &ctx->launches));
+    stage_event(ctx, "win_convert");
+    return GENPK_OK;
+}
+
+// Staged host deposits of the pending pass, then the pending accumulator:
+// afterwards every grid holds what its state says.
+int flush_staged(genpk_ctx *ctx);
+
 int flush_pending(genpk_ctx *ctx)
+{
+    GENPK_TRY(flush_staged(ctx));
+    return flush_acc(ctx);
+}
+
+int flush_staged(genpk_ctx *ctx)
 {
     if (!ctx->pend.active)
         return GENPK_OK;
@@ -596,7 +631,7 @@ struct FusedAuto {
 
 int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused = nullptr)
 {
-    GENPK_TRY(flush_pending(ctx));
+    GENPK_TRY(flush_staged(ctx));
     std::vector<int> todo;
     for (int f : need) {
         const int st = ctx->state[(size_t)f];
@@ -613,6 +648,17 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
     }
     std::sort(todo.begin(), todo.end());
     todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
+    const bool planes = use_xfft(ctx);
+    // The z pass reads a pending accumulator only for a field transformed on
+    // its own (the accumulator holds one field); otherwise convert it now.
+    if (ctx->acc_pending >= 0) {
+        const auto it = std::find(todo.begin(), todo.end(), ctx->acc_pending);
+        const bool alone = planes && it != todo.end() &&
+                           (it == todo.begin() || *(it - 1) != ctx->acc_pending - 1) &&
+                           (it + 1 == todo.end() || *(it + 1) != ctx->acc_pending + 1);
+        if (!alone)
+            GENPK_TRY(flush_acc(ctx));
+    }
     timing_touch(ctx);
     stage_event(ctx, "host");
     size_t i = 0;
@@ -621,19 +667,30 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
         while (j < todo.size() && todo[j] == todo[j - 1] + 1)
             j++;
         const int batch = (int)(j - i);
-        const bool planes = use_xfft(ctx);
-        cufftHandle h;
-        GENPK_TRY(make_r2c(ctx, batch, planes, &h));
         float *base = grid_of(ctx, todo[i]);
-        GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
         if (planes) {
+            // own z, y and x passes (the x pass may bin a single auto spectrum)
+            const bool from_acc = batch == 1 && todo[i] == ctx->acc_pending;
+            GENPK_CUDA(zfft_pass(ctx->gg, base, from_acc ? ctx->dscr.win_acc : nullptr, batch,
+                                 ctx->d_xtw, ctx->d_status, ctx->num_sms, ctx->stream,
+                                 &ctx->launches));
+            if (from_acc)
+                ctx->acc_pending = -1;
+            stage_event(ctx, "zfft");
+            GENPK_CUDA(yfft_pass(ctx->gg, base, batch, ctx->d_xtw, ctx->num_sms, ctx->stream,
+                                 &ctx->launches));
+            stage_event(ctx, "yfft");
             const bool bin = fused && batch == 1 && todo[i] == fused->field;
-            stage_event(ctx, "fft");
             GENPK_CUDA(xfft_pass(ctx->gg, base, batch, ctx->d_xtw, bin ? &fused->bin : nullptr,
                                  ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches));
             stage_event(ctx, bin ? "xfft_bin" : "xfft");
             if (bin)
                 fused->done = true;
+        } else {
+            cufftHandle h;
+            GENPK_TRY(make_r2c(ctx, batch, false, &h));
+            GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
+            stage_event(ctx, "fft");
         }
         for (size_t k = i; k < j; k++) {
             ctx->state[(size_t)todo[k]] = F_SPECTRUM;
@@ -641,7 +698,6 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
         }
         i = j;
     }
-    stage_event(ctx, "fft");
     return GENPK_OK;
 }
 
@@ -910,7 +966,9 @@ int genpk_zero(genpk_ctx *ctx, int field)
     GENPK_TRY(check_field(ctx, field));
     cudaSetDevice(ctx->device);
     if (ctx->pend.active && ctx->pend.field == field)
-        GENPK_TRY(flush_pending(ctx));
+        GENPK_TRY(flush_staged(ctx));
+    if (ctx->acc_pending == field)
+        ctx->acc_pending = -1;  // its accumulator is not needed any more
     ctx->state[(size_t)field] = F_CLEAN;
     ctx->auto_valid[(size_t)field] = false;
     GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
@@ -1057,7 +1115,9 @@ int genpk_sync(genpk_ctx *ctx)
     if (!ctx)
         return GENPK_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    GENPK_TRY(flush_pending(ctx));
+    // A pass left in the accumulator counts as done: its grid is materialised
+    // when something reads it.
+    GENPK_TRY(flush_staged(ctx));
     return collect_status(ctx);
 }
 

@@ -124,11 +124,19 @@ cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
 // One window-engine pass; mass_part needs mass_ctas doubles (variable masses);
 // acc (nfloat 64-bit integers) is the exact accumulator.  stream_mode: the
 // stream mode (reductions straight to acc, neighbour-merged), no windows.
+// defer_convert (clean grids only): acc is left holding the pass, for
+// zfft_pass to read or window_convert to turn into the FP32 grid later (both
+// use the pass's mean and scale in dstat: no other pass may run before).
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
                                 bool stream_mode, double *mass_part, int mass_ctas,
-                                unsigned long long *acc, int num_sms, DeviceStatus *dstat,
-                                cudaStream_t stream, int64_t *launches, StageHook hook,
-                                void *hook_user);
+                                unsigned long long *acc, bool defer_convert, int num_sms,
+                                DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
+                                StageHook hook, void *hook_user);
+// The accumulator of the last window pass minus its mean, rounded once to FP32,
+// into `grid` (clean: stored, else added).
+cudaError_t window_convert(const GridGeom &g, const unsigned long long *acc, float *grid,
+                           bool clean, const DeviceStatus *dstat, int num_sms,
+                           cudaStream_t stream, int64_t *launches);
 
 // ---------------------------------------------------------------------------
 // Binning (deconvolution + log-k shells)
@@ -181,6 +189,16 @@ bool xfft_supported(int dims);
 bool xfft_bin_supported(int dims, int nrbins);
 void xfft_twiddles(int dims, std::vector<float> *out);  // 2*dims floats
 int xfft_bin_ctas(int dims, int nbatch, int num_sms);
+// The z and y transforms of every x-plane for xfft_supported sizes (xfft.cu):
+// zfft_pass is the length-N r2c along z, from the grids in place or (acc not
+// null, nbatch 1) from the window engine's 64-bit accumulator, converted as
+// its conversion pass does; yfft_pass is the complex length-N pass along y.
+// Followed by xfft_pass they leave the 3-D r2c transform.
+cudaError_t zfft_pass(const GridGeom &g, float *grids, const unsigned long long *acc, int nbatch,
+                      const float2 *tw, const DeviceStatus *dstat, int num_sms,
+                      cudaStream_t stream, int64_t *launches);
+cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int num_sms,
+                      cudaStream_t stream, int64_t *launches);
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
                       const XfftBin *bin, int num_sms, DeviceStatus *dstat, cudaStream_t stream,
                       int64_t *launches);

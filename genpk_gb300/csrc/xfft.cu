@@ -571,6 +571,234 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         atomicAdd(&st->timeouts, (unsigned long long)timeouts);
 }
 
+// ---- z and y passes of the forward transform (64 <= N <= 512, powers of two)
+//
+// k_zfft: the length-N real-to-complex transform of every z row, one warp per
+// row.  The row's N reals become M = N/2 complex values z[n] = x[2n] +
+// i x[2n+1]; an M-point FFT with n = lane + 32 m (R = M/32 values per lane):
+//   1. an R-point DFT over m in registers, twiddles W_M^{lane k1};
+//   2. the 32-point DFTs over lanes, one per k1: for R = 8, a shared-memory
+//      exchange gives the four lanes 4 k1 + q the values of l = q + 4 i
+//      (i = 0..7); an 8-point DFT over i in registers, twiddles W_32^{q ki},
+//      a 4-point DFT across those four lanes (two shuffle stages).  For
+//      R < 8, five radix-2 shuffle stages across the warp;
+//   3. X[k] = E[k] + W_N^k O[k], k = 0..M, with E = (Z[k] + conj Z[M-k]) / 2
+//      and O = (Z[k] - conj Z[M-k]) / 2i.
+// The input is the FP32 grid (in place: a warp holds its whole row before
+// writing it) or the window engine's 64-bit accumulator, converted as
+// k_window_convert does (accumulator minus the fixed-point mean, rounded once).
+// Accumulator rows are prefetched one row ahead by 16-byte asynchronous
+// copies into a per-warp buffer; each lane copies and later reads only its
+// own chunks, so the buffer needs no warp synchronisation.
+constexpr int kZThreads = 256;
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ int zpad(int i)
+{
+    return i + (i >> 5);
+}
+
+// Radix-2 decimation-in-frequency step across lanes xor s (upper lanes take
+// (a - b) W, lower lanes a + b).
+__device__ __forceinline__ float2 dif_shfl(float2 v, int s, bool upper, float2 w)
+{
+    const float2 q = make_float2(__shfl_xor_sync(0xffffffffu, v.x, s),
+                                 __shfl_xor_sync(0xffffffffu, v.y, s));
+    return upper ? cmul(csub(q, v), w) : cadd(v, q);
+}
+
+template <int N, bool FROM_ACC>
+__global__ void __launch_bounds__(kZThreads)
+    k_zfft(const unsigned long long *__restrict__ acc, float *grid, int64_t nrows,
+           int row_floats, const float2 *__restrict__ tw_g, const DeviceStatus *__restrict__ st)
+{
+    constexpr int M = N / 2;
+    constexpr int R = M / 32;
+    __shared__ float2 tw[N];
+    __shared__ float2 zs_all[kZThreads / 32][M + M / 32];  // Z[k] (or exchange) at zpad(k)
+    extern __shared__ __align__(16) unsigned char zdyn[];  // [warps][M] longlong2 (FROM_ACC)
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        tw[i] = tw_g[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float2 *zs = zs_all[wid];
+    longlong2 *pre = reinterpret_cast<longlong2 *>(zdyn) + (FROM_ACC ? wid * M : 0);
+    auto prefetch = [&](int64_t r) {
+        const longlong2 *src = reinterpret_cast<const longlong2 *>(acc + (size_t)r * row_floats);
+#pragma unroll
+        for (int m = 0; m < R; m++)
+            cp_async16(pre + lane + 32 * m, src + lane + 32 * m);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    const long long mean = FROM_ACC ? st->mean_fixed : 0;
+    const float inv_scale = FROM_ACC ? ldexpf(1.f, -st->fx_shift) : 0.f;
+    const int br = (int)(__brev((unsigned)lane) >> 27);
+    const int k1g = lane >> 2, qg = lane & 3;                   // R = 8: group and member
+    const int qrev = ((qg & 1) << 1) | (qg >> 1);               // 2-bit reversal
+    const int64_t nw = (int64_t)gridDim.x * (kZThreads / 32);
+    const int64_t row0 = (int64_t)blockIdx.x * (kZThreads / 32) + wid;
+    if (FROM_ACC && row0 < nrows)
+        prefetch(row0);
+    for (int64_t row = row0; row < nrows; row += nw) {
+        const size_t base = (size_t)row * (size_t)row_floats;
+        float2 v[R];
+        if (FROM_ACC)
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            const int n = lane + 32 * m;
+            if (FROM_ACC) {
+                const longlong2 a = pre[n];
+                v[m] = make_float2(i64_to_f32_rn(a.x - mean) * inv_scale,
+                                   i64_to_f32_rn(a.y - mean) * inv_scale);
+            } else {
+                v[m] = reinterpret_cast<const float2 *>(grid + base)[n];
+            }
+        }
+        // the values are in registers: this lane's chunks of the buffer are free
+        if (FROM_ACC && row + nw < nrows)
+            prefetch(row + nw);
+        if constexpr (R > 1)
+            dft<R>(v);
+#pragma unroll
+        for (int k1 = 1; k1 < R; k1++)
+            v[k1] = cmul(v[k1], tw[(2 * lane * k1) & (N - 1)]);
+        if constexpr (R == 8) {
+            // exchange: y_l[k1] at (k1, l) -> lane 4 k1 + q takes l = q + 4 i
+#pragma unroll
+            for (int k1 = 0; k1 < 8; k1++)
+                zs[zpad(k1 * 32 + lane)] = v[k1];
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                v[i] = zs[zpad(k1g * 32 + qg + 4 * i)];
+            __syncwarp();
+            dft8(v);
+#pragma unroll
+            for (int ki = 1; ki < 8; ki++)
+                v[ki] = cmul(v[ki], tw[(qg * ki * (N / 32)) & (N - 1)]);  // W_32^{q ki}
+            // 4-point DFT over q across the lanes of the group (xor 2, then xor 1)
+            const float2 w2 = tw[(qg & 1) * (N / 4)];  // W_4^{q mod 2}
+#pragma unroll
+            for (int ki = 0; ki < 8; ki++) {
+                v[ki] = dif_shfl(v[ki], 2, (qg & 2) != 0, w2);
+                v[ki] = dif_shfl(v[ki], 1, (qg & 1) != 0, make_float2(1.f, 0.f));
+            }
+            // lane holds Z[k1 + 8 (ki + 8 bitrev2(q))]
+#pragma unroll
+            for (int ki = 0; ki < 8; ki++)
+                zs[zpad(k1g + 8 * (ki + 8 * qrev))] = v[ki];
+        } else {
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) {
+                const bool upper = (lane & s) != 0;
+                const float2 w = tw[(lane & (s - 1)) * (N / (2 * s))];  // W_{2s}^{lane mod s}
+#pragma unroll
+                for (int k1 = 0; k1 < R; k1++)
+                    v[k1] = dif_shfl(v[k1], s, upper, w);
+            }
+            // lane holds Z[k1 + R bitrev5(lane)]
+#pragma unroll
+            for (int k1 = 0; k1 < R; k1++)
+                zs[zpad(k1 + R * br)] = v[k1];
+        }
+        __syncwarp();
+        float2 *out = reinterpret_cast<float2 *>(grid + base);
+#pragma unroll
+        for (int j = 0; j <= R; j++) {
+            const int k = lane + 32 * j;
+            if (k <= M) {
+                const int ka = k == M ? 0 : k;      // Z[N/2] = Z[0]
+                const int kb = k == 0 ? 0 : M - k;  // Z[(N/2 - k) mod N/2]
+                const float2 a = zs[zpad(ka)], b = zs[zpad(kb)];
+                const float2 e = make_float2(a.x + b.x, a.y - b.y);
+                const float2 o = make_float2(a.x - b.x, a.y + b.y);
+                const float2 wo = cmul(tw[k], o);
+                out[k] = make_float2(0.5f * (e.x + wo.y), 0.5f * (e.y - wo.x));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// k_yfft: the length-N complex transform along y of every (x-plane, kz)
+// column, in place in the in-place r2c layout.  Tiles of N rows x TZ columns
+// (consecutive kz of one x-plane) are copied into shared memory by 8-byte
+// asynchronous copies (cp.async; the rows are (N/2+1)*8 bytes apart, which
+// tensor copies cannot address), double-buffered so the next tile streams in
+// while this one is transformed by the x pass's Stockham stages; the last
+// stage writes straight back.  Columns past kz = N/2 are zero-filled.
+__device__ __forceinline__ void cp_async8(void *dst, const void *src, unsigned src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
+    k_yfft(float2 *spec, int hc, int tiles_per_plane, int64_t ntiles,
+           const float2 *__restrict__ tw_g)
+{
+    constexpr int TZ = kXTileBytes / 8 / N;
+    using P = FftPlan<N>;
+    extern __shared__ __align__(16) unsigned char ys[];
+    float2 *tiles = reinterpret_cast<float2 *>(ys);                   // [2][N][TZ]
+    float2 *tw_s = reinterpret_cast<float2 *>(ys + 2 * kXTileBytes);  // [N]
+    const int tid = threadIdx.x;
+    const int c = tid % TZ, g = tid / TZ;
+    for (int i = tid; i < N; i += kXThreads)
+        tw_s[i] = tw_g[i];
+    auto fetch = [&](int64_t t, float2 *dst) {
+        const int64_t plane = t / tiles_per_plane;
+        const int kz0 = (int)(t - plane * tiles_per_plane) * TZ;
+        const float2 *pl = spec + (size_t)plane * (size_t)N * (size_t)hc;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int e = tid + kXThreads * q;
+            const int row = e / TZ, col = e - row * TZ;
+            const int kz = kz0 + col;
+            const bool in = kz < hc;
+            cp_async8(dst + row * TZ + col, pl + (size_t)row * hc + (in ? kz : 0), in ? 8u : 0u);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int k = 0;
+    if ((int64_t)blockIdx.x < ntiles)
+        fetch(blockIdx.x, tiles);
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
+        float2 *tile = tiles + (k & 1) * (kXTileBytes / (int)sizeof(float2));
+        __syncthreads();  // every thread is done with the other buffer
+        const bool next = t + gridDim.x < ntiles;
+        if (next)
+            fetch(t + gridDim.x, tiles + ((k + 1) & 1) * (kXTileBytes / (int)sizeof(float2)));
+        if (next)
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();  // this tile's copies, from every thread, have landed
+        const int64_t plane = t / tiles_per_plane;
+        const int kz0 = (int)(t - plane * tiles_per_plane) * TZ;
+        float2 *pl = spec + (size_t)plane * (size_t)N * (size_t)hc;
+        float2 v[8];
+        fft_to_last<N>(tile, tw_s, c, g, v);
+        const int kz = kz0 + c;
+        if (kz < hc) {
+#pragma unroll
+            for (int m = 0; m < 8 / P::RL; m++)
+#pragma unroll
+                for (int r = 0; r < P::RL; r++)
+                    pl[(size_t)stage_out_row<N, P::NSL, P::RL>(g, m, r) * hc + kz] =
+                        v[m * P::RL + r];
+        }
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -701,6 +929,79 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
                                     (int)smem)) != cudaSuccess)
         return err;
     kern<<<ctas, kXThreads, smem, stream>>>(map, p, dstat);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t zfft_pass(const GridGeom &g, float *grids, const unsigned long long *acc, int nbatch,
+                      const float2 *tw, const DeviceStatus *dstat, int num_sms,
+                      cudaStream_t stream, int64_t *launches)
+{
+    const int n = g.dims;
+    const int64_t nrows = (int64_t)n * n * nbatch;
+    const int ctas = (int)std::min<int64_t>((nrows + 7) / 8, (int64_t)num_sms * 8);
+    // prefetch buffers of the accumulator rows: one row per warp
+    const int pre = (int)(sizeof(longlong2) * (kZThreads / 32) * (n / 2));
+    cudaError_t err = cudaSuccess;
+#define GENPK_ZFFT(NN)                                                                        \
+    case NN:                                                                                  \
+        if (acc) {                                                                            \
+            err = cudaFuncSetAttribute(k_zfft<NN, true>,                                      \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, pre);     \
+            if (err != cudaSuccess)                                                           \
+                return err;                                                                   \
+            k_zfft<NN, true><<<ctas, kZThreads, pre, stream>>>(acc, grids, nrows, g.row, tw,  \
+                                                               dstat);                        \
+        } else {                                                                              \
+            k_zfft<NN, false><<<ctas, kZThreads, 0, stream>>>(nullptr, grids, nrows, g.row,   \
+                                                              tw, dstat);                     \
+        }                                                                                     \
+        break;
+    switch (n) {
+        GENPK_ZFFT(64)
+        GENPK_ZFFT(128)
+        GENPK_ZFFT(256)
+        GENPK_ZFFT(512)
+    default:
+        return cudaErrorNotSupported;
+    }
+#undef GENPK_ZFFT
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int num_sms,
+                      cudaStream_t stream, int64_t *launches)
+{
+    const int n = g.dims;
+    const int tz = xfft_tz(n);
+    const int per_plane = (g.hc + tz - 1) / tz;
+    const int64_t ntiles = (int64_t)per_plane * n * nbatch;
+    const int ctas = (int)std::min<int64_t>(ntiles, (int64_t)num_sms * kXCtasPerSm);
+    const size_t smem = 2 * kXTileBytes + sizeof(float2) * n;
+    void (*kern)(float2 *, int, int, int64_t, const float2 *) = nullptr;
+    switch (n) {
+    case 64:
+        kern = k_yfft<64>;
+        break;
+    case 128:
+        kern = k_yfft<128>;
+        break;
+    case 256:
+        kern = k_yfft<256>;
+        break;
+    case 512:
+        kern = k_yfft<512>;
+        break;
+    default:
+        return cudaErrorNotSupported;
+    }
+    cudaError_t err;
+    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem)) != cudaSuccess)
+        return err;
+    kern<<<ctas, kXThreads, smem, stream>>>(reinterpret_cast<float2 *>(grids), g.hc, per_plane,
+                                            ntiles, tw);
     (*launches)++;
     return cudaGetLastError();
 }
