@@ -614,8 +614,8 @@ int make_c2r(genpk_ctx *ctx)
     return GENPK_OK;
 }
 
-// Bring every field in `need` to SPECTRUM form: pending deposits first, then
-// one batched r2c per run of consecutive field indices.
+// The own x pass (and, for a field pending in the accumulator, the own z and y
+// passes) replace cuFFT's x axis for the supported sizes.
 bool use_xfft(const genpk_ctx *ctx)
 {
     return ctx->fft_mode == GENPK_FFT_AUTO && ctx->d_xtw != nullptr;
@@ -629,6 +629,8 @@ struct FusedAuto {
     bool done;
 };
 
+// Bring every field in `need` to SPECTRUM form: pending deposits first, then
+// one batched r2c per run of consecutive field indices.
 int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused = nullptr)
 {
     GENPK_TRY(flush_staged(ctx));
@@ -649,37 +651,38 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
     std::sort(todo.begin(), todo.end());
     todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
     const bool planes = use_xfft(ctx);
-    // The z pass reads a pending accumulator only for a field transformed on
-    // its own (the accumulator holds one field); otherwise convert it now.
-    if (ctx->acc_pending >= 0) {
-        const auto it = std::find(todo.begin(), todo.end(), ctx->acc_pending);
-        const bool alone = planes && it != todo.end() &&
-                           (it == todo.begin() || *(it - 1) != ctx->acc_pending - 1) &&
-                           (it + 1 == todo.end() || *(it + 1) != ctx->acc_pending + 1);
-        if (!alone)
-            GENPK_TRY(flush_acc(ctx));
-    }
+    // A field whose pass is still in the accumulator is transformed on its own
+    // by the own z pass (which reads the accumulator) and y pass; other runs of
+    // consecutive fields take one batched 2-D cuFFT over their x-planes.  Both
+    // then run the x pass.
+    const int pend = planes ? ctx->acc_pending : -1;
+    if (ctx->acc_pending >= 0 && (pend < 0 || std::find(todo.begin(), todo.end(), pend) == todo.end()))
+        GENPK_TRY(flush_acc(ctx));
     timing_touch(ctx);
     stage_event(ctx, "host");
     size_t i = 0;
     while (i < todo.size()) {
         size_t j = i + 1;
-        while (j < todo.size() && todo[j] == todo[j - 1] + 1)
-            j++;
+        if (todo[i] != pend)
+            while (j < todo.size() && todo[j] == todo[j - 1] + 1 && todo[j] != pend)
+                j++;
         const int batch = (int)(j - i);
         float *base = grid_of(ctx, todo[i]);
         if (planes) {
-            // own z, y and x passes (the x pass may bin a single auto spectrum)
-            const bool from_acc = batch == 1 && todo[i] == ctx->acc_pending;
-            GENPK_CUDA(zfft_pass(ctx->gg, base, from_acc ? ctx->dscr.win_acc : nullptr, batch,
-                                 ctx->d_xtw, ctx->d_status, ctx->num_sms, ctx->stream,
-                                 &ctx->launches));
-            if (from_acc)
+            if (todo[i] == pend) {
+                GENPK_CUDA(zfft_pass(ctx->gg, base, ctx->dscr.win_acc, ctx->d_xtw, ctx->d_status,
+                                     ctx->num_sms, ctx->stream, &ctx->launches));
                 ctx->acc_pending = -1;
-            stage_event(ctx, "zfft");
-            GENPK_CUDA(yfft_pass(ctx->gg, base, batch, ctx->d_xtw, ctx->num_sms, ctx->stream,
-                                 &ctx->launches));
-            stage_event(ctx, "yfft");
+                stage_event(ctx, "zfft");
+                GENPK_CUDA(yfft_pass(ctx->gg, base, 1, ctx->d_xtw, ctx->num_sms, ctx->stream,
+                                     &ctx->launches));
+                stage_event(ctx, "yfft");
+            } else {
+                cufftHandle h;
+                GENPK_TRY(make_r2c(ctx, batch, true, &h));
+                GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
+                stage_event(ctx, "fft");
+            }
             const bool bin = fused && batch == 1 && todo[i] == fused->field;
             GENPK_CUDA(xfft_pass(ctx->gg, base, batch, ctx->d_xtw, bin ? &fused->bin : nullptr,
                                  ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches));

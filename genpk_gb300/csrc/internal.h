@@ -190,11 +190,12 @@ bool xfft_bin_supported(int dims, int nrbins);
 void xfft_twiddles(int dims, std::vector<float> *out);  // 2*dims floats
 int xfft_bin_ctas(int dims, int nbatch, int num_sms);
 // The z and y transforms of every x-plane for xfft_supported sizes (xfft.cu):
-// zfft_pass is the length-N r2c along z, from the grids in place or (acc not
-// null, nbatch 1) from the window engine's 64-bit accumulator, converted as
-// its conversion pass does; yfft_pass is the complex length-N pass along y.
-// Followed by xfft_pass they leave the 3-D r2c transform.
-cudaError_t zfft_pass(const GridGeom &g, float *grids, const unsigned long long *acc, int nbatch,
+// zfft_pass is the length-N r2c along z of one grid, read from the window
+// engine's 64-bit accumulator (converted as its conversion pass does, with the
+// pass's mean and scale in dstat) and written to `grid`; yfft_pass is the
+// complex length-N pass along y.  Followed by xfft_pass they leave the 3-D r2c
+// transform.
+cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *acc,
                       const float2 *tw, const DeviceStatus *dstat, int num_sms,
                       cudaStream_t stream, int64_t *launches);
 cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int num_sms,

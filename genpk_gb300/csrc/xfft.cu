@@ -584,12 +584,12 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
 //      R < 8, five radix-2 shuffle stages across the warp;
 //   3. X[k] = E[k] + W_N^k O[k], k = 0..M, with E = (Z[k] + conj Z[M-k]) / 2
 //      and O = (Z[k] - conj Z[M-k]) / 2i.
-// The input is the FP32 grid (in place: a warp holds its whole row before
-// writing it) or the window engine's 64-bit accumulator, converted as
-// k_window_convert does (accumulator minus the fixed-point mean, rounded once).
-// Accumulator rows are prefetched one row ahead by 16-byte asynchronous
-// copies into a per-warp buffer; each lane copies and later reads only its
-// own chunks, so the buffer needs no warp synchronisation.
+// The input is the window engine's 64-bit accumulator, converted as
+// k_window_convert does (accumulator minus the fixed-point mean, rounded
+// once), so that pass is skipped; the output is the FP32 grid's row.  Rows are
+// prefetched one row ahead by 16-byte asynchronous copies into a per-warp
+// buffer; each lane copies and later reads only its own chunks, so the buffer
+// needs no warp synchronisation.
 constexpr int kZThreads = 256;
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
@@ -612,7 +612,7 @@ __device__ __forceinline__ float2 dif_shfl(float2 v, int s, bool upper, float2 w
     return upper ? cmul(csub(q, v), w) : cadd(v, q);
 }
 
-template <int N, bool FROM_ACC>
+template <int N>
 __global__ void __launch_bounds__(kZThreads)
     k_zfft(const unsigned long long *__restrict__ acc, float *grid, int64_t nrows,
            int row_floats, const float2 *__restrict__ tw_g, const DeviceStatus *__restrict__ st)
@@ -621,13 +621,13 @@ __global__ void __launch_bounds__(kZThreads)
     constexpr int R = M / 32;
     __shared__ float2 tw[N];
     __shared__ float2 zs_all[kZThreads / 32][M + M / 32];  // Z[k] (or exchange) at zpad(k)
-    extern __shared__ __align__(16) unsigned char zdyn[];  // [warps][M] longlong2 (FROM_ACC)
+    extern __shared__ __align__(16) unsigned char zdyn[];  // [warps][M] longlong2
     for (int i = threadIdx.x; i < N; i += blockDim.x)
         tw[i] = tw_g[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float2 *zs = zs_all[wid];
-    longlong2 *pre = reinterpret_cast<longlong2 *>(zdyn) + (FROM_ACC ? wid * M : 0);
+    longlong2 *pre = reinterpret_cast<longlong2 *>(zdyn) + wid * M;
     auto prefetch = [&](int64_t r) {
         const longlong2 *src = reinterpret_cast<const longlong2 *>(acc + (size_t)r * row_floats);
 #pragma unroll
@@ -635,33 +635,27 @@ __global__ void __launch_bounds__(kZThreads)
             cp_async16(pre + lane + 32 * m, src + lane + 32 * m);
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    const long long mean = FROM_ACC ? st->mean_fixed : 0;
-    const float inv_scale = FROM_ACC ? ldexpf(1.f, -st->fx_shift) : 0.f;
+    const long long mean = st->mean_fixed;
+    const float inv_scale = ldexpf(1.f, -st->fx_shift);
     const int br = (int)(__brev((unsigned)lane) >> 27);
     const int k1g = lane >> 2, qg = lane & 3;                   // R = 8: group and member
     const int qrev = ((qg & 1) << 1) | (qg >> 1);               // 2-bit reversal
     const int64_t nw = (int64_t)gridDim.x * (kZThreads / 32);
     const int64_t row0 = (int64_t)blockIdx.x * (kZThreads / 32) + wid;
-    if (FROM_ACC && row0 < nrows)
+    if (row0 < nrows)
         prefetch(row0);
     for (int64_t row = row0; row < nrows; row += nw) {
         const size_t base = (size_t)row * (size_t)row_floats;
         float2 v[R];
-        if (FROM_ACC)
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
         for (int m = 0; m < R; m++) {
-            const int n = lane + 32 * m;
-            if (FROM_ACC) {
-                const longlong2 a = pre[n];
-                v[m] = make_float2(i64_to_f32_rn(a.x - mean) * inv_scale,
-                                   i64_to_f32_rn(a.y - mean) * inv_scale);
-            } else {
-                v[m] = reinterpret_cast<const float2 *>(grid + base)[n];
-            }
+            const longlong2 a = pre[lane + 32 * m];
+            v[m] = make_float2(i64_to_f32_rn(a.x - mean) * inv_scale,
+                               i64_to_f32_rn(a.y - mean) * inv_scale);
         }
         // the values are in registers: this lane's chunks of the buffer are free
-        if (FROM_ACC && row + nw < nrows)
+        if (row + nw < nrows)
             prefetch(row + nw);
         if constexpr (R > 1)
             dft<R>(v);
@@ -933,39 +927,38 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
     return cudaGetLastError();
 }
 
-cudaError_t zfft_pass(const GridGeom &g, float *grids, const unsigned long long *acc, int nbatch,
+cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *acc,
                       const float2 *tw, const DeviceStatus *dstat, int num_sms,
                       cudaStream_t stream, int64_t *launches)
 {
     const int n = g.dims;
-    const int64_t nrows = (int64_t)n * n * nbatch;
+    const int64_t nrows = (int64_t)n * n;
     const int ctas = (int)std::min<int64_t>((nrows + 7) / 8, (int64_t)num_sms * 8);
     // prefetch buffers of the accumulator rows: one row per warp
     const int pre = (int)(sizeof(longlong2) * (kZThreads / 32) * (n / 2));
-    cudaError_t err = cudaSuccess;
-#define GENPK_ZFFT(NN)                                                                        \
-    case NN:                                                                                  \
-        if (acc) {                                                                            \
-            err = cudaFuncSetAttribute(k_zfft<NN, true>,                                      \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, pre);     \
-            if (err != cudaSuccess)                                                           \
-                return err;                                                                   \
-            k_zfft<NN, true><<<ctas, kZThreads, pre, stream>>>(acc, grids, nrows, g.row, tw,  \
-                                                               dstat);                        \
-        } else {                                                                              \
-            k_zfft<NN, false><<<ctas, kZThreads, 0, stream>>>(nullptr, grids, nrows, g.row,   \
-                                                              tw, dstat);                     \
-        }                                                                                     \
-        break;
+    void (*kern)(const unsigned long long *, float *, int64_t, int, const float2 *,
+                 const DeviceStatus *) = nullptr;
     switch (n) {
-        GENPK_ZFFT(64)
-        GENPK_ZFFT(128)
-        GENPK_ZFFT(256)
-        GENPK_ZFFT(512)
+    case 64:
+        kern = k_zfft<64>;
+        break;
+    case 128:
+        kern = k_zfft<128>;
+        break;
+    case 256:
+        kern = k_zfft<256>;
+        break;
+    case 512:
+        kern = k_zfft<512>;
+        break;
     default:
         return cudaErrorNotSupported;
     }
-#undef GENPK_ZFFT
+    cudaError_t err;
+    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, pre)) !=
+        cudaSuccess)
+        return err;
+    kern<<<ctas, kZThreads, pre, stream>>>(acc, grid, nrows, g.row, tw, dstat);
     (*launches)++;
     return cudaGetLastError();
 }
