@@ -92,6 +92,12 @@ struct genpk_ctx {
     // 64-bit accumulator: the forward transform reads it from there (the
     // conversion pass is skipped); anything else converts it first.
     int acc_pending = -1;
+    // The accumulator holds zeros (the transform's x pass cleared it after its
+    // contents were used), so the next window pass skips its clear;
+    // acc_spent: its contents were used (converted or read by the z pass) and
+    // the next own x pass may clear it.
+    bool acc_zero = false;
+    bool acc_spent = false;
     // Recent automatic engine choices and the arrays they were made for (a few:
     // one per species of a multi-species loop).  Every engine yields the same
     // grid, so reusing a choice for the same particle arrays (a loop over the
@@ -437,8 +443,10 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         // accumulator: the z pass converts it on the fly.
         const bool defer = a.clean && use_xfft(ctx);
         GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
-                                       mass_ctas, s.win_acc, defer, ctx->num_sms, ctx->d_status,
-                                       ctx->stream, &ctx->launches, hook, ctx));
+                                       mass_ctas, s.win_acc, ctx->acc_zero, defer, ctx->num_sms,
+                                       ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
+        ctx->acc_zero = false;
+        ctx->acc_spent = !defer;  // converted in the pass
         if (defer)
             ctx->acc_pending = f;
     } else {
@@ -473,6 +481,7 @@ int flush_acc(genpk_ctx *ctx)
         return GENPK_OK;
     const int f = ctx->acc_pending;
     ctx->acc_pending = -1;
+    ctx->acc_spent = true;
     GENPK_CUDA(window_convert(ctx->gg, ctx->dscr.win_acc, grid_of(ctx, f), true, ctx->d_status,
                               ctx->num_sms, ctx->stream, &ctx->launches));
     stage_event(ctx, "win_convert");
@@ -660,6 +669,7 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
         GENPK_TRY(flush_acc(ctx));
     timing_touch(ctx);
     stage_event(ctx, "host");
+    const int64_t acc_bytes = (int64_t)sizeof(unsigned long long) * ctx->gg.nfloat;
     size_t i = 0;
     while (i < todo.size()) {
         size_t j = i + 1;
@@ -673,6 +683,7 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
                 GENPK_CUDA(zfft_pass(ctx->gg, base, ctx->dscr.win_acc, ctx->d_xtw, ctx->d_status,
                                      ctx->num_sms, ctx->stream, &ctx->launches));
                 ctx->acc_pending = -1;
+                ctx->acc_spent = true;
                 stage_event(ctx, "zfft");
                 GENPK_CUDA(yfft_pass(ctx->gg, base, 1, ctx->d_xtw, ctx->num_sms, ctx->stream,
                                      &ctx->launches));
@@ -684,8 +695,18 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
                 stage_event(ctx, "fft");
             }
             const bool bin = fused && batch == 1 && todo[i] == fused->field;
+            // The accumulator's clear, once its pass has been used, rides on a
+            // binning x pass, whose bin walk leaves HBM bandwidth idle; the plain
+            // x pass is faster and became HBM-bound with it (0.19 -> 0.36 ms at
+            // N = 512, against 0.15 ms for the separate clear).
+            const bool clear = bin && ctx->acc_spent && ctx->acc_pending < 0 && ctx->dscr.win_acc;
             GENPK_CUDA(xfft_pass(ctx->gg, base, batch, ctx->d_xtw, bin ? &fused->bin : nullptr,
+                                 clear ? ctx->dscr.win_acc : nullptr, clear ? acc_bytes : 0,
                                  ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches));
+            if (clear) {
+                ctx->acc_spent = false;
+                ctx->acc_zero = true;
+            }
             stage_event(ctx, bin ? "xfft_bin" : "xfft");
             if (bin)
                 fused->done = true;
@@ -970,8 +991,10 @@ int genpk_zero(genpk_ctx *ctx, int field)
     cudaSetDevice(ctx->device);
     if (ctx->pend.active && ctx->pend.field == field)
         GENPK_TRY(flush_staged(ctx));
-    if (ctx->acc_pending == field)
+    if (ctx->acc_pending == field) {
         ctx->acc_pending = -1;  // its accumulator is not needed any more
+        ctx->acc_spent = true;
+    }
     ctx->state[(size_t)field] = F_CLEAN;
     ctx->auto_valid[(size_t)field] = false;
     GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));

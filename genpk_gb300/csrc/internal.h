@@ -127,9 +127,12 @@ cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
 // defer_convert (clean grids only): acc is left holding the pass, for
 // zfft_pass to read or window_convert to turn into the FP32 grid later (both
 // use the pass's mean and scale in dstat: no other pass may run before).
+// acc_zero: acc is known to hold zeros (cleared by the last transform's x
+// pass), so the pass skips its clear.
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
                                 bool stream_mode, double *mass_part, int mass_ctas,
-                                unsigned long long *acc, bool defer_convert, int num_sms,
+                                unsigned long long *acc, bool acc_zero, bool defer_convert,
+                                int num_sms,
                                 DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
                                 StageHook hook, void *hook_user);
 // The accumulator of the last window pass minus its mean, rounded once to FP32,
@@ -194,15 +197,19 @@ int xfft_bin_ctas(int dims, int nbatch, int num_sms);
 // engine's 64-bit accumulator (converted as its conversion pass does, with the
 // pass's mean and scale in dstat) and written to `grid`; yfft_pass is the
 // complex length-N pass along y.  Followed by xfft_pass they leave the 3-D r2c
-// transform.
+// transform.  xfft_pass also stores zeros over `zero_bytes` (a multiple of 16)
+// at `zero`, when not null, spread over its tiles: the accumulator's clear for
+// the next deposit pass, in HBM bandwidth that the binning x pass leaves idle
+// (1.08 GB at N = 512 added 0.08 ms to it, against 0.15 ms for a separate
+// clear; the y pass slowed more for half of it).
 cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *acc,
                       const float2 *tw, const DeviceStatus *dstat, int num_sms,
                       cudaStream_t stream, int64_t *launches);
 cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int num_sms,
                       cudaStream_t stream, int64_t *launches);
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
-                      const XfftBin *bin, int num_sms, DeviceStatus *dstat, cudaStream_t stream,
-                      int64_t *launches);
+                      const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
+                      DeviceStatus *dstat, cudaStream_t stream, int64_t *launches);
 
 struct BinDevice {
     uint32_t *thr = nullptr;   // [nrbins+1]

@@ -45,6 +45,9 @@ constexpr int kXTileBytes = 32 * 1024;  // N rows x (4096/N) complex
 constexpr int kXMaxBins = 256;
 
 struct XParams {
+    uint4 *zero;           // region to clear (16-byte units), or null
+    int64_t zero_units;
+    int64_t zero_per_tile; // units cleared per tile
     int dims, hc, tz;
     int log2n;
     int n8;                // radix-8 stages before the last stage
@@ -61,6 +64,21 @@ struct XParams {
     const double *corner;  // exact (N/2,N/2,N/2) value or null
     double *partial;       // [gridDim.x][nrbins]
 };
+
+// This tile's share of a region cleared alongside the x pass: units
+// [t * per, (t + 1) * per) of the region's n 16-byte units, as streaming
+// stores (nothing waits on them; they use HBM bandwidth that the pass's
+// shared-memory-bound stages leave idle).
+template <int THREADS>
+__device__ __forceinline__ void zero_share(uint4 *z, int64_t n, int64_t per, int64_t t, int tid)
+{
+    if (z == nullptr)
+        return;
+    const int64_t a = t * per;
+    const int64_t e = min(a + per, n);
+    for (int64_t u = a + tid; u < e; u += THREADS)
+        __stcs(z + u, make_uint4(0u, 0u, 0u, 0u));
+}
 
 struct ColInfo {
     int r2;      // ky^2 + kz^2, or -1 for a column past the end
@@ -462,6 +480,7 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
             }
             cols2[(k & 1) * TZ + tid] = ci;
         }
+        zero_share<kXThreads>(p.zero, p.zero_units, p.zero_per_tile, t, tid);
         if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
             timeouts++;
         __syncthreads();
@@ -726,7 +745,10 @@ __global__ void __launch_bounds__(kZThreads)
 // asynchronous copies (cp.async; the rows are (N/2+1)*8 bytes apart, which
 // tensor copies cannot address), double-buffered so the next tile streams in
 // while this one is transformed by the x pass's Stockham stages; the last
-// stage writes straight back.  Columns past kz = N/2 are zero-filled.
+// stage writes straight back.  Columns past kz = N/2 are zero-filled.  (A third
+// buffer for the stages to alternate between, halving the barriers, made the
+// pass slower: 100 KB of shared memory per CTA leaves the 8-byte copies, which
+// go through L1, too little of it.)
 __device__ __forceinline__ void cp_async8(void *dst, const void *src, unsigned src_bytes)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src),
@@ -862,8 +884,8 @@ void xfft_twiddles(int dims, std::vector<float> *out)
 }
 
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
-                      const XfftBin *bin, int num_sms, DeviceStatus *dstat, cudaStream_t stream,
-                      int64_t *launches)
+                      const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
+                      DeviceStatus *dstat, cudaStream_t stream, int64_t *launches)
 {
     EncodeTiledFn enc = encode_fn();
     if (!enc)
@@ -891,6 +913,9 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
     p.iw = bin ? bin->iw : nullptr;
     p.corner = bin ? bin->corner : nullptr;
     p.partial = bin ? bin->partial : nullptr;
+    p.zero = zero_bytes > 0 ? static_cast<uint4 *>(zero) : nullptr;
+    p.zero_units = zero_bytes / 16;
+    p.zero_per_tile = (p.zero_units + p.ntiles - 1) / p.ntiles;
 
     CUtensorMap map;
     const cuuint64_t gdim[2] = {(cuuint64_t)2 * p.ncols, (cuuint64_t)n * nbatch};

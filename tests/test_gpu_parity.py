@@ -599,6 +599,77 @@ def test_fft_paths_agree(gp, dims):
         bins_close(pa, pr, cr)
 
 
+@pytest.mark.parametrize("engine", ["window", "stream"])
+def test_accumulator_cleared_by_the_transform(gp, engine):
+    """The own x pass clears the window engine's 64-bit accumulator once its
+    pass has been used (read by the z pass, or converted), and the next window
+    pass skips its own clear.  Spectra through one reused context equal those
+    of fresh contexts bit for bit: single-field steps, two fields per step (one
+    converted and batched through the 2-D transform), and a += pass whose
+    accumulator was cleared by the x pass of another field's spectrum."""
+    from genpk_gb300 import synth
+    dims, box, nrbins = 128, 1000.0, 32
+    eng = {"window": gp.api.ENGINE_WINDOW, "stream": gp.api.ENGINE_STREAM}[engine]
+    boxes = [synth.zeldovich(128, box, seed=s) for s in (31, 32, 33)]
+    m = O.total_mass(len(boxes[0]), None, 1.0)
+    pairs, pm = [(0, 0), (1, 1), (0, 1)], [(m, m)] * 3
+
+    def fresh(steps):
+        with gp.Context(dims, nrbins, nfields=2) as c:
+            c.set_engine(eng)
+            return steps(c)
+
+    def single(pos):
+        def steps(c):
+            c.zero(0)
+            c.deposit(0, box, pos, None, 1.0)
+            return c.power(0, 0, m, m)
+        return steps
+
+    def double(pa, pb):
+        def steps(c):
+            c.zero(0)
+            c.zero(1)
+            c.deposit(0, box, pa, None, 1.0)
+            c.deposit(1, box, pb, None, 1.0)
+            return c.power_multi(pairs, pm)
+        return steps
+
+    def same(a, b):
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
+
+    with gp.Context(dims, nrbins, nfields=2) as ctx:
+        ctx.set_engine(eng)
+        for pos in boxes:
+            same(single(pos)(ctx), fresh(single(pos)))
+        for pa, pb in ((boxes[0], boxes[1]), (boxes[2], boxes[0])):
+            same(double(pa, pb)(ctx), fresh(double(pa, pb)))
+        same(single(boxes[1])(ctx), fresh(single(boxes[1])))
+        # field 0 pending, field 1's spectrum converts it and clears the
+        # accumulator; the += pass into field 0 then starts from that clear
+        ctx.zero(0)
+        ctx.zero(1)
+        ctx.deposit(1, box, boxes[2], None, 1.0)
+        ctx.deposit(0, box, boxes[0], None, 1.0)
+        ctx.power(1, 1, m, m)
+        ctx.deposit(0, box, boxes[1], None, 1.0)
+        got = ctx.power(0, 0, 2 * m, 2 * m)
+
+    def twice(c):
+        # two passes, as above (without the sync the two staged host deposits
+        # would merge into one pass, rounded to FP32 once instead of twice)
+        c.zero(0)
+        c.deposit(0, box, boxes[0], None, 1.0)
+        c.sync()
+        c.deposit(0, box, boxes[1], None, 1.0)
+        return c.power(0, 0, 2 * m, 2 * m)
+    same(got, fresh(twice))
+    pr, cr, _ = O.pk(np.concatenate([boxes[0], boxes[1]]), box, dims, nrbins, None, 1.0,
+                     m_norm=2 * m)
+    bins_close(got[0], pr, cr)
+
+
 def test_cross_and_multi_spectra(gp):
     from genpk_gb300 import synth
     dims, box, nrbins = 64, 1000.0, 24
