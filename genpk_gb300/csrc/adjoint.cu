@@ -30,41 +30,66 @@ struct ModeGradParams {
     int64_t nmodes;
 };
 
+// One warp per (x, y) row of the half-complex spectrum: kx, ky, iw(kx) iw(ky)
+// and kx^2 + ky^2 once per row (no 64-bit division per mode), lanes over kz,
+// U modes per lane loaded before any is used.  Along a lane's kz the modulus
+// only grows, so after one log-guided lookup its bin only steps up.
 __global__ void __launch_bounds__(256)
     k_mode_gradient(ModeGradParams p, float2 *__restrict__ spec, const uint32_t *__restrict__ thr_g,
                     const float *__restrict__ iw, const float *__restrict__ gcoef)
 {
+    constexpr int U = 8;
     extern __shared__ uint32_t thr[];
     for (int i = threadIdx.x; i <= p.nrbins; i += blockDim.x)
         thr[i] = thr_g[i];
     __syncthreads();
     const bool even = (p.dims & 1) == 0;
-    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < p.nmodes;
-         m += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = m / p.hc;
-        const int kz = (int)(m - r * p.hc);
-        const int i = (int)(r / p.dims), j = (int)(r - (int64_t)i * p.dims);
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int nrows = p.dims * p.dims;
+    for (int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < nrows;
+         row += nwarps) {
+        const int i = row / p.dims, j = row - i * p.dims;
         const int ki = kval_adj(i, p.dims), kj = kval_adj(j, p.dims);
-        const uint32_t kk2 = (uint32_t)(ki * ki + kj * kj + kz * kz);
-        float2 h = make_float2(0.f, 0.f);
-        if (kk2 != 0) {
-            int b = (int)(p.bpu_half * __logf((float)kk2));
-            b = max(0, min(p.nrbins - 1, b));
-            while (b + 1 < p.nrbins && kk2 >= thr[b + 1])
-                b++;
-            while (b > 0 && kk2 < thr[b])
-                b--;
-            const float pz = (__ldg(iw + i) * __ldg(iw + j)) * __ldg(iw + kz);
-            const float p2 = pz * pz;
-            const bool edge = (kz == 0 || kz == p.half);        // reference weight 1
-            const bool selfconj = (kz == 0) || (even && kz == p.half);  // c2r counts once
-            const float cm = edge ? 1.f : 2.f;
-            const float mult = selfconj ? 1.f : 2.f;
-            const float s = __ldg(gcoef + b) * (p2 * p2) * (cm / mult);
-            const float2 f = spec[m];
-            h = make_float2(s * f.x, s * f.y);
+        const uint32_t r2 = (uint32_t)(ki * ki + kj * kj);
+        const float wij = __ldg(iw + i) * __ldg(iw + j);
+        float2 *rp = spec + (size_t)row * (size_t)p.hc;
+        int b = -1;
+        for (int kz0 = 0; kz0 < p.hc; kz0 += 32 * U) {
+            float2 f[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int kz = kz0 + lane + 32 * u;
+                f[u] = kz < p.hc ? rp[kz] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int kz = kz0 + lane + 32 * u;
+                if (kz >= p.hc)
+                    break;
+                const uint32_t kk2 = r2 + (uint32_t)(kz * kz);
+                float2 h = make_float2(0.f, 0.f);
+                if (kk2 != 0) {
+                    if (b < 0) {
+                        b = (int)(p.bpu_half * __logf((float)kk2));
+                        b = max(0, min(p.nrbins - 1, b));
+                        while (b > 0 && kk2 < thr[b])
+                            b--;
+                    }
+                    while (b + 1 < p.nrbins && kk2 >= thr[b + 1])
+                        b++;
+                    const float pz = wij * __ldg(iw + kz);
+                    const float p2 = pz * pz;
+                    const bool edge = (kz == 0 || kz == p.half);               // reference weight 1
+                    const bool selfconj = (kz == 0) || (even && kz == p.half);  // c2r counts once
+                    const float cm = edge ? 1.f : 2.f;
+                    const float mult = selfconj ? 1.f : 2.f;
+                    const float sc = __ldg(gcoef + b) * (p2 * p2) * (cm / mult);
+                    h = make_float2(sc * f[u].x, sc * f[u].y);
+                }
+                rp[kz] = h;
+            }
         }
-        spec[m] = h;
     }
 }
 
@@ -79,6 +104,52 @@ struct GatherParams {
     int64_t n;
 };
 
+// The trilinear value and the three derivatives of dL/drho at one particle.
+struct GatherOut {
+    float gx, gy, gz, val;
+};
+
+__device__ __forceinline__ GatherOut gather_one(const GatherParams &p, const float *__restrict__ grid,
+                                                float x, float y, float z, float m)
+{
+    int c[3];
+    float d[3];
+    split_cell(x, p.uh, p.ul, p.dims, c[0], d[0]);
+    split_cell(y, p.uh, p.ul, p.dims, c[1], d[1]);
+    split_cell(z, p.uh, p.ul, p.dims, c[2], d[2]);
+    int h[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        h[a] = c[a] + 1 == p.dims ? 0 : c[a] + 1;
+    float g[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        g[k] = __ldg(grid + cell_index(p.plane, p.row, (k & 1) ? h[0] : c[0], (k & 2) ? h[1] : c[1],
+                                       (k & 4) ? h[2] : c[2]));
+    const float t0 = 1.f - d[0], t1 = 1.f - d[1];
+    // Interpolate along z first, then y, then x; derivatives from the same tree.
+    const float g00 = fmaf(d[2], g[4] - g[0], g[0]);  // (x0,y0)
+    const float g10 = fmaf(d[2], g[5] - g[1], g[1]);  // (x1,y0)
+    const float g01 = fmaf(d[2], g[6] - g[2], g[2]);  // (x0,y1)
+    const float g11 = fmaf(d[2], g[7] - g[3], g[3]);  // (x1,y1)
+    const float gx0 = fmaf(d[1], g01 - g00, g00);
+    const float gx1 = fmaf(d[1], g11 - g10, g10);
+    const float val = fmaf(d[0], gx1 - gx0, gx0);
+    const float dgx = gx1 - gx0;
+    const float gy0 = fmaf(d[0], g10 - g00, g00);
+    const float gy1 = fmaf(d[0], g11 - g01, g01);
+    const float dgy = gy1 - gy0;
+    // d/dz: bilinear in (x, y) of the z-differences.
+    const float e00 = g[4] - g[0], e10 = g[5] - g[1], e01 = g[6] - g[2], e11 = g[7] - g[3];
+    const float dgz = t0 * (t1 * e00 + d[1] * e01) + d[0] * (t1 * e10 + d[1] * e11);
+    const float s = m * p.units;
+    return {s * dgx, s * dgy, s * dgz, val};
+}
+
+// One particle per thread, grid-stride.  (Tiles of 1024 particles staged
+// through shared memory with 16-byte loads and stores, four particles per
+// thread, ran slower: 1.20 ms against 0.93 at 512^3, with fewer warps resident
+// to cover the grid loads' latency.)  Non-finite positions get zero gradients.
 template <bool VARMASS>
 __global__ void __launch_bounds__(256)
     k_gather(GatherParams p, const float *__restrict__ grid, const float *__restrict__ pos,
@@ -94,43 +165,12 @@ __global__ void __launch_bounds__(256)
                 gmass[i] = 0.f;
             continue;
         }
-        int c[3];
-        float d[3];
-        split_cell(x, p.uh, p.ul, p.dims, c[0], d[0]);
-        split_cell(y, p.uh, p.ul, p.dims, c[1], d[1]);
-        split_cell(z, p.uh, p.ul, p.dims, c[2], d[2]);
-        int h[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-            h[a] = c[a] + 1 == p.dims ? 0 : c[a] + 1;
-        float g[8];
-#pragma unroll
-        for (int k = 0; k < 8; k++)
-            g[k] = __ldg(grid + cell_index(p.plane, p.row, (k & 1) ? h[0] : c[0],
-                                           (k & 2) ? h[1] : c[1], (k & 4) ? h[2] : c[2]));
-        const float t0 = 1.f - d[0], t1 = 1.f - d[1], t2 = 1.f - d[2];
-        // Interpolate along z first, then y, then x; derivatives from the same tree.
-        const float g00 = fmaf(d[2], g[4] - g[0], g[0]);  // (x0,y0)
-        const float g10 = fmaf(d[2], g[5] - g[1], g[1]);  // (x1,y0)
-        const float g01 = fmaf(d[2], g[6] - g[2], g[2]);  // (x0,y1)
-        const float g11 = fmaf(d[2], g[7] - g[3], g[3]);  // (x1,y1)
-        const float gx0 = fmaf(d[1], g01 - g00, g00);
-        const float gx1 = fmaf(d[1], g11 - g10, g10);
-        const float val = fmaf(d[0], gx1 - gx0, gx0);
-        const float dgx = gx1 - gx0;
-        const float gy0 = fmaf(d[0], g10 - g00, g00);
-        const float gy1 = fmaf(d[0], g11 - g01, g01);
-        const float dgy = gy1 - gy0;
-        // d/dz: bilinear in (x, y) of the z-differences.
-        const float e00 = g[4] - g[0], e10 = g[5] - g[1], e01 = g[6] - g[2], e11 = g[7] - g[3];
-        const float dgz = t0 * (t1 * e00 + d[1] * e01) + d[0] * (t1 * e10 + d[1] * e11);
-        (void)t2;
-        const float s = m * p.units;
-        gpos[3 * i] = s * dgx;
-        gpos[3 * i + 1] = s * dgy;
-        gpos[3 * i + 2] = s * dgz;
+        const GatherOut o = gather_one(p, grid, x, y, z, m);
+        gpos[3 * i] = o.gx;
+        gpos[3 * i + 1] = o.gy;
+        gpos[3 * i + 2] = o.gz;
         if (VARMASS)
-            gmass[i] = val + p.dl_dm;
+            gmass[i] = o.val + p.dl_dm;
     }
 }
 
@@ -147,7 +187,8 @@ cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, co
     p.nrbins = t.nrbins;
     p.bpu_half = (float)(0.5 * t.binsperunit);
     p.nmodes = (int64_t)g.dims * g.dims * g.hc;
-    const int blocks = (int)std::min<int64_t>((p.nmodes + 255) / 256, 152 * 16);
+    // one warp per row of kz modes; 4 CTAs of 8 warps per SM (46 registers)
+    const int blocks = (int)std::min<int64_t>(((int64_t)g.dims * g.dims + 7) / 8, 152 * 4);
     k_mode_gradient<<<blocks, 256, sizeof(uint32_t) * (t.nrbins + 1), stream>>>(p, spec, d.thr,
                                                                               d.iw, gcoef_dev);
     (*launches)++;

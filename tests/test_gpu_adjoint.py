@@ -104,6 +104,39 @@ def test_adjoint_device_pointers(gp):
     assert np.array_equal(d[1].cpu().numpy(), h[1])
 
 
+def test_adjoint_ragged_tile_and_unaligned_arrays(gp):
+    """A ragged particle count (not a multiple of 256 or 1024) through aligned
+    device arrays and through device arrays that start 12 bytes past a 16-byte
+    boundary: the same gradients bit for bit, and the FP64 reference
+    gradient."""
+    import torch
+    dims, box, nrbins, n = 32, 1000.0, 16, 3004
+    pos, masses = make_case("uniform", dims, box, 7, nrbins, True)
+    pos, masses = pos[:n].copy(), masses[:n].copy()
+    m = O.total_mass(n, masses)
+    g = np.linspace(-1.0, 1.0, nrbins) * 1e3
+    al = torch.from_numpy(pos).cuda()
+    am = torch.from_numpy(masses).cuda()
+    bp = torch.empty(3 * n + 3, dtype=torch.float32, device="cuda")
+    bp[3:] = al.reshape(-1)
+    bm = torch.empty(n + 3, dtype=torch.float32, device="cuda")
+    bm[3:] = am
+    gb = torch.empty(3 * n + 3, dtype=torch.float32, device="cuda")
+    gmb = torch.empty(n + 3, dtype=torch.float32, device="cuda")
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, masses)
+        ctx.power(0, 0, m, m)
+        a = ctx.adjoint(0, box, al, g, m, masses=am, recompute=True)
+        b = ctx.adjoint(0, box, bp[3:], g, m, masses=bm[3:], recompute=True,
+                        grad_pos=gb[3:], grad_mass=gmb[3:])
+    assert bp[3:].data_ptr() % 16 == 12
+    assert np.array_equal(a[0].cpu().numpy(), gb[3:].reshape(n, 3).cpu().numpy())
+    assert np.array_equal(a[1].cpu().numpy(), gmb[3:].cpu().numpy())
+    rpos, rmass, _ = O.reference_gradient(pos, box, dims, nrbins, g, masses, 0.0, m_norm=m)
+    grad_close(a[0].cpu().numpy(), rpos)
+    grad_close(a[1].cpu().numpy(), rmass)
+
+
 def test_adjoint_central_finite_differences_256_particles(gp):
     """Central differences (step 1e-3 cell) of the FP64 oracle loss on 256
     random particles against the GPU gradient."""
