@@ -589,6 +589,49 @@ int make_r2c(genpk_ctx *ctx, int batch, bool planes, cufftHandle *out)
     return GENPK_OK;
 }
 
+// The batched 2-D C2R over the x-planes (y and z), in place, that completes
+// the adjoint's inverse transform after its own x pass; kept in the plan map
+// under key 0 (the R2C plans use +-batch).
+int make_c2r_planes(genpk_ctx *ctx, cufftHandle *out)
+{
+    auto it = ctx->r2c.find(0);
+    if (it != ctx->r2c.end()) {
+        *out = it->second;
+        return GENPK_OK;
+    }
+    const long long n = ctx->dims;
+    long long dims2[2] = {n, n};
+    long long inembed[2] = {n, (long long)ctx->gg.hc};
+    long long onembed[2] = {n, (long long)ctx->gg.row};
+    cufftHandle h;
+    GENPK_CUFFT(cufftCreate(&h));
+    GENPK_CUFFT(cufftSetAutoAllocation(h, 0));
+    size_t ws = 0;
+    cufftResult r = cufftMakePlanMany64(h, 2, dims2, inembed, 1, n * ctx->gg.hc, onembed, 1,
+                                        n * ctx->gg.row, CUFFT_C2R, n, &ws);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(ctx, GENPK_ERR_CUFFT,
+                    "cufftMakePlanMany64 (c2r planes) failed: " + std::to_string((int)r));
+    }
+    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
+    if (ws > ctx->fft_work_size) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->fft_work);
+        ctx->fft_work = nullptr;
+        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
+        ctx->fft_work_size = ws;
+        for (auto &kv : ctx->r2c)
+            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
+        if (ctx->c2r_made)
+            GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
+    }
+    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    ctx->r2c[0] = h;
+    *out = h;
+    return GENPK_OK;
+}
+
 int make_c2r(genpk_ctx *ctx)
 {
     if (ctx->c2r_made)
@@ -1242,11 +1285,27 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     GENPK_CUDA(cudaMemcpyAsync(ctx->d_gcoef, gcoef.data(), sizeof(float) * nrb,
                                cudaMemcpyHostToDevice, ctx->stream));
     float *g = grid_of(ctx, field);
-    GENPK_CUDA(adjoint_mode_gradient_coef(ctx->gg, ctx->tables, ctx->bdev, (float2 *)g,
-                                          ctx->d_gcoef, ctx->stream, &ctx->launches));
-    stage_event(ctx, "adj_modes");
-    GENPK_TRY(make_c2r(ctx));
-    GENPK_CUFFT(cufftExecC2R(ctx->c2r, (cufftComplex *)g, (cufftReal *)g));
+    if (use_xfft(ctx)) {
+        // mode gradient fused into the inverse x pass, then the (y, z) C2R per x-plane
+        XfftGrad xg;
+        xg.nrbins = nrb;
+        xg.bpu_half = (float)(0.5 * ctx->tables.binsperunit);
+        xg.thr = ctx->bdev.thr;
+        xg.iw = ctx->bdev.iw;
+        xg.gcoef = ctx->d_gcoef;
+        GENPK_CUDA(xfft_grad_pass(ctx->gg, g, ctx->d_xtw, xg, ctx->num_sms, ctx->d_status,
+                                  ctx->stream, &ctx->launches));
+        stage_event(ctx, "adj_modes_x");
+        cufftHandle h;
+        GENPK_TRY(make_c2r_planes(ctx, &h));
+        GENPK_CUFFT(cufftExecC2R(h, (cufftComplex *)g, (cufftReal *)g));
+    } else {
+        GENPK_CUDA(adjoint_mode_gradient_coef(ctx->gg, ctx->tables, ctx->bdev, (float2 *)g,
+                                              ctx->d_gcoef, ctx->stream, &ctx->launches));
+        stage_event(ctx, "adj_modes");
+        GENPK_TRY(make_c2r(ctx));
+        GENPK_CUFFT(cufftExecC2R(ctx->c2r, (cufftComplex *)g, (cufftReal *)g));
+    }
     ctx->state[(size_t)field] = F_GRADIENT;
     ctx->auto_valid[(size_t)field] = false;
     stage_event(ctx, "adj_c2r");

@@ -178,8 +178,9 @@ bool build_bin_tables_into(int64_t dims, int nrbins, const TableSpans &o, double
 double ref_onedinvwindow(int64_t k, int64_t n);
 double ref_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
 
-// x-axis FFT pass with optional fused auto-spectrum binning (xfft.cu): the
-// grid's (z, y) transforms come from a batched 2-D cuFFT R2C over x-planes.
+// x-axis FFT pass with optional fused auto-spectrum binning (xfft.cu), after
+// the grid's (z, y) transforms (the own z and y passes, or a batched 2-D cuFFT
+// R2C over x-planes).
 struct XfftBin {
     int nrbins;
     float bpu_half;         // 0.5 * binsperunit (first-guess bin)
@@ -210,6 +211,21 @@ cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
                       const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
                       DeviceStatus *dstat, cudaStream_t stream, int64_t *launches);
+// The adjoint's first inverse pass (xfft.cu), for xfft_supported sizes: every
+// mode of the spectrum in `grid` is scaled by its bin's coefficient gcoef[b]
+// times V_m (the adjoint mode gradient), and the inverse (e^{+ikx})
+// transform along x follows in the same pass.  A batched 2-D C2R over the
+// x-planes then completes the unnormalised 3-D C2R.
+struct XfftGrad {
+    int nrbins;
+    float bpu_half;
+    const uint32_t *thr;
+    const float *iw;
+    const float *gcoef;  // [nrbins] G_b = 2 dL/dP_b / (M^2 C_b)
+};
+cudaError_t xfft_grad_pass(const GridGeom &g, float *grid, const float2 *tw, const XfftGrad &grad,
+                           int num_sms, DeviceStatus *dstat, cudaStream_t stream,
+                           int64_t *launches);
 
 struct BinDevice {
     uint32_t *thr = nullptr;   // [nrbins+1]

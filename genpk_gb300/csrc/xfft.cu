@@ -63,7 +63,15 @@ struct XParams {
     const float *iw;       // [dims]
     const double *corner;  // exact (N/2,N/2,N/2) value or null
     double *partial;       // [gridDim.x][nrbins]
+    const float *gcoef;    // adjoint: [nrbins] per-bin coefficients G_b
 };
+
+// What k_xfft does around its transform: the forward pass alone, the forward
+// pass binning its field's auto spectrum, or the adjoint's inverse pass, which
+// first scales every mode by the P(k) loss gradient (the mode gradient
+// H = G_b V_m c_m/mult_m F_m) and runs the inverse transform as
+// conj(FFT(conj(H))).
+constexpr int kXPlain = 0, kXBin = 1, kXGrad = 2;
 
 // This tile's share of a region cleared alongside the x pass: units
 // [t * per, (t + 1) * per) of the region's n 16-byte units, as streaming
@@ -336,6 +344,31 @@ __device__ __forceinline__ void fft_to_last(float2 *tile, const float2 *tw, int 
     stage_read<N, P::NSL, P::RL>(tile, tw, c, g, v);
 }
 
+// fft_to_last with every input value passed through f(row, value) as the
+// first stage (radix 8, span 1, no twiddles) reads it.
+template <int N, typename F>
+__device__ __forceinline__ void fft_to_last_in(float2 *tile, const float2 *tw, int c, int g,
+                                               float2 (&v)[8], F f)
+{
+    using P = FftPlan<N>;
+    static_assert(P::N8 >= 1, "the first stage is radix 8");
+    constexpr int TZ = kXTileBytes / 8 / N;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int row = g + r * (N / 8);
+        v[r] = f(row, tile[row * TZ + c]);
+    }
+    dft<8>(v);
+    __syncthreads();
+    stage_write<N, 1, 8>(tile, c, g, v);
+    __syncthreads();
+    if constexpr (P::N8 >= 2)
+        stage<N, 8>(tile, tw, c, g, v);
+    if constexpr (P::N8 >= 3)
+        stage<N, 64>(tile, tw, c, g, v);
+    stage_read<N, P::NSL, P::RL>(tile, tw, c, g, v);
+}
+
 __device__ __forceinline__ int kval_x(int i, int n)
 {
     return i <= n / 2 ? i : i - n;
@@ -377,10 +410,11 @@ __device__ __forceinline__ void last_write(float2 *tile, float *vals, const ColI
         }
 }
 
-template <int N, bool BIN>
+template <int N, int MODE>
 __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
     k_xfft(const __grid_constant__ CUtensorMap map, XParams p, DeviceStatus *st)
 {
+    constexpr bool BIN = MODE == kXBin, GRAD = MODE == kXGrad;
     constexpr int TZ = kXTileBytes / 8 / N;
     constexpr int BOX = N < 256 ? N : 256;
     constexpr int NBOX = N / BOX;
@@ -404,22 +438,28 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
     double *chist = reinterpret_cast<double *>(q);               // [nrbins]
     q += BIN ? sizeof(double) * p.nrbins : 0;
     uint32_t *thr = reinterpret_cast<uint32_t *>(q);             // [nrbins + 1]
+    q += (BIN || GRAD) ? sizeof(uint32_t) * (p.nrbins + 1) : 0;
+    float *gco = reinterpret_cast<float *>(q);                   // [nrbins] (GRAD)
     __shared__ __align__(8) unsigned long long bar[2];
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int c = tid % TZ, g = tid / TZ;  // FFT: column and butterfly group
     for (int i = tid; i < N; i += kXThreads) {
         tw_s[i] = p.tw[i];
-        iw_s[i] = BIN ? p.iw[i] : 0.f;
+        iw_s[i] = (BIN || GRAD) ? p.iw[i] : 0.f;
     }
     if (BIN) {
         for (int i = tid; i < (kXThreads / 32) * p.nrbins; i += kXThreads)
             whist[i] = 0.f;
         for (int i = tid; i < p.nrbins; i += kXThreads)
             chist[i] = 0.0;
+    }
+    if (BIN || GRAD)
         for (int i = tid; i <= p.nrbins; i += kXThreads)
             thr[i] = p.thr[i];
-    }
+    if (GRAD)
+        for (int i = tid; i < p.nrbins; i += kXThreads)
+            gco[i] = p.gcoef[i];
     if (tid == 0) {
         mbar_init(&bar[0]);
         mbar_init(&bar[1]);
@@ -460,7 +500,7 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
             issue(t + gridDim.x, buf ^ 1);
         }
         const int b = t / p.tiles_per_field, f0 = (t - b * p.tiles_per_field) * TZ;
-        if (BIN && tid < TZ) {
+        if ((BIN || GRAD) && tid < TZ) {
             const int f = f0 + tid;
             ColInfo ci;
             if (f < p.ncols) {
@@ -486,7 +526,33 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         __syncthreads();
 
         float2 v[8];
-        fft_to_last<N>(tile, tw_s, c, g, v);
+        if (GRAD) {
+            // H = G_b V_m F_m (c_m / mult_m = 1 for even N), conjugated on the
+            // way in; the same bins as the forward binning (thr, iw).
+            const ColInfo ci = cols2[(k & 1) * TZ + c];
+            auto scale = [&](int row, float2 x) -> float2 {
+                const int kx = kval_x(row, N);
+                const uint32_t kk2 = (uint32_t)(kx * kx) + (uint32_t)ci.r2;
+                if (ci.r2 < 0 || kk2 == 0)
+                    return make_float2(0.f, 0.f);
+                int bb = (int)(p.bpu_half * __logf((float)kk2));
+                bb = max(0, min(p.nrbins - 1, bb));
+                while (bb + 1 < p.nrbins && kk2 >= thr[bb + 1])
+                    bb++;
+                while (bb > 0 && kk2 < thr[bb])
+                    bb--;
+                const float pz = (iw_s[row] * ci.iwj) * ci.iwz;
+                const float p2 = pz * pz;
+                const float s = gco[bb] * (p2 * p2);
+                return make_float2(s * x.x, -(s * x.y));
+            };
+            fft_to_last_in<N>(tile, tw_s, c, g, v, scale);
+#pragma unroll
+            for (int r = 0; r < 8; r++)
+                v[r].y = -v[r].y;
+        } else {
+            fft_to_last<N>(tile, tw_s, c, g, v);
+        }
         __syncthreads();
         const ColInfo *cols = cols2 + (k & 1) * TZ;
         const ColInfo ci = BIN ? cols[c] : ColInfo{};
@@ -842,17 +908,21 @@ int xfft_tz(int dims)
     return kXTileBytes / 8 / dims;
 }
 
-size_t xfft_smem(int dims, int nrbins)
+size_t xfft_smem(int dims, int nrbins, int mode)
 {
     const int tz = xfft_tz(dims);
     size_t s = 2 * (size_t)kXTileBytes + sizeof(float2) * dims + sizeof(float) * dims +
                sizeof(ColInfo) * 2 * tz;
-    if (nrbins > 0) {
+    if (mode == kXBin) {
         s += sizeof(float) * tz * (dims + 1);
         s = (s + 15) & ~(size_t)15;
         s += sizeof(float) * (kXThreads / 32) * nrbins;
         s = (s + 15) & ~(size_t)15;
         s += sizeof(double) * nrbins + sizeof(uint32_t) * (nrbins + 1);
+    } else if (mode == kXGrad) {
+        s = (s + 15) & ~(size_t)15;
+        s = (s + 15) & ~(size_t)15;
+        s += sizeof(uint32_t) * (nrbins + 1) + sizeof(float) * nrbins;
     }
     return s;
 }
@@ -869,7 +939,7 @@ bool xfft_supported(int dims)
 bool xfft_bin_supported(int dims, int nrbins)
 {
     return xfft_supported(dims) && nrbins >= 1 && nrbins <= kXMaxBins &&
-           xfft_smem(dims, nrbins) <= 227 * 1024;
+           xfft_smem(dims, nrbins, kXBin) <= 227 * 1024;
 }
 
 void xfft_twiddles(int dims, std::vector<float> *out)
@@ -883,9 +953,11 @@ void xfft_twiddles(int dims, std::vector<float> *out)
     }
 }
 
-cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
-                      const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
-                      DeviceStatus *dstat, cudaStream_t stream, int64_t *launches)
+namespace {
+
+cudaError_t launch_xfft(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int mode,
+                        const XfftBin *bin, const XfftGrad *grad, void *zero, int64_t zero_bytes,
+                        int num_sms, DeviceStatus *dstat, cudaStream_t stream, int64_t *launches)
 {
     EncodeTiledFn enc = encode_fn();
     if (!enc)
@@ -907,12 +979,13 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
     p.ntiles = p.tiles_per_field * nbatch;
     p.box_rows = std::min(n, 256);
     p.tw = tw;
-    p.nrbins = bin ? bin->nrbins : 0;
-    p.bpu_half = bin ? bin->bpu_half : 0.f;
-    p.thr = bin ? bin->thr : nullptr;
-    p.iw = bin ? bin->iw : nullptr;
+    p.nrbins = bin ? bin->nrbins : grad ? grad->nrbins : 0;
+    p.bpu_half = bin ? bin->bpu_half : grad ? grad->bpu_half : 0.f;
+    p.thr = bin ? bin->thr : grad ? grad->thr : nullptr;
+    p.iw = bin ? bin->iw : grad ? grad->iw : nullptr;
     p.corner = bin ? bin->corner : nullptr;
     p.partial = bin ? bin->partial : nullptr;
+    p.gcoef = grad ? grad->gcoef : nullptr;
     p.zero = zero_bytes > 0 ? static_cast<uint4 *>(zero) : nullptr;
     p.zero_units = zero_bytes / 16;
     p.zero_per_tile = (p.zero_units + p.ntiles - 1) / p.ntiles;
@@ -927,11 +1000,12 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     const int ctas = std::min(p.ntiles, num_sms * kXCtasPerSm);
-    const size_t smem = xfft_smem(n, p.nrbins);
+    const size_t smem = xfft_smem(n, p.nrbins, mode);
     void (*kern)(const CUtensorMap, XParams, DeviceStatus *) = nullptr;
-#define GENPK_XFFT_PICK(NN)                                   \
-    case NN:                                                  \
-        kern = bin ? k_xfft<NN, true> : k_xfft<NN, false>;    \
+#define GENPK_XFFT_PICK(NN)                                                           \
+    case NN:                                                                          \
+        kern = mode == kXBin ? k_xfft<NN, kXBin>                                      \
+                             : mode == kXGrad ? k_xfft<NN, kXGrad> : k_xfft<NN, kXPlain>; \
         break;
     switch (n) {
         GENPK_XFFT_PICK(64)
@@ -950,6 +1024,24 @@ cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
     kern<<<ctas, kXThreads, smem, stream>>>(map, p, dstat);
     (*launches)++;
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
+                      const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
+                      DeviceStatus *dstat, cudaStream_t stream, int64_t *launches)
+{
+    return launch_xfft(g, grids, nbatch, tw, bin ? kXBin : kXPlain, bin, nullptr, zero,
+                       zero_bytes, num_sms, dstat, stream, launches);
+}
+
+cudaError_t xfft_grad_pass(const GridGeom &g, float *grid, const float2 *tw, const XfftGrad &grad,
+                           int num_sms, DeviceStatus *dstat, cudaStream_t stream,
+                           int64_t *launches)
+{
+    return launch_xfft(g, grid, 1, tw, kXGrad, nullptr, &grad, nullptr, 0, num_sms, dstat, stream,
+                       launches);
 }
 
 cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *acc,

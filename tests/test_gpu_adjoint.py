@@ -50,8 +50,11 @@ def make_case(kind, dims, box, seed, nrbins, var):
 
 
 @pytest.mark.parametrize("kind,dims,var", [("uniform", 32, False), ("zeldovich", 32, True),
-                                           ("zeldovich", 64, False), ("uniform", 48, True)])
+                                           ("zeldovich", 64, False), ("uniform", 48, True),
+                                           ("uniform", 64, True), ("zeldovich", 128, True)])
 def test_adjoint_matches_fp64_reference_gradient(gp, kind, dims, var):
+    """Grids of 64 to 512 cells (powers of two) take the fused inverse x pass
+    + 2-D C2R; the others the mode-gradient kernel + 3-D C2R."""
     box, nrbins, mass = 1000.0, 24, 1.0
     pos, masses = make_case(kind, dims, box, 3, nrbins, var)
     tgt_pos, _ = make_case(kind, dims, box, 4, nrbins, False)
