@@ -504,6 +504,26 @@ def main():
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
             "deposit_engine": engine}
 
+    # end to end through the C ABI from pinned host memory (before the adjoint
+    # section: after it, the host-link reads of a newly pinned buffer were
+    # sometimes slower, 14-23 ms against 9.0 ms per step)
+    if not args.no_e2e:
+        hpos = dpos.cpu().pin_memory()
+        for _ in range(2):
+            step(hpos)
+        torch.cuda.synchronize()
+        e2e_t = []
+        for _ in range(max(3, min(args.steps, 20))):
+            t1 = time.perf_counter()
+            step(hpos)
+            e2e_t.append(time.perf_counter() - t1)
+        e = float(np.mean(e2e_t))
+        line["e2e"] = {"value": npart * world / e, "unit": "particles/s",
+                       "h2d_bytes_per_step": npart * 12, "d2h_bytes_per_step": nrbins * 8,
+                       "ms_per_step": e * 1e3, "ms_min": min(e2e_t) * 1e3,
+                       "ms_max": max(e2e_t) * 1e3}
+        del hpos
+
     # forward + adjoint / forward
     if not args.no_adjoint:
         g = np.linspace(1.0, -1.0, nrbins) / np.maximum(np.abs(p), 1e-30)
@@ -530,23 +550,6 @@ def main():
         line["adjoint_ms"] = float(np.mean(adj))
         line["adjoint_stages_ms"] = {k: round(v, 5) for k, v in adj_st.items()}
         del gpos
-
-    # end to end through the C ABI from pinned host memory
-    if not args.no_e2e:
-        hpos = dpos.cpu().pin_memory()
-        for _ in range(2):
-            step(hpos)
-        torch.cuda.synchronize()
-        e2e_t = []
-        for _ in range(max(3, min(args.steps, 20))):
-            t1 = time.perf_counter()
-            step(hpos)
-            e2e_t.append(time.perf_counter() - t1)
-        e = float(np.mean(e2e_t))
-        line["e2e"] = {"value": npart * world / e, "unit": "particles/s",
-                       "h2d_bytes_per_step": npart * 12, "d2h_bytes_per_step": nrbins * 8,
-                       "ms_per_step": e * 1e3}
-        del hpos
 
     # FP64 oracle on the same particles (rank 0): parity at full size + CPU baseline
     if rank == 0 and not args.no_cpu:
