@@ -529,7 +529,7 @@ def main():
         g = np.linspace(1.0, -1.0, nrbins) / np.maximum(np.abs(p), 1e-30)
         gpos = torch.empty((npart, 3), device="cuda", dtype=torch.float32)
         fwd, adj, adj_rc = [], [], []
-        adj_st = {}
+        adj_st, rc_st = {}, {}
         for it in range(4):
             _, _, st = step(dpos)
             ctx.timing_reset()
@@ -544,11 +544,14 @@ def main():
                 adj_rc.append(sum(sr.values()))
                 for key, v in sa.items():
                     adj_st[key] = adj_st.get(key, 0.0) + v / 3
+                for key, v in sr.items():
+                    rc_st[key] = rc_st.get(key, 0.0) + v / 3
         f_ms = float(np.mean(fwd))
         line["fwd_adj_ratio"] = (f_ms + float(np.mean(adj))) / f_ms
         line["fwd_adj_recompute_ratio"] = (f_ms + float(np.mean(adj_rc))) / f_ms
         line["adjoint_ms"] = float(np.mean(adj))
         line["adjoint_stages_ms"] = {k: round(v, 5) for k, v in adj_st.items()}
+        line["adjoint_recompute_stages_ms"] = {k: round(v, 5) for k, v in rc_st.items()}
         del gpos
 
     # FP64 oracle on the same particles (rank 0): parity at full size + CPU baseline

@@ -212,6 +212,10 @@ cudaError_t adjoint_gather(const GridGeom &g, float units_hi, float units_lo, co
     p.mass = mass;
     p.dl_dm = dl_dmass_norm;
     p.n = n;
+    // Four CTAs per resident slot (8 per SM at 32-36 registers).  Sizing the
+    // grid to the resident CTAs, so that the stride sweeps the particles in
+    // order, cut the DRAM reads at 512^3 from 2.85 to 2.56 GB (2.15 GB of
+    // positions and grid) but took 1.00 ms against 0.92.
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
     if (masses)
         k_gather<true><<<blocks, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);
