@@ -1285,7 +1285,7 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     GENPK_CUDA(cudaMemcpyAsync(ctx->d_gcoef, gcoef.data(), sizeof(float) * nrb,
                                cudaMemcpyHostToDevice, ctx->stream));
     float *g = grid_of(ctx, field);
-    if (use_xfft(ctx)) {
+    if (use_xfft(ctx) && xfft_grad_supported((int)ctx->dims, nrb)) {
         // mode gradient fused into the inverse x pass, then the (y, z) C2R per x-plane
         XfftGrad xg;
         xg.nrbins = nrb;

@@ -223,6 +223,7 @@ struct XfftGrad {
     const float *iw;
     const float *gcoef;  // [nrbins] G_b = 2 dL/dP_b / (M^2 C_b)
 };
+bool xfft_grad_supported(int dims, int nrbins);  // its bin tables fit in shared memory
 cudaError_t xfft_grad_pass(const GridGeom &g, float *grid, const float2 *tw, const XfftGrad &grad,
                            int num_sms, DeviceStatus *dstat, cudaStream_t stream,
                            int64_t *launches);

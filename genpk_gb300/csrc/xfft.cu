@@ -936,6 +936,11 @@ bool xfft_supported(int dims)
     return dims >= 64 && dims <= 512 && (dims & (dims - 1)) == 0 && encode_fn() != nullptr;
 }
 
+bool xfft_grad_supported(int dims, int nrbins)
+{
+    return xfft_supported(dims) && nrbins >= 1 && xfft_smem(dims, nrbins, kXGrad) <= 227 * 1024;
+}
+
 bool xfft_bin_supported(int dims, int nrbins)
 {
     return xfft_supported(dims) && nrbins >= 1 && nrbins <= kXMaxBins &&

@@ -73,6 +73,26 @@ def test_adjoint_matches_fp64_reference_gradient(gp, kind, dims, var):
     assert abs(dldm - rdldm) <= G_RTOL * abs(rdldm) + 1e-300
 
 
+def test_adjoint_many_bins(gp):
+    """More bins than the fused forward binning takes (300 > 256): the forward
+    spectrum is binned by the separate kernel, the adjoint's fused inverse x
+    pass still holds its 300 thresholds and coefficients in shared memory."""
+    dims, box, nrbins = 64, 1000.0, 300
+    pos, _ = make_case("zeldovich", dims, box, 11, nrbins, False)
+    tgt, _ = make_case("zeldovich", dims, box, 12, nrbins, False)
+    m = O.total_mass(len(pos), None, 1.0)
+    target, cnt, _ = O.pk(tgt, box, dims, nrbins, None, 1.0)
+    target = np.where(cnt > 0, target, 1.0)
+    with gp.Context(dims, nrbins) as ctx:
+        ctx.deposit(0, box, pos, None, 1.0)
+        p, c, _ = ctx.power(0, 0, m, m)
+        _, g = loss_grad(p, target, c)
+        gpos, _, dldm = ctx.adjoint(0, box, pos, g, m, mass=1.0)
+    rpos, _, rdldm = O.reference_gradient(pos, box, dims, nrbins, g, None, 1.0, m_norm=m)
+    grad_close(gpos, rpos)
+    assert abs(dldm - rdldm) <= G_RTOL * abs(rdldm) + 1e-300
+
+
 def test_adjoint_recompute_equals_stored_spectrum(gp):
     dims, box, nrbins = 32, 100.0, 16
     pos, masses = make_case("zeldovich", dims, box, 9, nrbins, True)
