@@ -1,0 +1,71 @@
+"""The bench's multi-rank path on CPU (gloo, world size 2): the slowest rank's
+time is the job's, the throughput counts every rank's box, and under torchrun
+the reference arm runs on rank 0 alone while the other ranks exit cleanly.
+The GPU arm's ranks are independent replicas with no collective on the data
+path; these tests cover the host logic around them."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    slowest = bench.max_over_ranks(2.0 + 3.0 * rank, world, device="cpu")
+    value = bench.job_throughput(1000, world, slowest)
+    with open(os.path.join(out_dir, f"r{rank}.json"), "w") as f:
+        json.dump({"slowest": slowest, "value": value}, f)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_job_throughput_gloo(tmp_path):
+    import torch.multiprocessing as mp
+    world, port = 2, free_port()
+    mp.start_processes(_rank_main, args=(world, port, str(tmp_path)), nprocs=world,
+                       start_method="spawn", join=True)
+    for r in range(world):
+        d = json.loads((tmp_path / f"r{r}.json").read_text())
+        assert d["slowest"] == 5.0                      # rank 1's 5 ms
+        assert d["value"] == pytest.approx(2 * 1000 / 5e-3)
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(3.5, 1) == 3.5
+    assert bench.job_throughput(10, 1, 2.0) == pytest.approx(5000.0)
+
+
+def test_reference_arm_under_torchrun_two_ranks(tmp_path):
+    """`--impl reference` launched as the multi-GPU bench is: rank 0 prints one
+    JSON line, the other rank exits 0 without output."""
+    env = dict(os.environ, OMP_NUM_THREADS="2", CUDA_VISIBLE_DEVICES="")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", f"--master-port={free_port()}",
+           os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+           "--steps", "1", "--warmup", "0", "--nside", "32", "--grid", "32",
+           "--box", "1000"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=str(tmp_path),
+                       env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "particles/s" and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
