@@ -39,8 +39,25 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <mutex>
+#include <unordered_map>
 
 namespace genpk {
+
+cudaError_t ensure_dynamic_smem(const void *func, size_t bytes)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void *, size_t> limit;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limit[func];
+    if (bytes <= cur)
+        return cudaSuccess;
+    const cudaError_t err =
+        cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err == cudaSuccess)
+        cur = bytes;
+    return err;
+}
 
 GridGeom make_grid_geom(int dims)
 {
@@ -725,8 +742,7 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
 #define GENPK_TILE_LAUNCH(V, C)                                                                \
     do {                                                                                       \
         auto kern = k_tile_deposit<TX, TY, TZ, V, C>;                                          \
-        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
-                                   (int)smem);                                                 \
+        err = ensure_dynamic_smem(kern, smem);                                                 \
         if (err != cudaSuccess)                                                                \
             return err;                                                                        \
         kern<<<g.ntiles, kTileThreads, smem, stream>>>(tp, s.sorted, s.tile_start, dstat,      \
@@ -846,9 +862,7 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     const int tb = 256, tgrid = (g.ntiles + tb - 1) / tb;
     const size_t hsmem = deposit_hist_smem(g);
     if (shared_hist) {
-        if ((err = cudaFuncSetAttribute(k_sort_hist<false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)hsmem)) != cudaSuccess)
+        if ((err = ensure_dynamic_smem(k_sort_hist<false>, hsmem)) != cudaSuccess)
             return err;
         k_sort_hist<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.mass_part,
                                                                        dstat);
@@ -872,9 +886,7 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     if (shared_hist) {
         k_sort_offsets<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.tile_start);
         mark("dep_offsets");
-        if ((err = cudaFuncSetAttribute(k_sort_scatter<false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)hsmem)) != cudaSuccess)
+        if ((err = ensure_dynamic_smem(k_sort_scatter<false>, hsmem)) != cudaSuccess)
             return err;
         k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted,
                                                                          dstat);

@@ -1054,8 +1054,7 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
                                         : k_stream_deposit<true, false, true>)
                             : (p.corner ? k_stream_deposit<false, true, true>
                                         : k_stream_deposit<false, false, true>);
-        if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        smem)) != cudaSuccess)
+        if ((err = ensure_dynamic_smem(kern, (size_t)smem)) != cudaSuccess)
             return err;
         kern<<<ctas, kWinThreads, smem, stream>>>(p, dstat, acc);
         mark(stream_mode ? "stream_deposit" : "win_deposit");

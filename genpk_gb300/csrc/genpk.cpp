@@ -109,7 +109,8 @@ struct genpk_ctx {
         double boxsize = 0.0;
         int engine = 0, chunk = 0;
     };
-    Choice choices[8];
+    static constexpr int kChoices = 32;  // species of a loop, or a batch of boxes per grid size
+    Choice choices[kChoices];
     int choice_next = 0;
     size_t probe_cap = 0;
 
@@ -390,7 +391,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     if (ctx->engine == GENPK_ENGINE_AUTO && !reuse) {
         if (pos != ctx->stage_pos) {
             genpk_ctx::Choice &c = ctx->choices[ctx->choice_next];
-            ctx->choice_next = (ctx->choice_next + 1) % 8;
+            ctx->choice_next = (ctx->choice_next + 1) % genpk_ctx::kChoices;
             c.pos = pos;
             c.masses = masses;
             c.n = n;

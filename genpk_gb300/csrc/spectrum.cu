@@ -440,8 +440,7 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
 #define GENPK_BIN_LAUNCH(NF, CROSS1)                                                          \
     do {                                                                                      \
         auto kern = k_bin<NF, CROSS1>;                                                        \
-        if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
-                                        (int)smem)) != cudaSuccess)                           \
+        if ((err = ensure_dynamic_smem(kern, smem)) != cudaSuccess)                           \
             return err;                                                                       \
         kern<<<ctas, 32 * warps, smem, stream>>>(p, d.thr, d.iw, partial);                    \
     } while (0)

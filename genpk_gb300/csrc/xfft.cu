@@ -1023,8 +1023,7 @@ cudaError_t launch_xfft(const GridGeom &g, float *grids, int nbatch, const float
     }
 #undef GENPK_XFFT_PICK
     cudaError_t err;
-    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem)) != cudaSuccess)
+    if ((err = ensure_dynamic_smem(kern, smem)) != cudaSuccess)
         return err;
     kern<<<ctas, kXThreads, smem, stream>>>(map, p, dstat);
     (*launches)++;
@@ -1077,8 +1076,7 @@ cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *
         return cudaErrorNotSupported;
     }
     cudaError_t err;
-    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, pre)) !=
-        cudaSuccess)
+    if ((err = ensure_dynamic_smem(kern, (size_t)pre)) != cudaSuccess)
         return err;
     kern<<<ctas, kZThreads, pre, stream>>>(acc, grid, nrows, g.row, tw, dstat);
     (*launches)++;
@@ -1112,8 +1110,7 @@ cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
         return cudaErrorNotSupported;
     }
     cudaError_t err;
-    if ((err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem)) != cudaSuccess)
+    if ((err = ensure_dynamic_smem(kern, smem)) != cudaSuccess)
         return err;
     kern<<<ctas, kXThreads, smem, stream>>>(reinterpret_cast<float2 *>(grids), g.hc, per_plane,
                                             ntiles, tw);

@@ -34,7 +34,10 @@
  *    genpk_power on that context.
  *  - Output arrays of genpk_power* and genpk_adjoint are host memory unless a
  *    function says otherwise.  Results are complete when the call returns.
- *  - One context per host thread; a context is not thread-safe.
+ *  - One context per host thread; a context is not thread-safe.  Different
+ *    contexts may be used from different host threads at the same time (each
+ *    has its own stream): their work overlaps on the GPU and the results equal
+ *    those of the contexts run one at a time.
  */
 #ifndef GENPK_GB300_H
 #define GENPK_GB300_H

@@ -670,6 +670,50 @@ def test_accumulator_cleared_by_the_transform(gp, engine):
     bins_close(got[0], pr, cr)
 
 
+def test_contexts_on_concurrent_host_threads(gp):
+    """Contexts used from several host threads at once (one stream each), with
+    different grid sizes, so that kernels with size-dependent shared memory
+    launch concurrently: every spectrum equals the same context's result run
+    alone, bit for bit."""
+    import threading
+    import torch
+    from genpk_gb300 import synth
+    box, nrbins = 1000.0, 24
+    jobs = [(64, torch.from_numpy(synth.uniform(300_000, box, seed=40)).cuda()),
+            (128, torch.from_numpy(synth.uniform(1_500_000, box, seed=41)).cuda()),
+            (128, torch.from_numpy(synth.zeldovich(128, box, seed=42)).cuda()),
+            (256, torch.from_numpy(synth.zeldovich(128, box, seed=43)).cuda()),
+            (64, torch.from_numpy(synth.zeldovich(64, box, seed=44)).cuda()),
+            (256, torch.from_numpy(synth.uniform(2_000_000, box, seed=45)).cuda())]
+
+    def run(ctx, pos, reps, out, i):
+        m = O.total_mass(len(pos), None, 1.0)
+        for _ in range(reps):
+            ctx.zero(0)
+            ctx.deposit(0, box, pos, None, 1.0)
+            out[i] = ctx.power(0, 0, m, m)
+
+    ctxs = [gp.Context(n, nrbins) for n, _ in jobs]
+    try:
+        alone = [None] * len(jobs)
+        for i, (c, (_, pos)) in enumerate(zip(ctxs, jobs)):
+            run(c, pos, 1, alone, i)
+        together = [None] * len(jobs)
+        ths = [threading.Thread(target=run, args=(c, pos, 5, together, i))
+               for i, (c, (_, pos)) in enumerate(zip(ctxs, jobs))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+    finally:
+        for c in ctxs:
+            c.close()
+    for a, b in zip(alone, together):
+        assert b is not None
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
 def test_cross_and_multi_spectra(gp):
     from genpk_gb300 import synth
     dims, box, nrbins = 64, 1000.0, 24
