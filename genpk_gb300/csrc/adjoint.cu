@@ -9,7 +9,9 @@
 // G_b = 2 g_b / (M^2 C_b) and mult_m the c2r multiplicity of the mode (1 on the
 // self-conjugate kz = 0 and, for even N, kz = N/2 planes, 2 elsewhere).  The
 // position and mass gradients are then the CIC gather (transpose of the
-// deposit) of dL/drho.
+// deposit) of dL/drho.  For N = 64..512 (powers of two) the mode gradient is
+// applied inside the inverse x pass instead (xfft.cu, k_xfft<N, kXGrad>);
+// k_mode_gradient here serves the other sizes.
 #include "common.cuh"
 #include "internal.h"
 
@@ -27,7 +29,6 @@ struct ModeGradParams {
     int dims, hc, half;
     int nrbins;
     float bpu_half;
-    int64_t nmodes;
 };
 
 // One warp per (x, y) row of the half-complex spectrum: kx, ky, iw(kx) iw(ky)
@@ -186,7 +187,6 @@ cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, co
     p.half = g.half;
     p.nrbins = t.nrbins;
     p.bpu_half = (float)(0.5 * t.binsperunit);
-    p.nmodes = (int64_t)g.dims * g.dims * g.hc;
     // one warp per row of kz modes; 4 CTAs of 8 warps per SM (46 registers)
     const int blocks = (int)std::min<int64_t>(((int64_t)g.dims * g.dims + 7) / 8, 152 * 4);
     k_mode_gradient<<<blocks, 256, sizeof(uint32_t) * (t.nrbins + 1), stream>>>(p, spec, d.thr,
