@@ -39,21 +39,26 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <map>
 #include <mutex>
-#include <unordered_map>
+#include <utility>
 
 namespace genpk {
 
 cudaError_t ensure_dynamic_smem(const void *func, size_t bytes)
 {
+    // the limit is kept per device (a process may drive several GPUs)
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess)
+        return err;
     static std::mutex mu;
-    static std::unordered_map<const void *, size_t> limit;
+    static std::map<std::pair<int, const void *>, size_t> limit;
     std::lock_guard<std::mutex> lock(mu);
-    size_t &cur = limit[func];
+    size_t &cur = limit[std::make_pair(dev, func)];
     if (bytes <= cur)
         return cudaSuccess;
-    const cudaError_t err =
-        cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    err = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (err == cudaSuccess)
         cur = bytes;
     return err;

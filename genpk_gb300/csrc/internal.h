@@ -25,10 +25,11 @@ struct GridGeom {
 
 GridGeom make_grid_geom(int dims);
 
-// Raise `func`'s dynamic shared-memory limit to at least `bytes` (never lower
-// it).  The limit is per kernel for the whole process, so contexts used from
-// several host threads would otherwise race: one lowering it between another's
-// set and launch fails that launch.  Serialised by a process-wide mutex.
+// Raise `func`'s dynamic shared-memory limit on the current device to at
+// least `bytes` (never lower it).  The limit is per kernel and device for the
+// whole process, so contexts used from several host threads would otherwise
+// race: one lowering it between another's set and launch fails that launch.
+// Serialised by a process-wide mutex.
 cudaError_t ensure_dynamic_smem(const void *func, size_t bytes);
 template <typename F>
 inline cudaError_t ensure_dynamic_smem(F *func, size_t bytes)
