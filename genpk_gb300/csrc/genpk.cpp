@@ -443,10 +443,12 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         // A clean grid headed for the own z/y/x transform keeps the pass in the
         // accumulator: the z pass converts it on the fly.
         const bool defer = a.clean && use_xfft(ctx);
-        GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
-                                       mass_ctas, s.win_acc, ctx->acc_zero, defer, ctx->num_sms,
-                                       ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
+        // (a pass that fails part-way must not leave the accumulator marked clear)
+        const bool acc_zero = ctx->acc_zero;
         ctx->acc_zero = false;
+        GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
+                                       mass_ctas, s.win_acc, acc_zero, defer, ctx->num_sms,
+                                       ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
         ctx->acc_spent = !defer;  // converted in the pass
         if (defer)
             ctx->acc_pending = f;
