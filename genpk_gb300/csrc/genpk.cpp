@@ -543,6 +543,32 @@ int ensure_stage(genpk_ctx *ctx, int64_t need)
 
 // planes: a batched 2-D R2C over every x-plane of `batch` consecutive grids
 // (the x-axis pass then runs in xfft.cu); else the full 3-D R2C.
+// The common tail of a new cuFFT plan: failure reported (the plan destroyed),
+// the context's stream set, and the one work area that every plan shares grown
+// to the new plan's need (every existing plan then points at the new area).
+int finish_plan(genpk_ctx *ctx, cufftHandle h, cufftResult made, size_t ws, const char *what)
+{
+    if (made != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return fail(ctx, GENPK_ERR_CUFFT, std::string("cufftMakePlanMany64 (") + what +
+                                              ") failed: " + std::to_string((int)made));
+    }
+    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
+    if (ws > ctx->fft_work_size) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->fft_work);
+        ctx->fft_work = nullptr;
+        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
+        ctx->fft_work_size = ws;
+        for (auto &kv : ctx->r2c)
+            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
+        if (ctx->c2r_made)
+            GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
+    }
+    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    return GENPK_OK;
+}
+
 int make_r2c(genpk_ctx *ctx, int batch, bool planes, cufftHandle *out)
 {
     const int key = planes ? -batch : batch;
@@ -570,23 +596,7 @@ int make_r2c(genpk_ctx *ctx, int batch, bool planes, cufftHandle *out)
         r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat, onembed, 1,
                                 (long long)ctx->gg.nfloat / 2, CUFFT_R2C, batch, &ws);
     }
-    if (r != CUFFT_SUCCESS) {
-        cufftDestroy(h);
-        return fail(ctx, GENPK_ERR_CUFFT, "cufftMakePlanMany64 (r2c) failed: " + std::to_string((int)r));
-    }
-    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
-    if (ws > ctx->fft_work_size) {
-        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->fft_work);
-        ctx->fft_work = nullptr;
-        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
-        ctx->fft_work_size = ws;
-        for (auto &kv : ctx->r2c)
-            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
-        if (ctx->c2r_made)
-            GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
-    }
-    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    GENPK_TRY(finish_plan(ctx, h, r, ws, "r2c"));
     ctx->r2c[key] = h;
     *out = h;
     return GENPK_OK;
@@ -612,24 +622,7 @@ int make_c2r_planes(genpk_ctx *ctx, cufftHandle *out)
     size_t ws = 0;
     cufftResult r = cufftMakePlanMany64(h, 2, dims2, inembed, 1, n * ctx->gg.hc, onembed, 1,
                                         n * ctx->gg.row, CUFFT_C2R, n, &ws);
-    if (r != CUFFT_SUCCESS) {
-        cufftDestroy(h);
-        return fail(ctx, GENPK_ERR_CUFFT,
-                    "cufftMakePlanMany64 (c2r planes) failed: " + std::to_string((int)r));
-    }
-    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
-    if (ws > ctx->fft_work_size) {
-        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->fft_work);
-        ctx->fft_work = nullptr;
-        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
-        ctx->fft_work_size = ws;
-        for (auto &kv : ctx->r2c)
-            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
-        if (ctx->c2r_made)
-            GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
-    }
-    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    GENPK_TRY(finish_plan(ctx, h, r, ws, "c2r planes"));
     ctx->r2c[0] = h;
     *out = h;
     return GENPK_OK;
@@ -649,21 +642,7 @@ int make_c2r(genpk_ctx *ctx)
     size_t ws = 0;
     cufftResult r = cufftMakePlanMany64(h, 3, dims3, inembed, 1, (long long)ctx->gg.nfloat / 2,
                                         onembed, 1, (long long)ctx->gg.nfloat, CUFFT_C2R, 1, &ws);
-    if (r != CUFFT_SUCCESS) {
-        cufftDestroy(h);
-        return fail(ctx, GENPK_ERR_CUFFT, "cufftMakePlanMany64 (c2r) failed: " + std::to_string((int)r));
-    }
-    GENPK_CUFFT(cufftSetStream(h, ctx->stream));
-    if (ws > ctx->fft_work_size) {
-        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->fft_work);
-        ctx->fft_work = nullptr;
-        GENPK_CUDA(cudaMalloc(&ctx->fft_work, ws));
-        ctx->fft_work_size = ws;
-        for (auto &kv : ctx->r2c)
-            GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
-    }
-    GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
+    GENPK_TRY(finish_plan(ctx, h, r, ws, "c2r"));
     ctx->c2r = h;
     ctx->c2r_made = true;
     return GENPK_OK;
