@@ -1,12 +1,21 @@
-// xfft.cu -- the last (x-axis) pass of the forward 3-D FFT, fused with the
-// auto-spectrum binning (the GPU counterpart of the last FFTW pass of
-// gen-pk.cpp:186-193,233 followed by powerspectrum.c:35-111).
+// xfft.cu -- the forward 3-D r2c FFT for N = 64..512 (powers of two) as three
+// passes of our own (the GPU counterpart of the FFTW plan of
+// gen-pk.cpp:186-193,233), the last one fused with the auto-spectrum binning of
+// powerspectrum.c:35-111, and the adjoint's first inverse pass.
 //
-// The grid's (z, y) transforms are one batched 2-D cuFFT R2C per x-plane; this
-// kernel does the remaining length-N complex DFT along x for every (j, kz)
-// column, writes the spectrum back in place (the layout cuFFT's 3-D R2C
-// produces), and optionally bins |F|^2 for the auto spectrum in the same pass,
-// so the spectrum is read from HBM once instead of twice.
+//   k_zfft    the r2c along z of one freshly deposited field, read straight
+//             from the deposit's 64-bit accumulator (one warp per row);
+//   k_yfft    the complex pass along y (cp.async tiles, Stockham stages);
+//   k_xfft    the complex pass along x for every (j, kz) column, in place (the
+//             layout cuFFT's 3-D R2C produces).  It runs after k_zfft + k_yfft
+//             or after a batched 2-D cuFFT R2C over the x-planes (fields that
+//             were converted first).  Modes: plain; binning |F|^2 of the auto
+//             spectrum in the same pass, so the spectrum is read from HBM once
+//             instead of twice, and clearing the used accumulator with spare
+//             bandwidth; or the adjoint's inverse pass with the mode gradient
+//             applied as the first stage reads each mode.
+//
+// k_xfft:
 //
 //   tiles     TZ = 4096/N consecutive columns f = j*(N/2+1) + kz (a 32 KB
 //             tile of N rows x TZ complex), moved by TMA (cp.async.bulk.tensor
