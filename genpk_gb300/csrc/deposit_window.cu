@@ -37,8 +37,11 @@
 // and the pass accumulator (64-bit) are integers of 2^-s mass units (the
 // sorted engine's weights, common.cuh pair_w / z_mass / corner_w);
 // k_window_convert subtracts the fixed-point pass mean and rounds each cell
-// once to FP32.  The grid is therefore bit-identical to the sorted engine's,
-// in either mode, and independent of summation order.
+// once to FP32 (or the forward transform's z pass does the same as it reads
+// the accumulator, xfft.cu k_zfft).  The grid is therefore bit-identical to
+// the sorted engine's, in either mode, and independent of summation order.
+// The accumulator is zeroed before each pass: by a memset here, or already by
+// the binning x pass of the spectrum that used its previous contents.
 #include "common.cuh"
 #include "internal.h"
 
