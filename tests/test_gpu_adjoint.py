@@ -93,6 +93,29 @@ def test_adjoint_many_bins(gp):
     assert abs(dldm - rdldm) <= G_RTOL * abs(rdldm) + 1e-300
 
 
+def test_adjoint_paths_agree_at_512(gp):
+    """At N = 512 the mode-gradient kernel (3-D cuFFT mode) walks each row in
+    two chunks of kz (257 modes > 256); the default path applies the mode
+    gradient inside the inverse x pass.  The two gradients agree to FP32
+    transform rounding."""
+    import torch
+    from genpk_gb300 import synth
+    dims, box, nrbins = 512, 1000.0, 24
+    pos = torch.from_numpy(synth.uniform(200_000, box, seed=21)).cuda()
+    m = O.total_mass(200_000, None, 1.0)
+    g = np.linspace(1.0, -1.0, nrbins) * 1e3
+    out = {}
+    with gp.Context(dims, nrbins) as ctx:
+        for mode in (gp.api.FFT_AUTO, gp.api.FFT_CUFFT3D):
+            ctx.set_fft_mode(mode)
+            ctx.zero(0)
+            ctx.deposit(0, box, pos, None, 1.0)
+            ctx.power(0, 0, m, m)
+            out[mode] = ctx.adjoint(0, box, pos, g, m, mass=1.0)[0].cpu().numpy()
+    a, b = out[gp.api.FFT_AUTO], out[gp.api.FFT_CUFFT3D]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 1e-5
+
+
 def test_adjoint_recompute_equals_stored_spectrum(gp):
     dims, box, nrbins = 32, 100.0, 16
     pos, masses = make_case("zeldovich", dims, box, 9, nrbins, True)
