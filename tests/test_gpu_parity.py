@@ -670,6 +670,29 @@ def test_accumulator_cleared_by_the_transform(gp, engine):
     bins_close(got[0], pr, cr)
 
 
+@pytest.mark.parametrize("engine", ["sorted", "window", "stream"])
+def test_deposit_conserves_mass(gp, engine):
+    """The grid's real cells sum to the deposited mass in every engine
+    (variable masses, two passes into one field, positions outside the box)."""
+    from genpk_gb300 import synth
+    rng = np.random.default_rng(12)
+    box, dims = 1000.0, 128
+    lat = synth.zeldovich(128, box, seed=12)
+    out = rng.uniform(-2 * box, 3 * box, (len(lat), 3)).astype(np.float32)
+    m1 = rng.lognormal(0.0, 0.5, len(lat)).astype(np.float32)
+    m2 = rng.lognormal(-1.0, 0.5, len(lat)).astype(np.float32)
+    eng = {"sorted": gp.api.ENGINE_SORTED, "window": gp.api.ENGINE_WINDOW,
+           "stream": gp.api.ENGINE_STREAM}[engine]
+    with gp.Context(dims, 16) as ctx:
+        ctx.set_engine(eng)
+        ctx.deposit(0, box, lat, m1)
+        ctx.sync()
+        ctx.deposit(0, box, out, m2)
+        g = ctx.read_field(0)
+    total = m1.astype(np.float64).sum() + m2.astype(np.float64).sum()
+    assert abs(g[:, :, :dims].sum() - total) <= 1e-6 * total
+
+
 def test_contexts_on_concurrent_host_threads(gp):
     """Contexts used from several host threads at once (one stream each), with
     different grid sizes, so that kernels with size-dependent shared memory

@@ -118,6 +118,20 @@ def test_port_matches_reference_build_random():
             np.testing.assert_allclose(pr[0], pp[0], rtol=1e-11)
 
 
+def test_port_deposit_conserves_mass(oracle_port):
+    """Sum of the FP64 grid equals the deposited mass (CIC weights of each
+    particle sum to one), including positions outside the box (wrapped)."""
+    from genpk_gb300 import synth
+    rng = np.random.default_rng(8)
+    pos = np.concatenate([synth.uniform(20000, 100.0, seed=8),
+                          rng.uniform(-250.0, 350.0, (5000, 3)).astype(np.float32)])
+    masses = rng.lognormal(0.0, 1.0, len(pos)).astype(np.float32)
+    for dims in (16, 17, 32):
+        g = O.zeros_grid(dims)
+        oracle_port.fieldize(100.0, dims, g, pos, masses, 0.0, 1)
+        assert abs(g.sum() - masses.astype(np.float64).sum()) <= 1e-9 * masses.sum()
+
+
 def test_port_bin_of_is_monotone_and_in_range():
     port = O.port()
     for dims, nr in ((64, 64), (128, 17), (256, 256)):
