@@ -1,8 +1,9 @@
-"""The bench's multi-rank path on CPU (gloo, world size 2): the slowest rank's
-time is the job's, the throughput counts every rank's box, and under torchrun
-the reference arm runs on rank 0 alone while the other ranks exit cleanly.
-The GPU arm's ranks are independent replicas with no collective on the data
-path; these tests cover the host logic around them."""
+"""The bench's host logic on CPU.  The multi-rank path (gloo, world size 2):
+the slowest rank's time is the job's, the throughput counts every rank's box,
+and under torchrun the reference arm runs on rank 0 alone while the other
+ranks exit cleanly (the GPU arm's ranks are independent replicas with no
+collective on the data path).  Also the roofline's algorithmic bytes and the
+seeded batch of boxes."""
 import json
 import os
 import socket
@@ -69,3 +70,27 @@ def test_reference_arm_under_torchrun_two_ranks(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "particles/s" and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_algorithmic_bytes_match_the_stated_figures():
+    """The roofline's numerators: deposit = particles read once + FP32 padded
+    grid written once; binning = the half-complex spectrum read once.  512^3:
+    1.61 GB + 0.539 GB and 0.539 GB; 1024^3: 12.88 GB + 4.30 GB and 4.30 GB."""
+    sys.path.insert(0, ROOT)
+    import bench
+    dep, binb = bench.algorithmic_bytes(512 ** 3, 512)
+    assert dep == 512 ** 3 * 12 + 4 * 512 * 512 * 2 * 257
+    assert round(dep / 1e9, 2) == round(1.611 + 0.539, 2) and round(binb / 1e9, 3) == 0.539
+    dep, binb = bench.algorithmic_bytes(1024 ** 3, 1024)
+    assert round((dep - 1024 ** 3 * 12) / 1e9, 2) == 4.30 and round(binb / 1e9, 2) == 4.30
+    dep_m, _ = bench.algorithmic_bytes(1000, 64, var_masses=True)
+    assert dep_m - bench.algorithmic_bytes(1000, 64)[0] == 4000
+
+
+def test_box_batch_is_seeded_and_in_range():
+    sys.path.insert(0, ROOT)
+    import bench
+    a, box = bench.box_batch()
+    b, _ = bench.box_batch()
+    assert a == b and len(a) == 16 and box == 25000.0
+    assert all(1e5 <= c <= 3e7 and g in (128, 256) for c, g, _ in a)
