@@ -929,7 +929,7 @@ size_t xfft_smem(int dims, int nrbins, int mode)
         s = (s + 15) & ~(size_t)15;
         s += sizeof(double) * nrbins + sizeof(uint32_t) * (nrbins + 1);
     } else if (mode == kXGrad) {
-        s = (s + 15) & ~(size_t)15;
+        // the kernel's empty binning buffers still round the offset up to 16
         s = (s + 15) & ~(size_t)15;
         s += sizeof(uint32_t) * (nrbins + 1) + sizeof(float) * nrbins;
     }
