@@ -234,8 +234,14 @@ int64_t genpk_kernel_launches(const genpk_ctx *ctx);
  * Its scratch (about 2.5 MB: bin tables and per-block partial sums) is a
  * static array in the library's device image, held by every GPU that loads the
  * library until the process exits.  The first call on each device looks up
- * the array's device address.  Every call shares the array and keeps its last
- * contents, so calls that overlap on the GPU race; serialise them. */
+ * the array's device address; with CUDA's lazy module loading (the default)
+ * that lookup is what loads the module and reserves the array, so it can fail
+ * (GENPK_ERR_CUDA) once an allocator has claimed the whole device: make one
+ * call on each device before the allocator takes it.  A call with a
+ * (dims, nrbins) other than the previous call's on that device also rebuilds
+ * the bin tables on the host and copies them to the array on `stream`.
+ * Every call shares the array and keeps its last contents, so calls that
+ * overlap on the GPU race; serialise them. */
 int genpk_power_noalloc(const float *spectrum_a, const float *spectrum_b, int64_t dims,
                         int nrbins, double mass_a, double mass_b, double *power, int *count,
                         double *keffs, void *stream);

@@ -27,18 +27,37 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libgenpk_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libgenpk_ref.so")
-REF_SRC = os.environ.get("GENPK_REFERENCE_DIR", "/root/reference")
+# The reference source tree that oracle/_ref was compiled from: written by
+# build(ref_dir=...) beside the library, or named by GENPK_REFERENCE_DIR.  No
+# default: where neither exists, the reference build and its fixtures are skipped.
+REF_DIR_RECORD = os.path.join(HERE, "_ref", "source_dir")
 
 _f64p = ctypes.POINTER(ctypes.c_double)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i32p = ctypes.POINTER(ctypes.c_int)
 
 
-def build(ref: bool = True) -> None:
-    """Compile the port (always) and the reference build (when its sources exist)."""
+def reference_tree():
+    """The reference source tree (GENPK_REFERENCE_DIR, else the one the
+    reference build was made from), or None."""
+    d = os.environ.get("GENPK_REFERENCE_DIR")
+    if not d and os.path.exists(REF_DIR_RECORD):
+        with open(REF_DIR_RECORD) as f:
+            d = f.read().strip()
+    if d and os.path.exists(os.path.join(d, "fieldize.cpp")):
+        return d
+    return None
+
+
+def build(ref_dir=None) -> None:
+    """Compile the port (always) and, given the reference's source tree
+    (ref_dir, or GENPK_REFERENCE_DIR), the reference build from it."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if ref and os.path.exists(os.path.join(REF_SRC, "fieldize.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={REF_SRC}"], check=True)
+    d = ref_dir or os.environ.get("GENPK_REFERENCE_DIR")
+    if d and os.path.exists(os.path.join(d, "fieldize.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={d}"], check=True)
+        with open(REF_DIR_RECORD, "w") as f:
+            f.write(os.path.abspath(d) + "\n")
 
 
 def _bind(lib, name, restype, argtypes):
@@ -103,7 +122,7 @@ def port() -> _Impl:
     global _PORT
     if _PORT is None:
         if not os.path.exists(PORT_LIB):
-            build(ref=False)
+            build()
         _PORT = _Impl(PORT_LIB, "oracle_fieldize", "oracle_powerspectrum", "oracle_invwindow")
         lib = _PORT.lib
         _PORT.gather = _bind(lib, "oracle_cic_gather", ctypes.c_int,
@@ -122,9 +141,10 @@ def ref():
     global _REF
     if _REF is None:
         if not os.path.exists(REF_LIB):
-            if not os.path.exists(os.path.join(REF_SRC, "fieldize.cpp")):
+            tree = reference_tree()
+            if tree is None:
                 return None
-            build(ref=True)
+            build(ref_dir=tree)
         _REF = _Impl(REF_LIB, "ref_fieldize", "powerspectrum", "invwindow")
     return _REF
 

@@ -32,7 +32,7 @@ def native_lib():
 @pytest.fixture(scope="session")
 def oracle_port():
     from oracle import oracle as O
-    O.build(ref=False)
+    O.build()
     return O.port()
 
 

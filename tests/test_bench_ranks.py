@@ -70,6 +70,9 @@ def test_reference_arm_under_torchrun_two_ranks(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "particles/s" and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    # measured on the whole workload every step, not extrapolated from a sample
+    assert "whole workload" in d["cpu_baseline"]["sample"]
+    assert d["ms_per_step"] == pytest.approx(1e3 * sum(d["stages_s"].values()), rel=0.05)
 
 
 def test_algorithmic_bytes_match_the_stated_figures():

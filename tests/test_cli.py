@@ -79,9 +79,10 @@ def test_cli_reads_the_header(native_lib, tmp_path):
 def test_cli_reads_the_reference_snapshot_fixture(native_lib):
     """The reference's own two-file format-II fixture (written by Gadget), where
     its source tree is present: particle counts, box and scale factor."""
-    base = os.path.join(O.REF_SRC, "test_g2_snap")
-    if not os.path.exists(base + ".0"):
+    tree = O.reference_tree()
+    if tree is None or not os.path.exists(os.path.join(tree, "test_g2_snap.0")):
         pytest.skip("reference tree not present")
+    base = os.path.join(tree, "test_g2_snap")
     r = run_cli("-i", base, "-d")
     assert r.returncode == 0, r.stderr
     assert "files=2" in r.stdout and "Boxsize=3000" in r.stdout

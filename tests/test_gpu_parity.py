@@ -776,7 +776,9 @@ def test_cross_and_multi_spectra(gp):
 
 
 def test_compat_bound_fields_route_to_device(gp):
-    """The fieldize/powerspectrum drop-ins on a bound host field."""
+    """The fieldize/powerspectrum drop-ins on a bound host field: the reader's
+    chunked fieldize calls and the driver's powerspectrum call, unchanged,
+    reach the device grid of the context the field is bound to."""
     from genpk_gb300 import native, synth
     compat = native.load_compat()
     dims, box, nrbins = 32, 100.0, 16
