@@ -226,6 +226,12 @@ class Context:
     def bin_of(self, kk2: int) -> int:
         return int(self.lib.genpk_bin_of(self.h, int(kk2)))
 
+    def inject_copy_timeout(self, chunk: int, wait_clocks: int = 1 << 16):
+        """Testing aid: the next window/stream-engine pass leaves chunk
+        `chunk` without its bulk copy, so its bounded wait gives up
+        (genpk_inject_copy_timeout)."""
+        self._chk(self.lib.genpk_inject_copy_timeout(self.h, int(chunk), int(wait_clocks)))
+
 
 # ---------------------------------------------------------------------------
 # Reference-named functions

@@ -72,7 +72,15 @@ struct WinParams {
     int row;
     int corner;  // accumulate the exact (N/2,N/2,N/2) mode (even grids)
     int bulk;    // positions (and masses) 16-byte aligned: full chunks by bulk copy
+    // Testing aid (genpk_inject_copy_timeout): the bulk copy of chunk
+    // skip_chunk is not issued and the wait for it gives up after skip_wait
+    // clocks; -1 for none.
+    int64_t skip_chunk;
+    long long skip_wait;
 };
+
+// Clocks a bounded wait spins before it gives up: about a second.
+constexpr long long kWaitClocks = 1ll << 31;
 
 // ---- bulk asynchronous copies and mbarriers (inline PTX) -------------------
 
@@ -117,14 +125,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
     return ok != 0u;
 }
 
-// Bounded wait for a phase of `bar`: false after ~2^31 clocks (about a second).
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+// Bounded wait for a phase of `bar`: false after `limit` clocks.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          long long limit)
 {
     if (mbar_try_wait(bar, parity))
         return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1ll << 31))
+        if (clock64() - t0 > limit)
             return false;
     }
     return true;
@@ -239,6 +248,8 @@ template <bool VARMASS>
 __device__ __forceinline__ void issue_chunk(const WinParams &p, int64_t c, float *P, float *M,
                                             unsigned long long *bar)
 {
+    if (c == p.skip_chunk)  // testing aid: no copy, so the wait for it runs out
+        return;
     const unsigned pb = (unsigned)p.chunk * 12u, mb = VARMASS ? (unsigned)p.chunk * 4u : 0u;
     fence_proxy_async();
     mbar_expect_tx(bar, pb + mb);
@@ -273,6 +284,37 @@ __device__ __forceinline__ void copy_chunk(const WinParams &p, int64_t c, int cn
     copy_floats(P, p.pos + 3 * chunk_first(p, c), 3 * cnt);
     if (VARMASS)
         copy_floats(M, p.masses + chunk_first(p, c), cnt);
+}
+
+// Chunk arrival, every thread.  A bulk-copied chunk (bulk) is waited for on
+// bar's phase `parity`, with a bounded wait; any other chunk is loaded with
+// plain loads.  Ends with a barrier: the chunk is in place and every thread is
+// done with the other buffer.  If the wait ran out on any thread, the whole
+// CTA (the decision is made at the barrier, so it is uniform) waits once more,
+// bounded, for a copy that may still be in flight, counts one timeout, loads
+// the chunk with plain loads and sets `broken`: this CTA issues no further bulk
+// copies (the barrier's phase may never complete), so the pass still deposits
+// every particle and only its status reports the wait.
+template <bool VARMASS>
+__device__ __forceinline__ void arrive_chunk(const WinParams &p, int64_t c, int cnt, bool bulk,
+                                             float *P, float *M, unsigned long long *bar,
+                                             unsigned parity, bool &broken, unsigned &timeouts)
+{
+    const long long limit = c == p.skip_chunk ? p.skip_wait : kWaitClocks;
+    bool late = false;
+    if (bulk)
+        late = !mbar_wait(bar, parity, limit);
+    else
+        copy_chunk<VARMASS>(p, c, cnt, P, M);
+    if (__syncthreads_or(late)) {
+        mbar_wait(bar, parity, limit);
+        __syncthreads();
+        copy_chunk<VARMASS>(p, c, cnt, P, M);
+        __syncthreads();
+        broken = true;
+        if (threadIdx.x == 0)
+            timeouts++;
+    }
 }
 
 // The pass accumulates exact 64-bit integers acc[gi] for every padded grid
@@ -383,6 +425,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
 
     f2sum alt = {0.f, 0.f};
     unsigned bad = 0, timeouts = 0;
+    bool broken = false;  // a wait ran out: plain loads from then on
     const int64_t c0 = blockIdx.x;
     if (threadIdx.x == 0 && c0 < p.nchunks && chunk_by_bulk(p, c0))
         issue_chunk<VARMASS>(p, c0, pbuf, mbuf, &bar[0]);
@@ -393,13 +436,8 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         float *P = pbuf + buf * 3 * p.chunk;
         float *M = mbuf + buf * p.chunk;
         const int cnt = (int)min((int64_t)p.chunk, p.n - chunk_first(p, c));
-        if (chunk_by_bulk(p, c)) {
-            if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
-                timeouts++;
-        } else {
-            copy_chunk<VARMASS>(p, c, cnt, P, M);
-            __syncthreads();
-        }
+        arrive_chunk<VARMASS>(p, c, cnt, !broken && chunk_by_bulk(p, c), P, M, &bar[buf],
+                              (unsigned)(k >> 1) & 1u, broken, timeouts);
 
         // Pass A: float offsets of the approximate cells from the chunk's
         // first particle, periodic-wrapped into [-N/2, N/2].
@@ -431,7 +469,8 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         // Prefetch the chunk after this one into the other buffer (its last
         // reader, pass B of the previous chunk, finished before the previous
         // flush's barrier).
-        if (threadIdx.x == 0 && c + gridDim.x < p.nchunks && chunk_by_bulk(p, c + gridDim.x))
+        if (threadIdx.x == 0 && !broken && c + gridDim.x < p.nchunks &&
+            chunk_by_bulk(p, c + gridDim.x))
             issue_chunk<VARMASS>(p, c + gridDim.x, pbuf + (buf ^ 1) * 3 * p.chunk,
                                  mbuf + (buf ^ 1) * p.chunk, &bar[buf ^ 1]);
         const WinBox box = window_box(fmn, fmx, ref, p, sh_mm, sh_box);
@@ -589,6 +628,7 @@ __global__ void __launch_bounds__(kWinThreads, 1)
 
     f2sum alt = {0.f, 0.f};
     unsigned bad = 0, timeouts = 0;
+    bool broken = false;  // a wait ran out: plain loads from then on
     const int64_t c0 = blockIdx.x;
     if (threadIdx.x == 0 && c0 < p.nchunks && chunk_by_bulk(p, c0))
         issue_chunk<VARMASS>(p, c0, pbuf, mbuf, &bar[0]);
@@ -599,15 +639,11 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         float *P = pbuf + buf * 3 * p.chunk;
         float *M = mbuf + buf * p.chunk;
         const int cnt = (int)min((int64_t)p.chunk, p.n - chunk_first(p, c));
-        if (chunk_by_bulk(p, c)) {
-            if (!mbar_wait(&bar[buf], (unsigned)(k >> 1) & 1u))
-                timeouts++;
-        } else {
-            copy_chunk<VARMASS>(p, c, cnt, P, M);
-        }
         // The chunk is in place, and every thread is done with the other buffer.
-        __syncthreads();
-        if (threadIdx.x == 0 && c + gridDim.x < p.nchunks && chunk_by_bulk(p, c + gridDim.x))
+        arrive_chunk<VARMASS>(p, c, cnt, !broken && chunk_by_bulk(p, c), P, M, &bar[buf],
+                              (unsigned)(k >> 1) & 1u, broken, timeouts);
+        if (threadIdx.x == 0 && !broken && c + gridDim.x < p.nchunks &&
+            chunk_by_bulk(p, c + gridDim.x))
             issue_chunk<VARMASS>(p, c + gridDim.x, pbuf + (buf ^ 1) * 3 * p.chunk,
                                  mbuf + (buf ^ 1) * p.chunk, &bar[buf ^ 1]);
 
@@ -957,6 +993,8 @@ WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk)
               (!var || (uintptr_t)a.masses % 16 == 0))
                  ? 1
                  : 0;
+    p.skip_chunk = a.skip_chunk;
+    p.skip_wait = a.skip_wait;
     return p;
 }
 

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <math.h>
+#include <stddef.h>
 #include <string.h>
 
 #include <algorithm>
@@ -113,6 +114,9 @@ struct genpk_ctx {
     Choice choices[kChoices];
     int choice_next = 0;
     size_t probe_cap = 0;
+    // genpk_inject_copy_timeout: applied to the next window-engine pass only
+    int64_t inject_chunk = -1;
+    long long inject_clocks = 0;
 
     // staging of host particles
     float *stage_pos = nullptr;
@@ -258,14 +262,18 @@ int check_field(genpk_ctx *ctx, int f)
     return GENPK_OK;
 }
 
-// Read back and clear the device status words.
+// Read back and clear the device's error counters.  Only the counters: the
+// rest of the status (the latest pass's mean and scale) is still needed by a
+// pass whose conversion is deferred to the transform.
 int collect_status(genpk_ctx *ctx)
 {
     DeviceStatus st;
     GENPK_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     if (st.bad_particles || st.timeouts) {
-        GENPK_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(DeviceStatus), ctx->stream));
+        static_assert(offsetof(DeviceStatus, timeouts) == sizeof(unsigned long long),
+                      "the two counters lead DeviceStatus");
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(unsigned long long), ctx->stream));
         GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
         if (st.timeouts)
             return fail(ctx, GENPK_ERR_TIMEOUT,
@@ -419,6 +427,11 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     const bool chunked = engine == GENPK_ENGINE_WINDOW || engine == GENPK_ENGINE_STREAM;
     if (engine == GENPK_ENGINE_STREAM)
         chunk = kStreamChunk;
+    if (chunked && ctx->inject_chunk >= 0) {
+        a.skip_chunk = ctx->inject_chunk;
+        a.skip_wait = ctx->inject_clocks;
+        ctx->inject_chunk = -1;
+    }
     if (host_mapped && !chunked) {
         // The sorted engine reads positions twice: copy them over once instead.
         GENPK_TRY(ensure_stage(ctx, n));
@@ -1392,6 +1405,17 @@ int genpk_last_deposit_engine(const genpk_ctx *ctx)
 int64_t genpk_kernel_launches(const genpk_ctx *ctx)
 {
     return ctx ? ctx->launches : -1;
+}
+
+int genpk_inject_copy_timeout(genpk_ctx *ctx, int64_t chunk, int64_t wait_clocks)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (chunk < 0)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_inject_copy_timeout: negative chunk");
+    ctx->inject_chunk = chunk;
+    ctx->inject_clocks = std::min<int64_t>(std::max<int64_t>(wait_clocks, 1024), (int64_t)1 << 31);
+    return GENPK_OK;
 }
 
 }  // extern "C"

@@ -93,6 +93,11 @@ struct DepositArgs {
     double *field_corner;  // device: exact DFT value at k = (N/2, N/2, N/2), even N
     bool clean;            // grid content is undefined and must be overwritten
     bool host_mapped = false;  // pos/masses are pinned host memory read in place
+    // Testing aid for the window engine's bounded waits (genpk_inject_copy_timeout):
+    // chunk skip_chunk's bulk copy is not issued, and its wait gives up after
+    // skip_wait clocks.  -1: none.
+    int64_t skip_chunk = -1;
+    long long skip_wait = 0;
 };
 
 // Tile shapes the deposit kernels are instantiated for.

@@ -210,6 +210,18 @@ int genpk_set_fft_mode(genpk_ctx *ctx, int mode);
 /* Number of kernels the library launched on ctx since creation. */
 int64_t genpk_kernel_launches(const genpk_ctx *ctx);
 
+/* Testing aid for the bounded device waits (no reference counterpart; the
+ * reference has no device code).  The next window- or stream-engine deposit
+ * pass on ctx does not issue the bulk copy of its chunk number `chunk`
+ * (chunks of the pass's chunk length, 4096 particles in the stream mode,
+ * counted from 0 in particle order), so the kernel's bounded wait for that
+ * copy gives up after wait_clocks SM clocks (clamped to [1024, 2^31]).  The
+ * CTA then loads that chunk and its later ones with plain loads, so the grid
+ * is still complete, and the next sync point (genpk_sync, genpk_power)
+ * returns GENPK_ERR_TIMEOUT.  Nothing faults or hangs and the context stays
+ * usable.  Applies to one pass; a pass of the sorted engine ignores it. */
+int genpk_inject_copy_timeout(genpk_ctx *ctx, int64_t chunk, int64_t wait_clocks);
+
 /* Largest sizes genpk_power_noalloc accepts. */
 #define GENPK_NOALLOC_MAX_DIMS 1024
 #define GENPK_NOALLOC_MAX_NRBINS 1024
