@@ -162,9 +162,13 @@ def zeros_grid(dims: int) -> np.ndarray:
     return np.zeros((dims, dims, padded_len(dims)), dtype=np.float64)
 
 
-def rfft_padded(grid: np.ndarray) -> np.ndarray:
-    """FP64 r2c of the real part of a padded grid -> (dims, dims, dims/2+1) complex128."""
+def rfft_padded(grid: np.ndarray, workers=None) -> np.ndarray:
+    """FP64 r2c of the real part of a padded grid -> (dims, dims, dims/2+1) complex128.
+    workers: threads for scipy's pocketfft (large grids); None: numpy's."""
     dims = grid.shape[0]
+    if workers:
+        import scipy.fft as sfft
+        return sfft.rfftn(grid[:, :, :dims], axes=(0, 1, 2), workers=workers)
     return np.fft.rfftn(grid[:, :, :dims], axes=(0, 1, 2))
 
 
@@ -187,11 +191,13 @@ def deposit(pos, boxsize, dims, masses=None, mass=1.0, impl=None) -> np.ndarray:
     return g
 
 
-def pk(pos, boxsize, dims, nrbins, masses=None, mass=1.0, m_norm=None, impl=None):
+def pk(pos, boxsize, dims, nrbins, masses=None, mass=1.0, m_norm=None, impl=None,
+       workers=None):
     """Deposit + FP64 r2c + binning: the P(k) gen-pk writes for one species."""
     impl = impl or port()
     g = deposit(pos, boxsize, dims, masses, mass, impl)
-    f = rfft_padded(g)
+    f = rfft_padded(g, workers)
+    del g
     if m_norm is None:
         m_norm = total_mass(len(pos), masses, mass)
     return impl.powerspectrum(dims, f, f, nrbins, m_norm, m_norm)
@@ -219,9 +225,7 @@ def mode_tables(dims: int, nrbins: int):
     kv = kval(dims)
     kz = np.arange(half + 1)
     kk2 = (kv[:, None, None] ** 2 + kv[None, :, None] ** 2 + kz[None, None, :] ** 2)
-    uniq = np.unique(kk2)
-    lut = {int(v): (impl.bin_of(int(v), dims, nrbins) if v > 0 else -1) for v in uniq}
-    bins = np.vectorize(lambda v: lut[int(v)], otypes=[np.int64])(kk2)
+    bins = bin_lut(dims, nrbins)[kk2]
     c = np.full(kk2.shape, 2.0)
     c[:, :, 0] = 1.0
     c[:, :, half] = 1.0
@@ -279,3 +283,98 @@ def reference_gradient(pos, boxsize, dims, nrbins, gbin, masses=None, mass=1.0,
     dl_dm = float(np.sum(gb * (-2.0 * power / m_norm)))
     gmass = gw + dl_dm if masses is not None else None
     return gpos, gmass, dl_dm
+
+
+def bin_lut(dims: int, nrbins: int) -> np.ndarray:
+    """Bin of every integer |k|^2 from 0 to 3 (dims/2)^2 (-1 for 0), from the
+    port's restatement of the reference's bin expression (powerspectrum.c:38,66)."""
+    impl = port()
+    half = dims // 2
+    top = 3 * half * half
+    lut = np.array([impl.bin_of(v, dims, nrbins) for v in range(1, top + 1)], dtype=np.int64)
+    return np.concatenate([[-1], lut])
+
+
+def cic_gather_sample(drho, pos, boxsize, masses=None, mass=1.0):
+    """oracle_cic_gather for a few particles, in numpy: the CIC-weighted value
+    of the real grid drho [dims]^3 at each particle (the mass gradient before
+    dL/dM) and its position derivative m * units * sum (+-1) prod_{e!=a} w_e."""
+    dims = drho.shape[0]
+    units = dims / boxsize
+    x = np.asarray(pos, dtype=np.float32).reshape(-1, 3).astype(np.float64) * units
+    f = np.floor(x)
+    d = x - f
+    t = 1.0 - d
+    lo = np.mod(f.astype(np.int64), dims)
+    hi = np.mod(f.astype(np.int64) + 1, dims)
+    m = (np.asarray(masses, dtype=np.float32).astype(np.float64) if masses is not None
+         else np.full(len(x), float(mass)))
+    sw = np.zeros(len(x))
+    dg = np.zeros((len(x), 3))
+    for c in range(8):
+        b = [(c >> a) & 1 for a in range(3)]
+        w = [d[:, a] if b[a] else t[:, a] for a in range(3)]
+        idx = [hi[:, a] if b[a] else lo[:, a] for a in range(3)]
+        gv = drho[idx[0], idx[1], idx[2]]
+        sw += w[0] * w[1] * w[2] * gv
+        for a in range(3):
+            sgn = 1.0 if b[a] else -1.0
+            other = np.ones(len(x))
+            for e in range(3):
+                if e != a:
+                    other = other * w[e]
+            dg[:, a] += sgn * other * gv
+    return dg * (m * units)[:, None], sw
+
+
+def reference_gradient_sampled(pos, boxsize, dims, nrbins, gbin, sample, masses=None,
+                               mass=1.0, m_norm=None, quirk=1.0, workers=None):
+    """reference_gradient's mathematics for grids too large for its
+    full-size temporaries: the FP64 deposit and r2c of all particles, the
+    mode gradient applied one x-plane at a time, the unnormalised c2r, and
+    the CIC gather at the particles `sample` only.  Also returns the FP64
+    forward of the same run.
+    Returns (power, count, keffs, gpos [len(sample), 3], gmass or None, dL/dM)."""
+    impl = port()
+    n = len(pos)
+    if m_norm is None:
+        m_norm = total_mass(n, masses, mass, quirk)
+    f = rfft_padded(deposit(pos, boxsize, dims, masses, mass, impl), workers)
+    power, count, keffs = impl.powerspectrum(dims, f, f, nrbins, m_norm, m_norm)
+    half = dims // 2
+    kv = kval(dims)
+    kz = np.arange(half + 1)
+    lut = bin_lut(dims, nrbins)
+    iw1 = np.array([impl.onedinvwindow(int(k), dims) for k in kv], dtype=np.float32)
+    c = np.full((dims, half + 1), 2.0)
+    c[:, 0] = 1.0
+    c[:, half] = 1.0
+    mult = np.full((dims, half + 1), 2.0)
+    mult[:, 0] = 1.0
+    if dims % 2 == 0:
+        mult[:, half] = 1.0
+    cb = count.astype(np.float64)
+    gb = np.asarray(gbin, dtype=np.float64)
+    coef = np.zeros(nrbins)
+    okb = cb > 0
+    coef[okb] = 2.0 * gb[okb] / (m_norm ** 2 * cb[okb])
+    for i in range(dims):
+        kk2 = kv[i] ** 2 + kv[:, None] ** 2 + kz[None, :] ** 2
+        bins = lut[kk2]
+        ci = c.copy()
+        if i == 0:
+            ci[0, 0] = 0.0
+        prod = (iw1[i] * iw1[:, None]).astype(np.float32) * iw1[None, :half + 1]
+        v = prod.astype(np.float32).astype(np.float64) ** 4
+        scale = np.where(bins >= 0, coef[np.maximum(bins, 0)], 0.0) * v * ci / mult
+        f[i] *= scale
+    import scipy.fft as sfft
+    drho = sfft.irfftn(f, s=(dims, dims, dims), axes=(0, 1, 2), workers=workers or 1)
+    drho *= float(dims) ** 3
+    del f
+    sp = np.asarray(pos, dtype=np.float32).reshape(-1, 3)[sample]
+    sm = np.asarray(masses, dtype=np.float32)[sample] if masses is not None else None
+    gpos, gw = cic_gather_sample(drho, sp, boxsize, sm, mass)
+    dl_dm = float(np.sum(gb * (-2.0 * power / m_norm)))
+    gmass = gw + dl_dm if masses is not None else None
+    return power, count, keffs, gpos, gmass, dl_dm

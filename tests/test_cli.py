@@ -121,6 +121,35 @@ def test_cli_per_type_spectra(native_lib, tmp_path):
 
 
 @pytest.mark.gpu
+def test_cli_uniform_128_snapshot(native_lib, tmp_path):
+    """The 128^3 snapshot configuration: one format-II file holding only
+    type 1, 128^3 = 2,097,152 particles with float32 positions i.i.d. uniform
+    in [0, 25000) kpc/h and the header mass 1.0e-2 (box 25000, a = 1,
+    h = 0.7), run as gen-pk -g 128 -b 64.  The PK-DM file against the oracle
+    normalised with the reader's +1 (read_fieldize.cpp:94): every bin within
+    1e-5 (printed to 7 digits), counts bit-exact."""
+    from genpk_gb300 import synth
+    box, n = 25000.0, 128 ** 3
+    pos = synth.uniform(n, box, seed=1)
+    base = str(tmp_path / "snap_128")
+    synth.write_gadget2(base, {1: pos}, {1: 1.0e-2}, box, nfiles=1, time=1.0, redshift=0.0,
+                        hubble=0.7)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = run_cli("-i", base, "-o", str(out), "-g", "128", "-b", "64")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "FFT grid dimension: 128" in r.stdout
+    M = O.total_mass(n, None, 1.0e-2)
+    assert f"total_mass in type 1 = {M:g}" in r.stdout
+    pe, ce, ke = O.pk(pos, box, 128, 64, None, 1.0e-2, m_norm=M)
+    k, p, c = read_pk(out / "PK-DM-snap_128")
+    ok = ce > 0
+    assert np.array_equal(c, ce[ok])
+    assert close(p, pe[ok], 1e-5) and close(k, ke[ok], 1e-6)
+    assert sorted(os.listdir(out)) == ["PK-DM-snap_128"]
+
+
+@pytest.mark.gpu
 def test_cli_default_grid_rule_and_stars_in_baryons(native_lib, tmp_path):
     """No -g / -b: grid = max over types of 2*nexttwo(cbrt(npart)) = 32 for
     16^3 dark-matter particles, nrbins = grid.  -s 1 adds the stars to the

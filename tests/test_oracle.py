@@ -172,3 +172,30 @@ def test_reference_gradient_matches_finite_differences():
         mm[i] -= h
         fd = (loss(pos, mp.astype(np.float32))[0] - loss(pos, mm.astype(np.float32))[0]) / (2 * h)
         assert abs(fd - gmass[i]) <= 2e-2 * abs(fd) + 1e-6, (i, fd, gmass[i])
+
+
+def test_sampled_reference_gradient_matches_the_full_one():
+    """The plane-by-plane, sampled FP64 gradient (used where the full one's
+    temporaries would not fit) equals reference_gradient at the sampled
+    particles, with the same forward; even and odd grids, both mass kinds."""
+    from genpk_gb300 import synth
+    for dims, var in ((32, True), (24, False), (15, True)):
+        box, nrbins = 1000.0, 12
+        pos = synth.zeldovich(dims, box, seed=dims)
+        masses = (np.random.default_rng(dims).random(len(pos)) + 0.5).astype(np.float32) \
+            if var else None
+        g = np.linspace(1.0, -2.0, nrbins) * 1e3
+        m = O.total_mass(len(pos), masses, 0.0 if var else 1.0)
+        rpos, rmass, rdm = O.reference_gradient(pos, box, dims, nrbins, g, masses,
+                                                0.0 if var else 1.0, m_norm=m)
+        pr, cr, kr = O.pk(pos, box, dims, nrbins, masses, 0.0 if var else 1.0, m_norm=m)
+        idx = np.random.default_rng(1).choice(len(pos), 200, replace=False)
+        p, c, k, gpos, gmass, dm = O.reference_gradient_sampled(
+            pos, box, dims, nrbins, g, idx, masses, 0.0 if var else 1.0, m_norm=m, workers=2)
+        assert np.array_equal(c, cr)
+        np.testing.assert_allclose(p, pr, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(gpos, rpos[idx], rtol=1e-9, atol=1e-12 * np.abs(rpos).max())
+        if var:
+            np.testing.assert_allclose(gmass, rmass[idx], rtol=1e-9,
+                                       atol=1e-12 * np.abs(rmass).max())
+        assert dm == pytest.approx(rdm, rel=1e-12)
