@@ -12,6 +12,8 @@ particles, r2c FFT, fused deconvolution + binning, read the 64 bins back.
              ranks (each rank an independent box: replicas, weak scaling).
   e2e        the same through the C ABI from pinned host buffers: the H2D copy
              of the positions and the D2H of the bins are inside each step.
+  e2e_pageable  the same from pageable host memory in chunks of 2^26 particles,
+             the way the reference's reader hands them to fieldize.
   roofline   HBM roofline of the deposit pass (the dominant stage): algorithmic
              bytes Np*12 + 4*N^2*2(N/2+1) over its device time; also the
              binning kernel and deposit+binning together.
@@ -591,6 +593,32 @@ def main():
                        "ms_per_step": e_ms, "ms_min": min(e2e_t) * 1e3,
                        "ms_max": max(e2e_t) * 1e3}
         del hpos
+        # the same from pageable host memory handed over in chunks of at most 2^26
+        # particles, as the reference's reader calls fieldize (read_fieldize.cpp:45-93)
+        hp = dpos.cpu().numpy()
+        chunk = 1 << 26
+
+        def step_pageable():
+            ctx.timing_reset()
+            ctx.zero(0)
+            for a in range(0, npart, chunk):
+                ctx.deposit(0, box, hp[a:a + chunk], None, mass)
+            ctx.power(0, 0, m_norm, m_norm)
+
+        for _ in range(2):
+            step_pageable()
+        pg_t = []
+        for _ in range(max(3, min(args.steps, 10))):
+            t1 = time.perf_counter()
+            step_pageable()
+            pg_t.append(time.perf_counter() - t1)
+        p_ms = max_over_ranks(float(np.mean(pg_t)) * 1e3, world)
+        line["e2e_pageable"] = {"value": job_throughput(npart, world, p_ms), "unit": "particles/s",
+                                "h2d_bytes_per_step": npart * 12,
+                                "d2h_bytes_per_step": nrbins * 8, "ms_per_step": p_ms,
+                                "chunk_particles": chunk,
+                                "vs_pinned": p_ms / e_ms}
+        del hp
 
     # forward + adjoint / forward
     if not args.no_adjoint:

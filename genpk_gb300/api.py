@@ -217,7 +217,25 @@ class Context:
         return int(self.lib.genpk_last_deposit_engine(self.h))
 
     def set_tile(self, tx: int, ty: int, tz: int):
+        """Fix the sorted engine's tile (turns its autotuner off); (0, 0, 0):
+        automatic again."""
         self._chk(self.lib.genpk_set_deposit_tile(self.h, tx, ty, tz))
+
+    def deposit_trials(self) -> list:
+        """The sorted engine's latest tuning: [(tile, sort CTAs, ms), ...]."""
+        from . import native
+        cap = 8
+        tx = (ctypes.c_int * cap)()
+        ty = (ctypes.c_int * cap)()
+        tz = (ctypes.c_int * cap)()
+        sc = (ctypes.c_int * cap)()
+        ms = (ctypes.c_float * cap)()
+        k = self.lib.genpk_deposit_trials(self.h, ctypes.cast(tx, native.c_i32p),
+                                          ctypes.cast(ty, native.c_i32p),
+                                          ctypes.cast(tz, native.c_i32p),
+                                          ctypes.cast(sc, native.c_i32p),
+                                          ctypes.cast(ms, native.c_f32p), cap)
+        return [((tx[i], ty[i], tz[i]), sc[i], ms[i]) for i in range(max(k, 0))]
 
     @property
     def launches(self) -> int:

@@ -31,7 +31,7 @@ CU_SOURCES = ["deposit.cu", "deposit_window.cu", "spectrum.cu", "xfft.cu", "adjo
 CXX_SOURCES = {"genpk.cpp": ["-O2"], "tables.cpp": ["-O2", "-ffast-math"]}
 COMPAT_SOURCE = "compat.cpp"
 # The gen-pk command line (format-II reader + driver) over the C ABI.
-CLI_SOURCES = ["gadget2.cpp", "gen_pk_gb300.cpp"]
+CLI_SOURCES = ["gadget2.cpp", "bigfile.cpp", "gen_pk_gb300.cpp"]
 
 
 def _run(cmd):
@@ -85,6 +85,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         o = os.path.join(BUILD, "cli_" + src + ".o")
         cli_objs.append(o)
         if force or _stale(o, [s, os.path.join(cli_dir, "gadget2.h"),
+                               os.path.join(cli_dir, "bigfile.h"),
                                os.path.join(ROOT, "include", "genpk_gb300.h")]):
             jobs.append(["g++", "-O2", "-std=c++17", "-Wall", f"-I{ROOT}/include", "-c", s,
                          "-o", o])

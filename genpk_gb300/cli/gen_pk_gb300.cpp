@@ -1,7 +1,10 @@
 // gen_pk_gb300.cpp -- the gen-pk command line on the GB300 library.
 //
 // Same flags, files and flow as the reference driver (gen-pk.cpp:72-367):
-//   -i snapshot   format-II file, or the base name of a set base.0, base.1, ...
+//   -i snapshot   a BigFile snapshot directory (bigfile.h), else a format-II
+//                 file or the base name of a set base.0, base.1, ...
+//                 (gen-pk.cpp:121-152 tries HDF5, then BigFile, then Gadget;
+//                 HDF5 files are recognised and refused: libhdf5 is absent)
 //   -o outdir     one file per particle type: outdir/PK-<type>-<input>
 //   -j snapshot2  cross spectrum of each type between the two snapshots:
 //                 outdir/PX-<type>-<input>   (gen-pk.cpp:240-303)
@@ -17,10 +20,14 @@
 //
 // Each type is read in chunks of at most 2^26 particles and deposited with
 // genpk_deposit (+= across chunks, as read_fieldize.cpp:41-93 calls fieldize);
-// the normalising mass is the sum of the particle masses plus 1, the
-// reference's own convention (read_fieldize.cpp:94).
+// the normalising mass is the sum of the particle masses, plus 1 for a Gadget
+// snapshot (read_fieldize.cpp:94) and nothing more for a BigFile one
+// (read_fieldize_bigfile.cpp:117): the reference's own conventions.
+#include "bigfile.h"
 #include "gadget2.h"
 #include "genpk_gb300.h"
+
+#include <memory>
 
 #include <getopt.h>
 
@@ -29,6 +36,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -86,6 +94,51 @@ struct Fail : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// A snapshot in either format, as the driver uses it.
+class Source {
+public:
+    explicit Source(const std::string &path)
+    {
+        if (bigfile::Snapshot::is_bigfile(path)) {
+            bf_.reset(new bigfile::Snapshot(path));
+            return;
+        }
+        FILE *f = fopen(path.c_str(), "rb");
+        if (f) {
+            unsigned char sig[8] = {};
+            const size_t got = fread(sig, 1, 8, f);
+            fclose(f);
+            static const unsigned char hdf5[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+            if (got == 8 && memcmp(sig, hdf5, 8) == 0)
+                throw Fail(path + " is an HDF5 snapshot: this build has no HDF5 library");
+        }
+        g2_.reset(new g2::Snapshot(path));
+    }
+    const char *format() const { return bf_ ? "bigfile" : "gadget format-II"; }
+    int num_files() const { return bf_ ? 1 : g2_->num_files(); }
+    int64_t npart(int t) const { return bf_ ? bf_->npart(t) : g2_->npart(t); }
+    double mass(int t) const { return bf_ ? bf_->mass(t) : g2_->mass(t); }
+    double box() const { return bf_ ? bf_->box() : g2_->box(); }
+    double time() const { return bf_ ? bf_->time() : g2_->header().time; }
+    double redshift() const { return bf_ ? 1.0 / bf_->time() - 1.0 : g2_->header().redshift; }
+    double hubble() const { return bf_ ? bf_->hubble() : g2_->header().hubble; }
+    double omega0() const { return bf_ ? bf_->omega0() : g2_->header().omega0; }
+    // Added to each type's normalising mass per read: read_fieldize.cpp:94
+    // (Gadget) adds 1, read_fieldize_bigfile.cpp:117 (BigFile) nothing.
+    double mass_offset() const { return bf_ ? 0.0 : 1.0; }
+    void read(int type, int64_t start, int64_t n, float *pos, float *m) const
+    {
+        if (bf_)
+            bf_->read(type, start, n, pos, m);
+        else
+            g2_->read(type, start, n, pos, m);
+    }
+
+private:
+    std::unique_ptr<g2::Snapshot> g2_;
+    std::unique_ptr<bigfile::Snapshot> bf_;
+};
+
 void check(genpk_ctx *ctx, int status, const char *what)
 {
     if (status != GENPK_OK)
@@ -94,10 +147,9 @@ void check(genpk_ctx *ctx, int status, const char *what)
 }
 
 // Deposit every particle of `type` into grid `field`; adds the normalising
-// mass (particle masses + 1) to *total_mass.  Returns false if the snapshot
-// holds no particle of that type.
-bool read_fieldize(genpk_ctx *ctx, int field, const g2::Snapshot &snap, int type,
-                   double *total_mass)
+// mass (particle masses + the format's offset) to *total_mass.  Returns false
+// if the snapshot holds no particle of that type.
+bool read_fieldize(genpk_ctx *ctx, int field, const Source &snap, int type, double *total_mass)
 {
     const int64_t n = snap.npart(type);
     if (n == 0)
@@ -121,7 +173,7 @@ bool read_fieldize(genpk_ctx *ctx, int field, const g2::Snapshot &snap, int type
                             masses.empty() ? nullptr : masses.data(), mass, parts),
               "genpk_deposit");
     }
-    *total_mass += 1.0;
+    *total_mass += snap.mass_offset();
     return true;
 }
 
@@ -184,22 +236,22 @@ int run(int argc, char **argv)
         usage();
         return 0;
     }
-    const g2::Snapshot snap(infiles);
+    const Source snap(infiles);
     int64_t npart[g2::kTypes];
     for (int t = 0; t < g2::kTypes; t++)
         npart[t] = snap.npart(t);
-    const g2::Header &h = snap.header();
     printf("Boxsize=%g, ", snap.box());
     printf("NPart=(%g,%g,%g,%g,%g,%g)**3\n", cbrt((double)npart[0]), cbrt((double)npart[1]),
            cbrt((double)npart[2]), cbrt((double)npart[3]), cbrt((double)npart[4]),
            cbrt((double)npart[5]));
-    printf("Masses=[%g %g %g ]\n", h.mass[0], h.mass[1], h.mass[2]);
-    printf("redshift=%g, Omega_M=%g\n", h.redshift, h.omega0);
+    printf("Masses=[%g %g %g ]\n", snap.mass(0), snap.mass(1), snap.mass(2));
+    printf("redshift=%g, Omega_M=%g\n", snap.redshift(), snap.omega0());
     if (describe) {
-        printf("files=%d time=%g h=%g\n", snap.num_files(), h.time, h.hubble);
+        printf("format=%s files=%d time=%g h=%g\n", snap.format(), snap.num_files(), snap.time(),
+               snap.hubble());
         for (int t = 0; t < g2::kTypes; t++)
             printf("type %d (%s): npart=%lld mass=%.10g\n", t, type_str(t).c_str(),
-                   (long long)npart[t], h.mass[t]);
+                   (long long)npart[t], snap.mass(t));
         return 0;
     }
 
@@ -243,7 +295,7 @@ int run(int argc, char **argv)
         }
     } else if (!jinfiles.empty()) {
         // each type against the same type of a second snapshot (gen-pk.cpp:240-303)
-        const g2::Snapshot snap2(jinfiles);
+        const Source snap2(jinfiles);
         for (int type = 0; type < g2::kTypes; type++) {
             if (npart[type] == 0)
                 continue;

@@ -174,6 +174,36 @@ __device__ __forceinline__ AxisQ split_q28(float p, float uh, float ul, int dims
     return {fi, (uint32_t)q & (kFracOne - 1u), u, xlu};
 }
 
+// split_q28 where 1 <= |xh| < 2^22, xh = p * uh rounded as split_q28 rounds
+// it, without the wrap into [0, dims): the same cell (before the wrap),
+// fraction, u and xl.  In that range split_q28's near-origin step does not
+// apply and |xl| < 2^22 * 2^-23, so xl * 2^28 needs no clamp.  The caller
+// wraps the (rare) cells outside [0, dims).
+constexpr float kFastSplitMax = 4194304.f;  // 2^22 cells
+
+__device__ __forceinline__ AxisQ split_q28_unwrapped(float p, float xh, float uh, float ul)
+{
+    const float xe = fmaf(p, uh, -xh);
+    const float xl = fmaf(p, ul, xe);
+    const float f = floorf(xh);
+    const float a = __fsub_rn(xh, f);
+    float u = fmaf(-2.f, a, 1.f);
+    const int q = __float2int_rn(a * 268435456.f) + __float2int_rn(xl * 268435456.f);
+    const int carry = q >> kFracBits;
+    u = fmaf(2.f, (float)carry, u);
+    return {(int)f + carry, (uint32_t)q & (kFracOne - 1u), u, xl};
+}
+
+__device__ __forceinline__ int wrap_cell(int fi, int dims)
+{
+    if ((unsigned)fi >= (unsigned)dims) {
+        fi %= dims;
+        if (fi < 0)
+            fi += dims;
+    }
+    return fi;
+}
+
 // The CIC weights of one particle in 2^-s mass units, shared by every deposit
 // path so that they produce identical integer cell sums.  Factors per axis:
 // 2^28 - q (lower cell) and q (upper), so f / 2^28 is the CIC factor; the

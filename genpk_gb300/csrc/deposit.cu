@@ -789,7 +789,8 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
 // cell beside each 28-bit fraction.
 bool deposit_tile_supported(int tx, int ty, int tz)
 {
-    return (tx == 8 && ty == 8 && tz == 8) || (tx == 16 && ty == 16 && tz == 16);
+    return (tx == 8 && ty == 8 && tz == 8) || (tx == 16 && ty == 16 && tz == 8) ||
+           (tx == 16 && ty == 16 && tz == 16);
 }
 
 TileShape deposit_default_tile(int dims, int64_t n)
@@ -817,12 +818,12 @@ bool deposit_shared_hist(const DepositGeom &g)
     return deposit_hist_smem(g) <= 160 * 1024;
 }
 
-int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms)
+int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms, int max_per_sm)
 {
-    int per_sm = 4;
+    int per_sm = std::max(1, max_per_sm);
     if (deposit_shared_hist(g)) {
         const size_t smem = deposit_hist_smem(g) + 1024;
-        per_sm = (int)std::min<size_t>(4, (200 * 1024) / std::max<size_t>(smem, 1));
+        per_sm = (int)std::min<size_t>((size_t)per_sm, (200 * 1024) / std::max<size_t>(smem, 1));
         per_sm = std::max(per_sm, 1);
     }
     const int64_t want = (n + 4095) / 4096;
@@ -903,6 +904,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         return err;
     if (g.tx == 8)
         return launch_tile_kernels<8, 8, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
+    if (g.tz == 8)
+        return launch_tile_kernels<16, 16, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
     return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook, hook_user);
 }
 

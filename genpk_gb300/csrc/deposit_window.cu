@@ -651,24 +651,52 @@ __global__ void __launch_bounds__(kWinThreads, 1)
         for (int j0 = 0; j0 < cnt; j0 += blockDim.x) {
             const int j = j0 + threadIdx.x;
             float x = 0.f, y = 0.f, z = 0.f, m = p.umass;
-            bool valid = j < cnt;
-            if (valid) {
+            if (j < cnt) {
                 x = P[3 * j];
                 y = P[3 * j + 1];
                 z = P[3 * j + 2];
-                // the products split_q28 forms first
-                bool ok = fabsf(__fmul_rn(x, p.uh)) <= kPosLimit &&
-                          fabsf(__fmul_rn(y, p.uh)) <= kPosLimit &&
-                          fabsf(__fmul_rn(z, p.uh)) <= kPosLimit;
-                if (VARMASS) {
+                if (VARMASS)
                     m = M[j];
-                    ok = ok && fabsf(m) <= 3.4028235e38f;
+            }
+            // The products split_q28 forms first.  Particles at 1 <= |x N/L| <
+            // 2^22 cells on every axis (all but those within a cell of the
+            // origin, far outside the box, or invalid) take the split without
+            // its near-origin step and clamp; the others the general split.
+            const float xh = __fmul_rn(x, p.uh), yh = __fmul_rn(y, p.uh), zh = __fmul_rn(z, p.uh);
+            bool fast = j < cnt && fabsf(xh) >= 1.f && fabsf(xh) < kFastSplitMax &&
+                        fabsf(yh) >= 1.f && fabsf(yh) < kFastSplitMax && fabsf(zh) >= 1.f &&
+                        fabsf(zh) < kFastSplitMax;
+            if (VARMASS)
+                fast = fast && fabsf(m) <= 3.4028235e38f;
+            bool valid = fast;
+            AxisQ ax, ay, az;
+            if (fast) {
+                ax = split_q28_unwrapped(x, xh, p.uh, p.ul);
+                ay = split_q28_unwrapped(y, yh, p.uh, p.ul);
+                az = split_q28_unwrapped(z, zh, p.uh, p.ul);
+                // as unsigned values, so that a negative cell reads as out of range
+                if (max((unsigned)ax.cell, max((unsigned)ay.cell, (unsigned)az.cell)) >=
+                    (unsigned)p.dims) {
+                    ax.cell = wrap_cell(ax.cell, p.dims);
+                    ay.cell = wrap_cell(ay.cell, p.dims);
+                    az.cell = wrap_cell(az.cell, p.dims);
                 }
-                if (!ok) {
-                    bad++;
-                    valid = false;
-                    x = y = z = 0.f;
+            } else {
+                valid = j < cnt;
+                if (valid) {
+                    bool ok = fabsf(xh) <= kPosLimit && fabsf(yh) <= kPosLimit &&
+                              fabsf(zh) <= kPosLimit;
+                    if (VARMASS)
+                        ok = ok && fabsf(m) <= 3.4028235e38f;
+                    if (!ok) {
+                        bad++;
+                        valid = false;
+                        x = y = z = 0.f;
+                    }
                 }
+                ax = split_q28(x, p.uh, p.ul, p.dims);
+                ay = split_q28(y, p.uh, p.ul, p.dims);
+                az = split_q28(z, p.uh, p.ul, p.dims);
             }
             unsigned mant = umant;
             int ef = uef;
@@ -681,9 +709,6 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             }
             valid = valid && ef != 0;  // zero or subnormal mass deposits nothing
             const int dsh = max(emax - ef, 0);
-            const AxisQ ax = split_q28(x, p.uh, p.ul, p.dims);
-            const AxisQ ay = split_q28(y, p.uh, p.ul, p.dims);
-            const AxisQ az = split_q28(z, p.uh, p.ul, p.dims);
             if (CORNER && valid) {
                 f2sum v = corner_factor_q(ax, ay, az);
                 if (VARMASS) {

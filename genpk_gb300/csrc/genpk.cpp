@@ -84,7 +84,27 @@ struct genpk_ctx {
     size_t fft_work_size = 0;
 
     // deposit
-    TileShape tile{16, 16, 16};
+    TileShape tile{16, 16, 16};  // sorted engine's tile when fixed by the caller
+    bool tile_fixed = false;     // genpk_set_deposit_tile chose it; else the tuner does
+    // The sorted engine's tuned configurations, by particle-density band and
+    // mass kind (chosen on the first clean pass of that band; see tune_sorted).
+    struct Tuned {
+        int band = 0;
+        bool var = false;
+        TileShape tile{16, 16, 16};
+        int per_sm = 4;
+    };
+    static constexpr int kTuned = 16;
+    Tuned tuned[kTuned];
+    int ntuned = 0;
+    // the latest tuning's trials, and the configuration the latest sorted pass used
+    static constexpr int kMaxTrials = 8;
+    TileShape trial_tile[kMaxTrials];
+    int trial_ctas[kMaxTrials] = {};
+    float trial_ms[kMaxTrials] = {};
+    int ntrials = 0;
+    TileShape last_tile{16, 16, 16};
+    int last_sort_ctas = 0;
     DepositScratch dscr;
     int engine = GENPK_ENGINE_AUTO;   // requested deposit engine
     int last_engine = GENPK_ENGINE_AUTO;  // engine the latest pass used
@@ -285,13 +305,13 @@ int collect_status(genpk_ctx *ctx)
     return GENPK_OK;
 }
 
-DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize)
+DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize, TileShape tile)
 {
     DepositGeom g;
     g.grid = ctx->gg;
-    g.tx = ctx->tile.tx;
-    g.ty = ctx->tile.ty;
-    g.tz = ctx->tile.tz;
+    g.tx = tile.tx;
+    g.ty = tile.ty;
+    g.tz = tile.tz;
     const int n = (int)ctx->dims;
     g.ntx = (n + g.tx - 1) / g.tx;
     g.nty = (n + g.ty - 1) / g.ty;
@@ -304,7 +324,134 @@ DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize)
     return g;
 }
 
+DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize)
+{
+    return deposit_geom(ctx, boxsize, ctx->tile);
+}
+
 int ensure_stage(genpk_ctx *ctx, int64_t need);
+
+// Scratch of one sorted-engine pass of n particles with geometry g.
+int grow_sorted_scratch(genpk_ctx *ctx, const DepositGeom &g, int64_t n, int sort_ctas)
+{
+    DepositScratch &s = ctx->dscr;
+    if (deposit_shared_hist(g)) {
+        GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
+    } else {
+        GENPK_TRY(grow(ctx, &s.cursor, &s.cursor_cap, (size_t)g.ntiles));
+    }
+    GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
+    GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
+    GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
+    size_t nface = 0, nhalo = 0;
+    deposit_scratch_sizes(g, &nface, &nhalo);
+    GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface));
+    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo));
+    size_t mp = (size_t)s.mass_part_cap;
+    GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
+    s.mass_part_cap = (int)mp;
+    return GENPK_OK;
+}
+
+// Particle-density band of a pass: half octaves of particles per cell.
+int density_band(const genpk_ctx *ctx, int64_t n)
+{
+    const double cells = (double)ctx->dims * (double)ctx->dims * (double)ctx->dims;
+    return (int)std::floor(2.0 * std::log2(std::max((double)n, 1.0) / cells));
+}
+
+constexpr int64_t kTuneMinParticles = (int64_t)1 << 16;
+
+// The sorted engine's autotuner.  On the first clean pass of a density band
+// (and mass kind) it runs the pass once per candidate -- tiles 8^3, 16x16x8
+// and 16^3, each with up to 2 and up to 4 sort CTAs per SM -- timed with
+// CUDA events, and keeps the fastest.  Every candidate writes the same grid
+// (the sums are exact), so the trials only cost time: each overwrites the
+// clean grid, and the field's running sums and the error counters are put
+// back before the next.  The chosen candidate then runs as the real pass.
+int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a,
+                const genpk_ctx::Tuned **out)
+{
+    static const TileShape tiles[] = {{8, 8, 8}, {16, 16, 8}, {16, 16, 16}};
+    static const int pers[] = {2, 4};
+    const size_t stash = 0;  // the error counters are kept in the probe buffer meanwhile
+    GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)4));
+    GENPK_CUDA(cudaMemcpyAsync(ctx->d_probe + stash, ctx->d_status, 2 * sizeof(long long),
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+    cudaEvent_t e0, e1;
+    GENPK_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(ctx, GENPK_ERR_CUDA, "tune_sorted: cudaEventCreate failed");
+    }
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } ev{e0, e1};
+    auto reset_field = [&]() -> int {
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + f, 0, sizeof(double), ctx->stream));
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + ctx->nfields + f, 0, sizeof(double),
+                                   ctx->stream));
+        GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + 2 * ctx->nfields + f, 0, sizeof(double),
+                                   ctx->stream));
+        return GENPK_OK;
+    };
+    genpk_ctx::Tuned best;
+    best.band = density_band(ctx, a.n);
+    best.var = a.masses != nullptr;
+    float best_ms = 1e30f;
+    ctx->ntrials = 0;
+    for (const TileShape &t : tiles) {
+        if (!deposit_tile_supported(t.tx, t.ty, t.tz))
+            continue;
+        int last_ctas = -1;
+        for (int per : pers) {
+            const DepositGeom g = deposit_geom(ctx, boxsize, t);
+            const int ctas = deposit_sort_ctas(g, a.n, ctx->num_sms, per);
+            if (ctas == last_ctas)  // capped to the same count: nothing new to try
+                continue;
+            last_ctas = ctas;
+            GENPK_TRY(grow_sorted_scratch(ctx, g, a.n, ctas));
+            GENPK_TRY(reset_field());
+            GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
+            GENPK_CUDA(deposit_pass(g, a, ctx->dscr, ctx->d_status, ctas, ctx->stream,
+                                    &ctx->launches, nullptr, nullptr));
+            GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
+            GENPK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            GENPK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ctx->ntrials < genpk_ctx::kMaxTrials) {
+                ctx->trial_tile[ctx->ntrials] = t;
+                ctx->trial_ctas[ctx->ntrials] = ctas;
+                ctx->trial_ms[ctx->ntrials] = ms;
+                ctx->ntrials++;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.tile = t;
+                best.per_sm = per;
+            }
+        }
+    }
+    GENPK_TRY(reset_field());
+    GENPK_CUDA(cudaMemcpyAsync(ctx->d_status, ctx->d_probe + stash, 2 * sizeof(long long),
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+    genpk_ctx::Tuned &slot = ctx->tuned[ctx->ntuned % genpk_ctx::kTuned];
+    ctx->ntuned++;
+    slot = best;
+    *out = &slot;
+    return GENPK_OK;
+}
+
+const genpk_ctx::Tuned *find_tuned(const genpk_ctx *ctx, int64_t n, bool var)
+{
+    const int band = density_band(ctx, n);
+    const int have = std::min(ctx->ntuned, genpk_ctx::kTuned);
+    for (int i = 0; i < have; i++)
+        if (ctx->tuned[i].band == band && ctx->tuned[i].var == var)
+            return &ctx->tuned[i];
+    return nullptr;
+}
 
 // One deposit pass from device particle arrays, or (host_mapped) from pinned
 // host arrays read in place by the window engine.
@@ -466,23 +613,25 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         if (defer)
             ctx->acc_pending = f;
     } else {
-        const int sort_ctas = deposit_sort_ctas(g, n, ctx->num_sms);
-        if (deposit_shared_hist(g)) {
-            GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, (size_t)sort_ctas * g.ntiles));
-        } else {
-            GENPK_TRY(grow(ctx, &s.cursor, &s.cursor_cap, (size_t)g.ntiles));
+        TileShape tile = ctx->tile;
+        int per_sm = 4;
+        if (!ctx->tile_fixed) {
+            const genpk_ctx::Tuned *t = find_tuned(ctx, n, masses != nullptr);
+            if (!t && a.clean && n >= kTuneMinParticles) {
+                GENPK_TRY(tune_sorted(ctx, f, boxsize, a, &t));
+                stage_event(ctx, "tune");
+            }
+            if (t) {
+                tile = t->tile;
+                per_sm = t->per_sm;
+            }
         }
-        GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)g.ntiles + 1));
-        GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)g.ntiles + 1));
-        GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(n, 1)));
-        size_t nface = 0, nhalo = 0;
-        deposit_scratch_sizes(g, &nface, &nhalo);
-        GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface));
-        GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo));
-        size_t mp = (size_t)s.mass_part_cap;
-        GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)sort_ctas));
-        s.mass_part_cap = (int)mp;
-        GENPK_CUDA(deposit_pass(g, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
+        const DepositGeom gs = deposit_geom(ctx, boxsize, tile);
+        const int sort_ctas = deposit_sort_ctas(gs, n, ctx->num_sms, per_sm);
+        GENPK_TRY(grow_sorted_scratch(ctx, gs, n, sort_ctas));
+        ctx->last_tile = tile;
+        ctx->last_sort_ctas = sort_ctas;
+        GENPK_CUDA(deposit_pass(gs, a, s, ctx->d_status, sort_ctas, ctx->stream, &ctx->launches,
                                 hook, ctx));
     }
     ctx->state[(size_t)f] = F_DENSITY;
@@ -1349,29 +1498,61 @@ int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *ti
 {
     if (!ctx)
         return GENPK_ERR_INVALID;
+    const bool ran = ctx->last_sort_ctas > 0;
+    const TileShape t = ran ? ctx->last_tile : ctx->tile;
     if (tile_x)
-        *tile_x = ctx->tile.tx;
+        *tile_x = t.tx;
     if (tile_y)
-        *tile_y = ctx->tile.ty;
+        *tile_y = t.ty;
     if (tile_z)
-        *tile_z = ctx->tile.tz;
+        *tile_z = t.tz;
     if (sort_ctas) {
-        DepositGeom g = deposit_geom(const_cast<genpk_ctx *>(ctx), 1.0);
-        *sort_ctas = deposit_sort_ctas(g, (int64_t)1 << 30, ctx->num_sms);
+        if (ran) {
+            *sort_ctas = ctx->last_sort_ctas;
+        } else {
+            DepositGeom g = deposit_geom(const_cast<genpk_ctx *>(ctx), 1.0);
+            *sort_ctas = deposit_sort_ctas(g, (int64_t)1 << 30, ctx->num_sms);
+        }
     }
     return GENPK_OK;
+}
+
+int genpk_deposit_trials(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
+                         int *sort_ctas, float *ms, int cap)
+{
+    if (!ctx || cap < 0)
+        return -1;
+    const int k = std::min(cap, ctx->ntrials);
+    for (int i = 0; i < k; i++) {
+        if (tile_x)
+            tile_x[i] = ctx->trial_tile[i].tx;
+        if (tile_y)
+            tile_y[i] = ctx->trial_tile[i].ty;
+        if (tile_z)
+            tile_z[i] = ctx->trial_tile[i].tz;
+        if (sort_ctas)
+            sort_ctas[i] = ctx->trial_ctas[i];
+        if (ms)
+            ms[i] = ctx->trial_ms[i];
+    }
+    return k;
 }
 
 int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z)
 {
     if (!ctx)
         return GENPK_ERR_INVALID;
-    if (!deposit_tile_supported(tile_x, tile_y, tile_z))
+    const bool automatic = tile_x == 0 && tile_y == 0 && tile_z == 0;
+    if (!automatic && !deposit_tile_supported(tile_x, tile_y, tile_z))
         return fail(ctx, GENPK_ERR_UNSUPPORTED, "deposit tile shape not instantiated");
     GENPK_TRY(flush_pending(ctx));
-    const TileShape old = ctx->tile;
-    ctx->tile = TileShape{tile_x, tile_y, tile_z};
-    (void)old;
+    if (automatic) {
+        ctx->tile_fixed = false;
+        ctx->tile = deposit_default_tile((int)ctx->dims, 0);
+    } else {
+        ctx->tile_fixed = true;
+        ctx->tile = TileShape{tile_x, tile_y, tile_z};
+    }
     return GENPK_OK;
 }
 

@@ -51,6 +51,8 @@ ABI = {
     "genpk_last_deposit_engine": (ctypes.c_int, [c_void_p]),
     "genpk_set_fft_mode": (ctypes.c_int, [c_void_p, ctypes.c_int]),
     "genpk_inject_copy_timeout": (ctypes.c_int, [c_void_p, ctypes.c_int64, ctypes.c_int64]),
+    "genpk_deposit_trials": (ctypes.c_int, [c_void_p, c_i32p, c_i32p, c_i32p, c_i32p, c_f32p,
+                                            ctypes.c_int]),
     "genpk_power_noalloc": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_double, c_void_p, c_i32p,
                                            c_f64p, c_void_p]),

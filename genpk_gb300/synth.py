@@ -193,3 +193,63 @@ def write_gadget2(base: str, pos_by_type: dict, masses_by_type: dict, box: float
             if mass_parts:
                 block(f, "MASS", b"".join(m.tobytes() for m in mass_parts))
     return paths
+
+
+def write_bigfile(root: str, pos_by_type: dict, masses_by_type: dict, box: float,
+                  time: float = 1.0, hubble: float = 0.7, omega0: float = 0.3,
+                  nfiles: int = 2, pos_dtype: str = "<f8", mass_dtype: str = "<f4"):
+    """Write a BigFile snapshot directory (the layout MP-Gadget writes): a
+    "Header" block whose attr-v2 file holds TotNumPart, MassTable, Time,
+    HubbleParam, Omega0 and BoxSize, and per type the columns
+    "<type>/Position" (pos_dtype x 3) and, where masses_by_type[type] is an
+    array (MassTable 0), "<type>/Mass" (mass_dtype), each split over nfiles
+    data files named 000000, 000001, ...
+
+    pos_by_type: {type: float32 [n, 3]}.  masses_by_type: {type: float (the
+    MassTable entry) or float32 [n]}."""
+    import os
+
+    def attr_line(name, dtype, values):
+        arr = np.asarray(values, dtype=np.dtype(dtype))
+        human = " ".join(repr(v) for v in arr.tolist())
+        return f"{name} {dtype} {arr.size} {arr.tobytes().hex().upper()} #HUMANE [ {human} ]\n"
+
+    def column(name, data, dtype, nmemb):
+        d = os.path.join(root, name)
+        os.makedirs(d, exist_ok=True)
+        arr = np.ascontiguousarray(np.asarray(data).reshape(-1, nmemb).astype(np.dtype(dtype)))
+        n = len(arr)
+        edges = [n * k // nfiles for k in range(nfiles + 1)]
+        lines = [f"DTYPE: {dtype}\n", f"NMEMB: {nmemb}\n", f"NFILE: {nfiles}\n"]
+        for f in range(nfiles):
+            part = arr[edges[f]:edges[f + 1]]
+            with open(os.path.join(d, f"{f:06X}"), "wb") as fh:
+                fh.write(part.tobytes())
+            lines.append(f"{f:06X}: {len(part)} : 0 : 0\n")
+        with open(os.path.join(d, "header"), "w") as fh:
+            fh.writelines(lines)
+        with open(os.path.join(d, "attr-v2"), "w") as fh:
+            fh.write("")
+
+    ntypes = 6
+    counts = [len(pos_by_type.get(t, ())) for t in range(ntypes)]
+    table = [0.0 if not np.isscalar(masses_by_type.get(t, 0.0)) else float(masses_by_type.get(t, 0.0))
+             for t in range(ntypes)]
+    hdir = os.path.join(root, "Header")
+    os.makedirs(hdir, exist_ok=True)
+    with open(os.path.join(hdir, "header"), "w") as fh:
+        fh.write("DTYPE: <f8\nNMEMB: 1\nNFILE: 0\n")
+    with open(os.path.join(hdir, "attr-v2"), "w") as fh:
+        fh.write(attr_line("TotNumPart", "<u8", counts))
+        fh.write(attr_line("MassTable", "<f8", table))
+        fh.write(attr_line("Time", "<f8", [time]))
+        fh.write(attr_line("HubbleParam", "<f8", [hubble]))
+        fh.write(attr_line("Omega0", "<f8", [omega0]))
+        fh.write(attr_line("BoxSize", "<f8", [box]))
+    for t in range(ntypes):
+        if counts[t] == 0:
+            continue
+        column(f"{t}/Position", pos_by_type[t], pos_dtype, 3)
+        if table[t] == 0.0:
+            column(f"{t}/Mass", masses_by_type[t], mass_dtype, 1)
+    return root

@@ -166,12 +166,25 @@ int genpk_stage_times(const genpk_ctx *ctx, const char **names, float *ms, int c
 /* Start a new timing window (see genpk_stage_times). */
 int genpk_timing_reset(genpk_ctx *ctx);
 
-/* Deposit tuning actually in use (tile edge lengths and sort CTA count). */
+/* The sorted engine's configuration: that of its latest pass (tile edge
+ * lengths and sort CTA count), or before any pass the default. */
 int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
                          int *sort_ctas);
 
-/* Choose the deposit tile of the sorted engine (cells per edge; supported:
- * 8^3 and 16^3).  The sorted engine's grid does not depend on it. */
+/* The sorted engine's autotuner: on its first clean pass of each particle
+ * density band (half octaves of particles per cell) and mass kind, the pass
+ * runs once per candidate -- tiles 8^3, 16x16x8 and 16^3, each with up to 2
+ * and up to 4 sort CTAs per SM -- timed with CUDA events, and the fastest is
+ * kept for that band.  Every candidate writes the same grid.  This returns
+ * the latest tuning's trials (at most cap, the number written): tile edges,
+ * sort CTA count and milliseconds each.  No reference counterpart (the
+ * reference's deposit has no tunable). */
+int genpk_deposit_trials(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
+                         int *sort_ctas, float *ms, int cap);
+
+/* Fix the deposit tile of the sorted engine (cells per edge; supported:
+ * 8^3, 16x16x8 and 16^3), which turns its autotuner off; (0, 0, 0) turns it
+ * back on.  The sorted engine's grid does not depend on the tile. */
 int genpk_set_deposit_tile(genpk_ctx *ctx, int tile_x, int tile_y, int tile_z);
 
 /* Deposit engines.  All three add the same integer CIC weights exactly (64-bit

@@ -186,7 +186,7 @@ def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
     masses = np.linspace(0.2, 3.0, len(pos)).astype(np.float32)
     ref = O.deposit(pos, box, dims, masses, 0.0)
     grids = []
-    for tile in [(8, 8, 8), (16, 16, 16)]:
+    for tile in [(8, 8, 8), (16, 16, 8), (16, 16, 16)]:
         with gp.Context(dims, 16) as ctx:
             ctx.set_engine(gp.api.ENGINE_SORTED)
             ctx.set_tile(*tile)
@@ -668,6 +668,37 @@ def test_accumulator_cleared_by_the_transform(gp, engine):
     pr, cr, _ = O.pk(np.concatenate([boxes[0], boxes[1]]), box, dims, nrbins, None, 1.0,
                      m_norm=2 * m)
     bins_close(got[0], pr, cr)
+
+
+def test_sorted_engine_autotuner(gp):
+    """The sorted engine's first clean pass of a density band tries every
+    tile and sort-CTA candidate, keeps the fastest, and the grid equals the
+    one a fixed tile gives, bit for bit; the next pass of that band reuses the
+    choice (no new trials); fixing a tile turns the tuner off."""
+    from genpk_gb300 import synth
+    dims, box = 128, 1000.0
+    pos = synth.uniform(2_000_000, box, seed=31)
+    with gp.Context(dims, 16) as ctx:
+        ctx.set_engine(gp.api.ENGINE_SORTED)
+        ctx.deposit(0, box, pos, None, 1.0)
+        tuned = ctx.read_field(0)
+        trials = ctx.deposit_trials()
+        assert len(trials) >= 3 and all(ms > 0 for _, _, ms in trials)
+        assert {t for t, _, _ in trials} == {(8, 8, 8), (16, 16, 8), (16, 16, 16)}
+        best = min(trials, key=lambda r: r[2])
+        cfg = ctx.deposit_config()
+        assert cfg["tile"] == best[0] and cfg["sort_ctas"] == best[1]
+        ctx.zero(0)
+        ctx.deposit(0, box, pos[:1_900_000], None, 1.0)  # the same band: no new tuning
+        ctx.read_field(0)
+        assert ctx.deposit_trials() == trials
+        for tile in ((16, 16, 16), (8, 8, 8)):
+            ctx.set_tile(*tile)
+            ctx.zero(0)
+            ctx.deposit(0, box, pos, None, 1.0)
+            assert np.array_equal(ctx.read_field(0), tuned)
+            assert ctx.deposit_config()["tile"] == tile
+    grid_close(tuned, O.deposit(pos, box, dims, None, 1.0))
 
 
 @pytest.mark.parametrize("engine", ["sorted", "window", "stream"])
