@@ -80,6 +80,11 @@ struct genpk_ctx {
     float2 *d_xtw = nullptr;        // x-pass twiddles, null when unsupported
     cufftHandle c2r = 0;
     bool c2r_made = false;
+    // N = 1024: batched 2-D C2C over the kz planes of a kz-major spectrum
+    cufftHandle c2c_kz = 0;
+    bool c2c_kz_made = false;
+    // per field: its spectrum is kz-major, S[kz][x][y] (the N = 1024 transform)
+    std::vector<bool> kzmajor;
     void *fft_work = nullptr;
     size_t fft_work_size = 0;
 
@@ -457,6 +462,7 @@ const genpk_ctx::Tuned *find_tuned(const genpk_ctx *ctx, int64_t n, bool var)
 // host arrays read in place by the window engine.
 int flush_acc(genpk_ctx *ctx);
 bool use_xfft(const genpk_ctx *ctx);
+bool use_kz(const genpk_ctx *ctx);
 
 int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const float *masses,
                 float mass, int64_t n, bool host_mapped = false)
@@ -602,7 +608,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         s.mass_part_cap = (int)mp;
         // A clean grid headed for the own z/y/x transform keeps the pass in the
         // accumulator: the z pass converts it on the fly.
-        const bool defer = a.clean && use_xfft(ctx);
+        const bool defer = a.clean && (use_xfft(ctx) || use_kz(ctx));
         // (a pass that fails part-way must not leave the accumulator marked clear)
         const bool acc_zero = ctx->acc_zero;
         ctx->acc_zero = false;
@@ -726,6 +732,8 @@ int finish_plan(genpk_ctx *ctx, cufftHandle h, cufftResult made, size_t ws, cons
             GENPK_CUFFT(cufftSetWorkArea(kv.second, ctx->fft_work));
         if (ctx->c2r_made)
             GENPK_CUFFT(cufftSetWorkArea(ctx->c2r, ctx->fft_work));
+        if (ctx->c2c_kz_made)
+            GENPK_CUFFT(cufftSetWorkArea(ctx->c2c_kz, ctx->fft_work));
     }
     GENPK_CUFFT(cufftSetWorkArea(h, ctx->fft_work));
     return GENPK_OK;
@@ -814,15 +822,71 @@ int make_c2r(genpk_ctx *ctx)
 // passes) replace cuFFT's x axis for the supported sizes.
 bool use_xfft(const genpk_ctx *ctx)
 {
-    return ctx->fft_mode == GENPK_FFT_AUTO && ctx->d_xtw != nullptr;
+    return ctx->fft_mode == GENPK_FFT_AUTO && ctx->d_xtw != nullptr &&
+           xfft_supported((int)ctx->dims);
+}
+
+// N = 1024: a single field pending in the accumulator is transformed by the
+// kz-major z pass (reads and clears the accumulator) and one batched 2-D C2C
+// over the kz planes, and binned in kz-major order.
+bool use_kz(const genpk_ctx *ctx)
+{
+    return ctx->fft_mode == GENPK_FFT_AUTO && ctx->d_xtw != nullptr &&
+           zfft_kz_supported((int)ctx->dims);
+}
+
+// Batched forward 2-D C2C over the N/2+1 contiguous N x N planes of a
+// kz-major spectrum, in place.
+int make_c2c_kz(genpk_ctx *ctx)
+{
+    if (ctx->c2c_kz_made)
+        return GENPK_OK;
+    const long long n = ctx->dims;
+    long long dims2[2] = {n, n};
+    cufftHandle h;
+    GENPK_CUFFT(cufftCreate(&h));
+    GENPK_CUFFT(cufftSetAutoAllocation(h, 0));
+    size_t ws = 0;
+    cufftResult r = cufftMakePlanMany64(h, 2, dims2, dims2, 1, n * n, dims2, 1, n * n, CUFFT_C2C,
+                                        (long long)ctx->gg.hc, &ws);
+    GENPK_TRY(finish_plan(ctx, h, r, ws, "c2c kz planes"));
+    ctx->c2c_kz = h;
+    ctx->c2c_kz_made = true;
+    return GENPK_OK;
+}
+
+// A kz-major spectrum back to the in-place r2c layout every other consumer
+// reads (cross spectra with other fields, the adjoint).  Out of place through
+// the window engine's accumulator, which then needs a clear before its next
+// pass.
+int ensure_row_major(genpk_ctx *ctx, int f)
+{
+    if (!ctx->kzmajor[(size_t)f])
+        return GENPK_OK;
+    float2 *tmp = reinterpret_cast<float2 *>(ctx->dscr.win_acc);
+    if (!tmp)
+        return fail(ctx, GENPK_ERR_STATE, "kz-major spectrum without its work buffer");
+    GENPK_CUDA(kz_to_rows(ctx->gg, reinterpret_cast<const float2 *>(grid_of(ctx, f)), tmp,
+                          ctx->stream, &ctx->launches));
+    GENPK_CUDA(cudaMemcpyAsync(grid_of(ctx, f), tmp, sizeof(float) * (size_t)ctx->gg.nfloat,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->acc_zero = false;
+    ctx->acc_spent = false;
+    ctx->kzmajor[(size_t)f] = false;
+    stage_event(ctx, "kz_to_rows");
+    return GENPK_OK;
 }
 
 // fused: when not null and its field is transformed alone, the x-pass also
-// bins that field's auto spectrum into fused->bin (fused->done := true).
+// bins that field's auto spectrum into fused->bin (fused->done := true); at
+// N = 1024 (kz_ctas > 0) the field pending in the accumulator takes the
+// kz-major transform and is binned in that order (fused->done := true).
 struct FusedAuto {
     int field;
     XfftBin bin;
     bool done;
+    int kz_ctas = 0, kz_warps = 0;
+    size_t kz_smem = 0;
 };
 
 // Bring every field in `need` to SPECTRUM form: pending deposits first, then
@@ -846,6 +910,33 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
     }
     std::sort(todo.begin(), todo.end());
     todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
+    if (fused && fused->kz_ctas > 0 && use_kz(ctx) && todo.size() == 1 &&
+        todo[0] == fused->field && ctx->acc_pending == fused->field && ctx->dscr.win_acc) {
+        const int f = fused->field;
+        timing_touch(ctx);
+        stage_event(ctx, "host");
+        float *grid = grid_of(ctx, f);
+        GENPK_CUDA(zfft_kz_pass(ctx->gg, grid, ctx->dscr.win_acc, ctx->d_xtw, ctx->d_status,
+                                ctx->stream, &ctx->launches));
+        ctx->acc_pending = -1;
+        ctx->acc_spent = false;
+        ctx->acc_zero = true;  // the z pass cleared what it read
+        stage_event(ctx, "zfft_kz");
+        GENPK_TRY(make_c2c_kz(ctx));
+        GENPK_CUFFT(cufftExecC2C(ctx->c2c_kz, (cufftComplex *)grid, (cufftComplex *)grid,
+                                 CUFFT_FORWARD));
+        stage_event(ctx, "fft2d_kz");
+        GENPK_CUDA(bin_spectrum_kz(ctx->gg, ctx->tables, ctx->bdev,
+                                   reinterpret_cast<const float2 *>(grid), fused->bin.corner,
+                                   fused->bin.partial, fused->kz_ctas, fused->kz_warps,
+                                   fused->kz_smem, ctx->stream, &ctx->launches));
+        stage_event(ctx, "bin_kz");
+        ctx->state[(size_t)f] = F_SPECTRUM;
+        ctx->corner_valid[(size_t)f] = true;
+        ctx->kzmajor[(size_t)f] = true;
+        fused->done = true;
+        return GENPK_OK;
+    }
     const bool planes = use_xfft(ctx);
     // A field whose pass is still in the accumulator is transformed on its own
     // by the own z pass (which reads the accumulator) and y pass; other runs of
@@ -943,13 +1034,45 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         fa.bin.partial = ctx->d_partial;
         fused = &fa;
     }
+    const bool auto1 = np == 1 && pairs[0] == pairs[1] && pair_mass[0] == pair_mass[1];
+    if (!fused && auto1 && use_kz(ctx) && ctx->state[(size_t)pairs[0]] == F_DENSITY) {
+        const int ctas = bin_kz_ctas(ctx->gg, nrb, ctx->num_sms, &fa.kz_warps, &fa.kz_smem);
+        if (ctas > 0) {
+            GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * nrb));
+            fa.field = pairs[0];
+            fa.kz_ctas = ctas;
+            fa.bin.corner = ctx->d_field_mass + 2 * ctx->nfields + pairs[0];
+            fa.bin.partial = ctx->d_partial;
+            fused = &fa;
+        }
+    }
     GENPK_TRY(to_spectrum(ctx, fields, fused));
     std::sort(fields.begin(), fields.end());
     fields.erase(std::unique(fields.begin(), fields.end()), fields.end());
+    if (!fa.done && auto1 && ctx->kzmajor[(size_t)pairs[0]]) {
+        // re-binning a kz-major spectrum: the same kernel as its transform's
+        int warps = 0;
+        size_t smem = 0;
+        const int ctas = bin_kz_ctas(ctx->gg, nrb, ctx->num_sms, &warps, &smem);
+        if (ctas > 0) {
+            GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * nrb));
+            const int f = pairs[0];
+            GENPK_CUDA(bin_spectrum_kz(
+                ctx->gg, ctx->tables, ctx->bdev, reinterpret_cast<const float2 *>(grid_of(ctx, f)),
+                ctx->corner_valid[(size_t)f] ? ctx->d_field_mass + 2 * ctx->nfields + f : nullptr,
+                ctx->d_partial, ctas, warps, smem, ctx->stream, &ctx->launches));
+            fa.kz_ctas = ctas;
+            fa.done = true;
+        }
+    }
+    if (!fa.done)  // every other binning reads the in-place r2c layout
+        for (int f : fields)
+            GENPK_TRY(ensure_row_major(ctx, f));
     if (fa.done) {
-        GENPK_CUDA(finalize_power(ctx->d_partial, xfft_bin_ctas(ctx->dims, 1, ctx->num_sms), nrb,
-                                  ctx->bdev.count, pair_mass[0], pair_mass[1], ctx->d_power,
-                                  ctx->stream, &ctx->launches));
+        const int ctas =
+            fa.kz_ctas > 0 ? fa.kz_ctas : xfft_bin_ctas(ctx->dims, 1, ctx->num_sms);
+        GENPK_CUDA(finalize_power(ctx->d_partial, ctas, nrb, ctx->bdev.count, pair_mass[0],
+                                  pair_mass[1], ctx->d_power, ctx->stream, &ctx->launches));
     }
     // Pairs are binned in groups whose fields fit one kernel instantiation.
     int q0 = fa.done ? np : 0;
@@ -1066,6 +1189,8 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
         cufftDestroy(kv.second);
     if (ctx->c2r_made)
         cufftDestroy(ctx->c2r);
+    if (ctx->c2c_kz_made)
+        cufftDestroy(ctx->c2c_kz);
     cudaFree(ctx->fft_work);
     cudaFree(ctx->grids);
     cudaFree(ctx->d_field_mass);
@@ -1153,7 +1278,7 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     CREATE_CUDA(cudaMemcpy(ctx->bdev.count, cnt.data(), sizeof(double) * nrbins,
                            cudaMemcpyHostToDevice));
     CREATE_CUDA(cudaMalloc(&ctx->d_gcoef, sizeof(float) * nrbins));
-    if (xfft_supported((int)dims)) {
+    if (xfft_supported((int)dims) || zfft_kz_supported((int)dims)) {
         std::vector<float> tw;
         xfft_twiddles((int)dims, &tw);
         CREATE_CUDA(cudaMalloc(&ctx->d_xtw, sizeof(float) * tw.size()));
@@ -1166,6 +1291,7 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     ctx->auto_mass.assign((size_t)nfields, 0.0);
     ctx->auto_valid.assign((size_t)nfields, false);
     ctx->corner_valid.assign((size_t)nfields, false);
+    ctx->kzmajor.assign((size_t)nfields, false);
     ctx->tile = deposit_default_tile((int)dims, 0);
     (void)rc;
     *out = ctx;
@@ -1184,6 +1310,7 @@ int genpk_zero(genpk_ctx *ctx, int field)
     }
     ctx->state[(size_t)field] = F_CLEAN;
     ctx->auto_valid[(size_t)field] = false;
+    ctx->kzmajor[(size_t)field] = false;
     GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
     GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + ctx->nfields + field, 0, sizeof(double),
                                ctx->stream));
@@ -1313,6 +1440,7 @@ int genpk_load_spectrum(genpk_ctx *ctx, int field, const double *spectrum)
     ctx->state[(size_t)field] = F_SPECTRUM;
     ctx->auto_valid[(size_t)field] = false;
     ctx->corner_valid[(size_t)field] = false;
+    ctx->kzmajor[(size_t)field] = false;
     return GENPK_OK;
 }
 
@@ -1403,6 +1531,7 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     std::vector<double> pw((size_t)nrb);
     if (recompute || !have) {
         ctx->state[(size_t)field] = F_CLEAN;
+        ctx->kzmajor[(size_t)field] = false;
         GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + field, 0, sizeof(double), ctx->stream));
         GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass + ctx->nfields + field, 0, sizeof(double),
                                    ctx->stream));
@@ -1413,6 +1542,7 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     } else {
         pw = ctx->auto_power[(size_t)field];
     }
+    GENPK_TRY(ensure_row_major(ctx, field));
     timing_touch(ctx);
     stage_event(ctx, "host");
     // dL/dM and the per-bin coefficients G_b = 2 g_b / (M^2 C_b).

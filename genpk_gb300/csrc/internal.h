@@ -227,6 +227,18 @@ cudaError_t zfft_pass(const GridGeom &g, float *grid, const unsigned long long *
                       cudaStream_t stream, int64_t *launches);
 cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw, int num_sms,
                       cudaStream_t stream, int64_t *launches);
+// The kz-major z pass (xfft.cu, N = 1024): the length-N r2c along z of one
+// grid read from the window engine's accumulator (converted as its conversion
+// pass does) and written kz-major, S[kz][x][y] (N/2+1 planes of N x N complex
+// values in the grid's memory), for a batched 2-D C2C over the planes to
+// finish; the accumulator rows read are cleared.
+bool zfft_kz_supported(int dims);
+// kz-major spectrum -> the in-place r2c layout, out of place (`rows` holds
+// N * N * (N/2+1) complex values and must not overlap kz_major).
+cudaError_t kz_to_rows(const GridGeom &g, const float2 *kz_major, float2 *rows,
+                       cudaStream_t stream, int64_t *launches);
+cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, unsigned long long *acc, const float2 *tw,
+                         const DeviceStatus *dstat, cudaStream_t stream, int64_t *launches);
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
                       const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
                       DeviceStatus *dstat, cudaStream_t stream, int64_t *launches);
@@ -285,6 +297,13 @@ int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms
 cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const double *count,
                            double ma, double mb, double *out, cudaStream_t stream,
                            int64_t *launches);
+// Binning of one kz-major spectrum S[kz][x][y] (after zfft_kz_pass and the
+// batched 2-D C2C): the auto pair's partial sums, one FP64 histogram per CTA
+// (partial: ctas * nrbins doubles), for finalize_power.
+int bin_kz_ctas(const GridGeom &g, int nrbins, int num_sms, int *warps, size_t *smem);
+cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                            const float2 *spec, const double *corner, double *partial, int ctas,
+                            int warps, size_t smem, cudaStream_t stream, int64_t *launches);
 cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
                         const BinLaunch &l, double *partial, double *out_power, int ctas,
                         int warps, size_t smem, cudaStream_t stream, int64_t *launches);

@@ -320,6 +320,180 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ---- binning of a kz-major spectrum (the N = 1024 transform) --------------
+//
+// The spectrum is stored as S[kz][x][y] (kz = 0..N/2, planes of N x N complex
+// values; xfft.cu k_zfft_t1024 + a batched 2-D C2C).  Each (kz, x) row of N
+// modes along y is binned as two half-rows along which |k|^2 grows: y = 0..N/2
+// (ky = y) and y = N-1 down to N/2+1 (ky = y - N, |ky| = 1..N/2-1).  The rest
+// is k_bin's: lane runs of RP modes with a running FP32 sum and the next
+// threshold in a register, a segmented warp scan of the lanes' open sums,
+// FP64 promotion every kPromoteRows half-rows, one FP64 partial histogram per
+// CTA, k_bin_finalize.  Per mode: weight c = 1 on the kz = 0 and kz = N/2
+// planes, 2 elsewhere; value c * p^4 |F|^2 with p = (iw_x iw_y) iw_z, the
+// float product order of k_bin; (0,0,0) skipped; the exact corner value at
+// (N/2, N/2, N/2).  One spectrum (its auto pair).
+struct BinKzParams {
+    const float2 *f;
+    const double *corner;  // exact (N/2, N/2, N/2) value, or null
+    int dims, half, hc;
+    int nrbins;
+    float bpu_half;
+    int rp;     // modes per lane per piece (odd)
+    int warps;  // warps per CTA
+};
+
+// Half-row r (physical row r/2 = kz * N + x, half r & 1): piece loads.
+__device__ __forceinline__ void load_piece_kz(const BinKzParams &p, int64_t r, int pb, int lane,
+                                              float2 (&v)[kMaxRP])
+{
+    const int h = (int)(r & 1);
+    const int len = h ? p.half - 1 : p.hc;
+    const float2 *row = p.f + (size_t)(r >> 1) * (size_t)p.dims;
+#pragma unroll
+    for (int t = 0; t < kMaxRP; t++) {
+        const int m = pb + t * 32 + lane;
+        const bool in = t < p.rp && m < len;
+        const int y = h ? p.dims - 1 - m : m;
+        v[t] = in ? __ldg(row + y) : make_float2(0.f, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_bin_kz(BinKzParams p, const uint32_t *__restrict__ thr_g, const float *__restrict__ iw_g,
+             double *__restrict__ partial)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nrb = p.nrbins;
+    const int rp = p.rp, piece = 32 * rp;
+    const BinLayout L = bin_layout(nrb, p.hc, 1, 1, rp);
+    uint32_t *thr = (uint32_t *)smem;
+    float *iwy = (float *)(smem + L.izc);  // [dims]: 4 dims bytes fit the layout's 8 hc
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned char *wbase = smem + L.warps + L.per_warp * wid;
+    double *whist = (double *)(wbase + L.whist);
+    float *rhist = (float *)(wbase + L.rhist);
+    float2 *buf = (float2 *)(wbase + L.buf);
+
+    for (int i = threadIdx.x; i <= nrb; i += blockDim.x)
+        thr[i] = thr_g[i];
+    for (int i = threadIdx.x; i < p.dims; i += blockDim.x)
+        iwy[i] = iw_g[i];
+    for (int i = lane; i < nrb; i += 32) {
+        whist[i] = 0.0;
+        rhist[i] = 0.f;
+    }
+    __syncthreads();
+
+    const int64_t nrows = (int64_t)2 * p.hc * p.dims;  // half-rows
+    const int64_t gw = (int64_t)blockIdx.x * p.warps + wid;
+    const int64_t nw = (int64_t)gridDim.x * p.warps;
+    const int64_t per = (nrows + nw - 1) / nw;
+    const int64_t r_begin = min(nrows, gw * per), r_end = min(nrows, r_begin + per);
+    int bmin = nrb, bmax = -1;
+    int rows_since = 0;
+    float2 v[kMaxRP];
+    if (r_begin < r_end)
+        load_piece_kz(p, r_begin, 0, lane, v);
+    for (int64_t r = r_begin; r < r_end; r++) {
+        const int h = (int)(r & 1);
+        const int64_t pr = r >> 1;
+        const int kz = (int)(pr / p.dims), x = (int)(pr - (int64_t)kz * p.dims);
+        const int kx = kval_dev(x, p.dims);
+        const uint32_t r2 = (uint32_t)(kx * kx + kz * kz);
+        const float cw = (kz == 0 || kz == p.half) ? 1.f : 2.f;
+        const float iwx = iwy[x], iwz = iwy[kz];
+        const int len = h ? p.half - 1 : p.hc;
+        const bool origin = kz == 0 && x == 0 && h == 0;
+        const bool corner = p.corner && kz == p.half && x == p.half && h == 0;
+        for (int pb = 0; pb < len; pb += piece) {
+            if (origin && pb == 0 && lane == 0)
+                v[0] = make_float2(0.f, 0.f);
+            if (corner) {
+#pragma unroll
+                for (int t = 0; t < kMaxRP; t++)
+                    if (pb + t * 32 + lane == p.half)
+                        v[t] = make_float2((float)*p.corner, 0.f);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < kMaxRP; t++)
+                if (t < rp)
+                    buf[t * 32 + lane] = v[t];
+            __syncwarp();
+            if (pb + piece < len)
+                load_piece_kz(p, r, pb + piece, lane, v);
+            else if (r + 1 < r_end)
+                load_piece_kz(p, r + 1, 0, lane, v);
+
+            const int m0 = pb + lane * rp;
+            int cb = nrb;
+            float acc = 0.f;
+            if (m0 < len) {
+                int ky = m0 + h;  // |ky| of the run's first mode
+                uint32_t kk2 = r2 + (uint32_t)(ky * ky);
+                cb = bin_lookup(kk2, thr, nrb, p.bpu_half);
+                bmin = min(bmin, cb);
+                uint32_t nx = thr[cb + 1];
+                const int lim = min(rp, len - m0);
+                const float2 *bl = buf + lane * rp;
+                for (int t = 0; t < lim; t++) {
+                    if (kk2 >= nx) {
+                        atomicAdd(&rhist[cb], acc);
+                        acc = 0.f;
+                        do {
+                            cb++;
+                            nx = thr[cb + 1];
+                        } while (kk2 >= nx);
+                    }
+                    const int m = m0 + t;
+                    const int y = h ? p.dims - 1 - m : m;
+                    const float pz = (iwx * iwy[y]) * iwz;
+                    const float p2 = pz * pz;
+                    const float w = cw * (p2 * p2);
+                    const float2 fv = bl[t];
+                    acc = fmaf(w, fmaf(fv.x, fv.x, fv.y * fv.y), acc);
+                    kk2 += (uint32_t)(2 * ky + 1);
+                    ky++;
+                }
+                bmax = max(bmax, cb);
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int ku = __shfl_up_sync(0xffffffffu, cb, o);
+                const float xo = __shfl_up_sync(0xffffffffu, acc, o);
+                if (lane >= o && ku == cb)
+                    acc += xo;
+            }
+            const int kd = __shfl_down_sync(0xffffffffu, cb, 1);
+            if (cb < nrb && (lane == 31 || kd != cb))
+                rhist[cb] += acc;
+            __syncwarp();
+        }
+        if (++rows_since == kPromoteRows || r + 1 == r_end) {
+            rows_since = 0;
+            const int lo = (int)__reduce_min_sync(0xffffffffu, (unsigned)bmin);
+            const int hi = (int)__reduce_max_sync(0xffffffffu, (unsigned)(bmax + 1)) - 1;
+            for (int b = lo + lane; b <= hi; b += 32) {
+                whist[b] += (double)rhist[b];
+                rhist[b] = 0.f;
+            }
+            __syncwarp();
+            bmin = nrb;
+            bmax = -1;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nrb; k += blockDim.x) {
+        double sum = 0.0;
+        for (int w = 0; w < p.warps; w++) {
+            const double *wh = (const double *)(smem + L.warps + L.per_warp * w + L.whist);
+            sum += wh[k];
+        }
+        partial[(size_t)blockIdx.x * nrb + k] = sum;
+    }
+}
+
 struct NormParams {
     double ma[kMaxBinPairs], mb[kMaxBinPairs];
     int src[kMaxBinPairs];  // the partials' pair slot of each reported pair
@@ -470,6 +644,44 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
     const int k = l.npairs * t.nrbins;
     k_bin_finalize<<<k, kFinalizeThreads, 0, stream>>>(partial, ctas, t.nrbins, d.count, mn,
                                                         out_power);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+int bin_kz_ctas(const GridGeom &g, int nrbins, int num_sms, int *warps, size_t *smem)
+{
+    int w = 8;
+    while (w > 1 && bin_smem(nrbins, g.hc, 1, 1, w) > 200 * 1024)
+        w /= 2;
+    const size_t sm = bin_smem(nrbins, g.hc, 1, 1, w);
+    if (sm > 220 * 1024 || (size_t)4 * g.dims > align16(sizeof(float2) * g.hc))
+        return 0;
+    *warps = w;
+    *smem = sm;
+    const int per_sm = std::max(1, std::min(2048 / (32 * w), (int)((220 * 1024) / sm)));
+    const int64_t rows = (int64_t)2 * g.hc * g.dims;
+    const int64_t want = (rows + w - 1) / w;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms * per_sm, want));
+}
+
+cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                            const float2 *spec, const double *corner, double *partial, int ctas,
+                            int warps, size_t smem, cudaStream_t stream, int64_t *launches)
+{
+    BinKzParams p;
+    p.f = spec;
+    p.corner = (g.dims % 2 == 0) ? corner : nullptr;
+    p.dims = g.dims;
+    p.half = g.half;
+    p.hc = g.hc;
+    p.nrbins = t.nrbins;
+    p.bpu_half = (float)(0.5 * t.binsperunit);
+    p.rp = bin_rp(g.hc);
+    p.warps = warps;
+    cudaError_t err;
+    if ((err = ensure_dynamic_smem(k_bin_kz, smem)) != cudaSuccess)
+        return err;
+    k_bin_kz<<<ctas, 32 * warps, smem, stream>>>(p, d.thr, d.iw, partial);
     (*launches)++;
     return cudaGetLastError();
 }
