@@ -538,7 +538,7 @@ def main():
     t_pass = sum(v for k, v in stages.items() if k.startswith(("dep_", "win_", "stream_"))) * 1e-3
     # binning time: the fused x-axis FFT + binning kernel when it ran (it also
     # does the last FFT pass, so this overstates the binning time), else k_bin
-    t_bin = (stages.get("xfft_bin", 0.0) + stages.get("bin", 0.0)) * 1e-3
+    t_bin = (stages.get("xfft_bin", 0.0) + stages.get("bin_kz", 0.0) + stages.get("bin", 0.0)) * 1e-3
     if engine in ("window", "stream"):
         stage = "win_deposit" if engine == "window" else "stream_deposit"
         t_k = stages.get(stage, 0.0) * 1e-3
@@ -558,6 +558,7 @@ def main():
                         "/ mean CUDA-event time of the kernel; peak = measured copy bandwidth",
                 "deposit_pass": {"ms": t_pass * 1e3, "frac": b_dep / t_pass / 1e9 / peak},
                 "bin": {"kernel": "k_xfft (x-axis FFT pass + binning)" if "xfft_bin" in stages
+                        else "k_bin_kz (kz-major binning)" if "bin_kz" in stages
                         else "k_bin", "achieved": ach_bin,
                         "frac": (ach_bin / peak) if ach_bin else None, "algorithmic_bytes": b_bin},
                 "deposit_plus_bin_frac": (b_dep + b_bin) / (t_pass + t_bin) / 1e9 / peak}

@@ -94,6 +94,54 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The mode gradient on a kz-major spectrum S[kz][x][y] (the N = 1024
+// transform), in place: one warp per (kz, x) row, lanes over y; the same
+// H = G_b V_m (c_m / mult_m) F_m as k_mode_gradient, p = (iw_x iw_y) iw_kz.
+__global__ void __launch_bounds__(256)
+    k_mode_gradient_kz(ModeGradParams p, float2 *__restrict__ spec,
+                       const uint32_t *__restrict__ thr_g, const float *__restrict__ iw,
+                       const float *__restrict__ gcoef)
+{
+    extern __shared__ uint32_t thr[];
+    for (int i = threadIdx.x; i <= p.nrbins; i += blockDim.x)
+        thr[i] = thr_g[i];
+    __syncthreads();
+    const bool even = (p.dims & 1) == 0;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nrows = (int64_t)p.hc * p.dims;
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows;
+         row += nwarps) {
+        const int kz = (int)(row / p.dims), x = (int)(row - (int64_t)kz * p.dims);
+        const int kx = kval_adj(x, p.dims);
+        const uint32_t r2 = (uint32_t)(kx * kx + kz * kz);
+        const float iwx = __ldg(iw + x), iwz = __ldg(iw + kz);
+        const bool edge = (kz == 0 || kz == p.half);
+        const bool selfconj = (kz == 0) || (even && kz == p.half);
+        const float cm = edge ? 1.f : 2.f, mult = selfconj ? 1.f : 2.f;
+        float2 *rp = spec + (size_t)row * (size_t)p.dims;
+        for (int y = lane; y < p.dims; y += 32) {
+            const int ky = kval_adj(y, p.dims);
+            const uint32_t kk2 = r2 + (uint32_t)(ky * ky);
+            float2 h = make_float2(0.f, 0.f);
+            if (kk2 != 0) {
+                int b = (int)(p.bpu_half * __logf((float)kk2));
+                b = max(0, min(p.nrbins - 1, b));
+                while (b + 1 < p.nrbins && kk2 >= thr[b + 1])
+                    b++;
+                while (b > 0 && kk2 < thr[b])
+                    b--;
+                const float pz = (iwx * __ldg(iw + y)) * iwz;
+                const float p2 = pz * pz;
+                const float sc = __ldg(gcoef + b) * (p2 * p2) * (cm / mult);
+                const float2 f = rp[y];
+                h = make_float2(sc * f.x, sc * f.y);
+            }
+            rp[y] = h;
+        }
+    }
+}
+
 struct GatherParams {
     int dims;
     int64_t plane;
@@ -176,6 +224,25 @@ __global__ void __launch_bounds__(256)
 }
 
 }  // namespace
+
+cudaError_t adjoint_mode_gradient_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                                     float2 *spec, const float *gcoef_dev, int num_sms,
+                                     cudaStream_t stream, int64_t *launches)
+{
+    ModeGradParams p;
+    p.dims = g.dims;
+    p.hc = g.hc;
+    p.half = g.half;
+    p.nrbins = t.nrbins;
+    p.bpu_half = (float)(0.5 * t.binsperunit);
+    const size_t smem = sizeof(uint32_t) * (size_t)(t.nrbins + 1);
+    cudaError_t err;
+    if ((err = ensure_dynamic_smem(k_mode_gradient_kz, smem)) != cudaSuccess)
+        return err;
+    k_mode_gradient_kz<<<num_sms * 8, 256, smem, stream>>>(p, spec, d.thr, d.iw, gcoef_dev);
+    (*launches)++;
+    return cudaGetLastError();
+}
 
 cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, const BinDevice &d,
                                        float2 *spec, const float *gcoef_dev, cudaStream_t stream,

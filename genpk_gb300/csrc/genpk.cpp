@@ -96,6 +96,8 @@ struct genpk_ctx {
     struct Tuned {
         int band = 0;
         bool var = false;
+        bool with_stream = false;         // the stream engine was among the trials
+        int engine = GENPK_ENGINE_SORTED;  // the faster: SORTED (tile, per_sm) or STREAM
         TileShape tile{16, 16, 16};
         int per_sm = 4;
     };
@@ -367,14 +369,20 @@ int density_band(const genpk_ctx *ctx, int64_t n)
 
 constexpr int64_t kTuneMinParticles = (int64_t)1 << 16;
 
-// The sorted engine's autotuner.  On the first clean pass of a density band
-// (and mass kind) it runs the pass once per candidate -- tiles 8^3, 16x16x8
-// and 16^3, each with up to 2 and up to 4 sort CTAs per SM -- timed with
-// CUDA events, and keeps the fastest.  Every candidate writes the same grid
-// (the sums are exact), so the trials only cost time: each overwrites the
-// clean grid, and the field's running sums and the error counters are put
-// back before the next.  The chosen candidate then runs as the real pass.
-int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a,
+// The deposit autotuner for particle orders without spatial coherence.  On
+// the first clean pass of a density band (and mass kind) it runs the pass once
+// per candidate -- the sorted engine with tiles 8^3, 16x16x8 and 16^3, each
+// with up to 2 and up to 4 sort CTAs per SM, and (with_stream) the stream
+// engine, whose reductions go straight to the accumulator -- timed with CUDA
+// events, and keeps the fastest.  (Measured on uniform random particles: the
+// stream engine is 2-2.6x faster at 1e6 particles, where the sort's fixed
+// costs dominate, about even at 3e7 on a 128^3 grid, and 1.75x slower at 3e7
+// on a 256^3 grid, whose accumulator exceeds the L2.)  Every candidate writes
+// the same grid (the sums are exact), so the trials only cost time: each
+// overwrites the clean grid, and the field's running sums and the error
+// counters are put back before the next.  The chosen candidate then runs as
+// the real pass.
+int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, bool with_stream,
                 const genpk_ctx::Tuned **out)
 {
     static const TileShape tiles[] = {{8, 8, 8}, {16, 16, 8}, {16, 16, 16}};
@@ -404,8 +412,42 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a,
     genpk_ctx::Tuned best;
     best.band = density_band(ctx, a.n);
     best.var = a.masses != nullptr;
+    best.with_stream = with_stream;
     float best_ms = 1e30f;
     ctx->ntrials = 0;
+    if (with_stream && !ctx->dscr.win_acc) {
+        GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (cudaMalloc(&ctx->dscr.win_acc,
+                       sizeof(unsigned long long) * (size_t)ctx->gg.nfloat) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->dscr.win_acc = nullptr;  // no room: the sorted engine only
+        }
+    }
+    if (with_stream && ctx->dscr.win_acc) {
+        const DepositGeom g = deposit_geom(ctx, boxsize);
+        const int mass_ctas = ctx->num_sms * 4;
+        size_t mp = (size_t)ctx->dscr.mass_part_cap;
+        GENPK_TRY(grow(ctx, &ctx->dscr.mass_part, &mp, (size_t)mass_ctas));
+        ctx->dscr.mass_part_cap = (int)mp;
+        GENPK_TRY(reset_field());
+        GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
+        GENPK_CUDA(deposit_window_pass(g, a, kStreamChunk, true, ctx->dscr.mass_part, mass_ctas,
+                                       ctx->dscr.win_acc, false, false, ctx->num_sms,
+                                       ctx->d_status, ctx->stream, &ctx->launches, nullptr,
+                                       nullptr));
+        GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
+        GENPK_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        GENPK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ctx->acc_zero = false;  // it holds the trial's sums
+        ctx->acc_spent = true;
+        ctx->trial_tile[0] = TileShape{0, 0, 0};
+        ctx->trial_ctas[0] = 0;
+        ctx->trial_ms[0] = ms;
+        ctx->ntrials = 1;
+        best_ms = ms;
+        best.engine = GENPK_ENGINE_STREAM;
+    }
     for (const TileShape &t : tiles) {
         if (!deposit_tile_supported(t.tx, t.ty, t.tz))
             continue;
@@ -433,6 +475,7 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a,
             }
             if (ms < best_ms) {
                 best_ms = ms;
+                best.engine = GENPK_ENGINE_SORTED;
                 best.tile = t;
                 best.per_sm = per;
             }
@@ -448,12 +491,13 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a,
     return GENPK_OK;
 }
 
-const genpk_ctx::Tuned *find_tuned(const genpk_ctx *ctx, int64_t n, bool var)
+const genpk_ctx::Tuned *find_tuned(const genpk_ctx *ctx, int64_t n, bool var, bool with_stream)
 {
     const int band = density_band(ctx, n);
     const int have = std::min(ctx->ntuned, genpk_ctx::kTuned);
     for (int i = 0; i < have; i++)
-        if (ctx->tuned[i].band == band && ctx->tuned[i].var == var)
+        if (ctx->tuned[i].band == band && ctx->tuned[i].var == var &&
+            ctx->tuned[i].with_stream == with_stream)
             return &ctx->tuned[i];
     return nullptr;
 }
@@ -549,6 +593,20 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     }
     if (engine == GENPK_ENGINE_AUTO)  // too few particles to judge the order
         engine = GENPK_ENGINE_SORTED;
+    // An automatic pass without spatial coherence: the tuner picks between the
+    // sorted engine (and its tile) and the stream engine, per density band.
+    const genpk_ctx::Tuned *tuned = nullptr;
+    const bool auto_sorted = ctx->engine == GENPK_ENGINE_AUTO && engine == GENPK_ENGINE_SORTED &&
+                             !ctx->tile_fixed && !host_mapped;
+    if (auto_sorted || (engine == GENPK_ENGINE_SORTED && !ctx->tile_fixed && !host_mapped)) {
+        tuned = find_tuned(ctx, n, masses != nullptr, auto_sorted);
+        if (!tuned && a.clean && n >= kTuneMinParticles) {
+            GENPK_TRY(tune_sorted(ctx, f, boxsize, a, auto_sorted, &tuned));
+            stage_event(ctx, "tune");
+        }
+        if (tuned && tuned->engine == GENPK_ENGINE_STREAM)
+            engine = GENPK_ENGINE_STREAM;
+    }
     if (ctx->engine == GENPK_ENGINE_AUTO && !reuse) {
         if (pos != ctx->stage_pos) {
             genpk_ctx::Choice &c = ctx->choices[ctx->choice_next];
@@ -621,16 +679,9 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     } else {
         TileShape tile = ctx->tile;
         int per_sm = 4;
-        if (!ctx->tile_fixed) {
-            const genpk_ctx::Tuned *t = find_tuned(ctx, n, masses != nullptr);
-            if (!t && a.clean && n >= kTuneMinParticles) {
-                GENPK_TRY(tune_sorted(ctx, f, boxsize, a, &t));
-                stage_event(ctx, "tune");
-            }
-            if (t) {
-                tile = t->tile;
-                per_sm = t->per_sm;
-            }
+        if (tuned) {
+            tile = tuned->tile;
+            per_sm = tuned->per_sm;
         }
         const DepositGeom gs = deposit_geom(ctx, boxsize, tile);
         const int sort_ctas = deposit_sort_ctas(gs, n, ctx->num_sms, per_sm);
@@ -919,17 +970,21 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
         GENPK_CUDA(zfft_kz_pass(ctx->gg, grid, ctx->dscr.win_acc, ctx->d_xtw, ctx->d_status,
                                 ctx->stream, &ctx->launches));
         ctx->acc_pending = -1;
-        ctx->acc_spent = false;
-        ctx->acc_zero = true;  // the z pass cleared what it read
+        ctx->acc_spent = true;
         stage_event(ctx, "zfft_kz");
         GENPK_TRY(make_c2c_kz(ctx));
         GENPK_CUFFT(cufftExecC2C(ctx->c2c_kz, (cufftComplex *)grid, (cufftComplex *)grid,
                                  CUFFT_FORWARD));
         stage_event(ctx, "fft2d_kz");
+        // the binning also clears the accumulator the z pass has read
         GENPK_CUDA(bin_spectrum_kz(ctx->gg, ctx->tables, ctx->bdev,
                                    reinterpret_cast<const float2 *>(grid), fused->bin.corner,
                                    fused->bin.partial, fused->kz_ctas, fused->kz_warps,
-                                   fused->kz_smem, ctx->stream, &ctx->launches));
+                                   fused->kz_smem, ctx->dscr.win_acc,
+                                   (int64_t)sizeof(unsigned long long) * ctx->gg.nfloat,
+                                   ctx->stream, &ctx->launches));
+        ctx->acc_spent = false;
+        ctx->acc_zero = true;
         stage_event(ctx, "bin_kz");
         ctx->state[(size_t)f] = F_SPECTRUM;
         ctx->corner_valid[(size_t)f] = true;
@@ -1060,7 +1115,7 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
             GENPK_CUDA(bin_spectrum_kz(
                 ctx->gg, ctx->tables, ctx->bdev, reinterpret_cast<const float2 *>(grid_of(ctx, f)),
                 ctx->corner_valid[(size_t)f] ? ctx->d_field_mass + 2 * ctx->nfields + f : nullptr,
-                ctx->d_partial, ctas, warps, smem, ctx->stream, &ctx->launches));
+                ctx->d_partial, ctas, warps, smem, nullptr, 0, ctx->stream, &ctx->launches));
             fa.kz_ctas = ctas;
             fa.done = true;
         }
@@ -1542,7 +1597,10 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     } else {
         pw = ctx->auto_power[(size_t)field];
     }
-    GENPK_TRY(ensure_row_major(ctx, field));
+    // A kz-major spectrum (N = 1024) takes the kz-major adjoint below.
+    const bool kz = ctx->kzmajor[(size_t)field] && use_kz(ctx) && ctx->dscr.win_acc;
+    if (!kz)
+        GENPK_TRY(ensure_row_major(ctx, field));
     timing_touch(ctx);
     stage_event(ctx, "host");
     // dL/dM and the per-bin coefficients G_b = 2 g_b / (M^2 C_b).
@@ -1559,7 +1617,27 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     GENPK_CUDA(cudaMemcpyAsync(ctx->d_gcoef, gcoef.data(), sizeof(float) * nrb,
                                cudaMemcpyHostToDevice, ctx->stream));
     float *g = grid_of(ctx, field);
-    if (use_xfft(ctx) && xfft_grad_supported((int)ctx->dims, nrb)) {
+    if (kz) {
+        // mode gradient in place, the inverse (x, y) transform per kz plane,
+        // then the inverse z pass into the accumulator's memory (it cannot run
+        // in place), which the gather reads; the accumulator needs a clear
+        // before its next pass.
+        GENPK_CUDA(adjoint_mode_gradient_kz(ctx->gg, ctx->tables, ctx->bdev, (float2 *)g,
+                                            ctx->d_gcoef, ctx->num_sms, ctx->stream,
+                                            &ctx->launches));
+        stage_event(ctx, "adj_modes_kz");
+        GENPK_TRY(make_c2c_kz(ctx));
+        GENPK_CUFFT(cufftExecC2C(ctx->c2c_kz, (cufftComplex *)g, (cufftComplex *)g,
+                                 CUFFT_INVERSE));
+        stage_event(ctx, "adj_fft2d_kz");
+        float *gbuf = reinterpret_cast<float *>(ctx->dscr.win_acc);
+        GENPK_CUDA(zifft_kz_pass(ctx->gg, g, gbuf, ctx->d_xtw, ctx->stream, &ctx->launches));
+        ctx->acc_zero = false;
+        ctx->acc_spent = false;
+        ctx->kzmajor[(size_t)field] = false;
+        g = gbuf;
+        stage_event(ctx, "adj_c2r");
+    } else if (use_xfft(ctx) && xfft_grad_supported((int)ctx->dims, nrb)) {
         // mode gradient fused into the inverse x pass, then the (y, z) C2R per x-plane
         XfftGrad xg;
         xg.nrbins = nrb;
@@ -1582,7 +1660,8 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
     }
     ctx->state[(size_t)field] = F_GRADIENT;
     ctx->auto_valid[(size_t)field] = false;
-    stage_event(ctx, "adj_c2r");
+    if (!kz)
+        stage_event(ctx, "adj_c2r");
     const DepositGeom dg = deposit_geom(ctx, boxsize);
     GENPK_CUDA(adjoint_gather(ctx->gg, dg.units_hi, dg.units_lo, g, dpos, dmass, (float)mass, n,
                               dgpos, dgmass, (float)dldm, ctx->stream, &ctx->launches));

@@ -231,13 +231,13 @@ cudaError_t yfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 
 // grid read from the window engine's accumulator (converted as its conversion
 // pass does) and written kz-major, S[kz][x][y] (N/2+1 planes of N x N complex
 // values in the grid's memory), for a batched 2-D C2C over the planes to
-// finish; the accumulator rows read are cleared.
+// finish.
 bool zfft_kz_supported(int dims);
 // kz-major spectrum -> the in-place r2c layout, out of place (`rows` holds
 // N * N * (N/2+1) complex values and must not overlap kz_major).
 cudaError_t kz_to_rows(const GridGeom &g, const float2 *kz_major, float2 *rows,
                        cudaStream_t stream, int64_t *launches);
-cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, unsigned long long *acc, const float2 *tw,
+cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, const unsigned long long *acc, const float2 *tw,
                          const DeviceStatus *dstat, cudaStream_t stream, int64_t *launches);
 cudaError_t xfft_pass(const GridGeom &g, float *grids, int nbatch, const float2 *tw,
                       const XfftBin *bin, void *zero, int64_t zero_bytes, int num_sms,
@@ -299,11 +299,15 @@ cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const do
                            int64_t *launches);
 // Binning of one kz-major spectrum S[kz][x][y] (after zfft_kz_pass and the
 // batched 2-D C2C): the auto pair's partial sums, one FP64 histogram per CTA
-// (partial: ctas * nrbins doubles), for finalize_power.
+// (partial: ctas * nrbins doubles), for finalize_power.  When `zero` is not
+// null the pass also stores zeros over zero_bytes (a multiple of 16) there,
+// spread over its half-rows: the accumulator's clear for the next deposit
+// pass, in HBM bandwidth the binning leaves idle.
 int bin_kz_ctas(const GridGeom &g, int nrbins, int num_sms, int *warps, size_t *smem);
 cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
                             const float2 *spec, const double *corner, double *partial, int ctas,
-                            int warps, size_t smem, cudaStream_t stream, int64_t *launches);
+                            int warps, size_t smem, void *zero, int64_t zero_bytes,
+                            cudaStream_t stream, int64_t *launches);
 cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
                         const BinLaunch &l, double *partial, double *out_power, int ctas,
                         int warps, size_t smem, cudaStream_t stream, int64_t *launches);
@@ -317,6 +321,17 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
 cudaError_t adjoint_mode_gradient_coef(const GridGeom &g, const BinTables &t, const BinDevice &d,
                                        float2 *spec, const float *gcoef_dev, cudaStream_t stream,
                                        int64_t *launches);
+
+// The same on a kz-major spectrum S[kz][x][y] (the N = 1024 transform).
+cudaError_t adjoint_mode_gradient_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
+                                     float2 *spec, const float *gcoef_dev, int num_sms,
+                                     cudaStream_t stream, int64_t *launches);
+// The adjoint's inverse z pass for N = 1024 (xfft.cu): from the kz-major array
+// left by the mode gradient and an inverse batched 2-D C2C over the kz planes,
+// the unnormalised C2R along z of every row, written to `out` in the padded
+// row layout (out must not overlap kz_major).
+cudaError_t zifft_kz_pass(const GridGeom &g, const float *kz_major, float *out, const float2 *tw,
+                          cudaStream_t stream, int64_t *launches);
 
 // CIC gather of the real gradient grid: grad_pos[n][3], grad_mass[n] (optional).
 cudaError_t adjoint_gather(const GridGeom &g, float units_hi, float units_lo, const float *grid,

@@ -341,6 +341,9 @@ struct BinKzParams {
     float bpu_half;
     int rp;     // modes per lane per piece (odd)
     int warps;  // warps per CTA
+    uint4 *zero;          // region to clear (16-byte units), or null
+    int64_t zero_units;
+    int64_t zero_per_row; // units cleared per half-row
 };
 
 // Half-row r (physical row r/2 = kz * N + x, half r & 1): piece loads.
@@ -406,6 +409,12 @@ __global__ void __launch_bounds__(256)
         const int len = h ? p.half - 1 : p.hc;
         const bool origin = kz == 0 && x == 0 && h == 0;
         const bool corner = p.corner && kz == p.half && x == p.half && h == 0;
+        if (p.zero) {  // this half-row's share of the clear (nothing waits on it)
+            const int64_t a0 = r * p.zero_per_row;
+            const int64_t e0 = min(a0 + p.zero_per_row, p.zero_units);
+            for (int64_t u = a0 + lane; u < e0; u += 32)
+                __stcs(p.zero + u, make_uint4(0u, 0u, 0u, 0u));
+        }
         for (int pb = 0; pb < len; pb += piece) {
             if (origin && pb == 0 && lane == 0)
                 v[0] = make_float2(0.f, 0.f);
@@ -666,7 +675,8 @@ int bin_kz_ctas(const GridGeom &g, int nrbins, int num_sms, int *warps, size_t *
 
 cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
                             const float2 *spec, const double *corner, double *partial, int ctas,
-                            int warps, size_t smem, cudaStream_t stream, int64_t *launches)
+                            int warps, size_t smem, void *zero, int64_t zero_bytes,
+                            cudaStream_t stream, int64_t *launches)
 {
     BinKzParams p;
     p.f = spec;
@@ -678,6 +688,10 @@ cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevi
     p.bpu_half = (float)(0.5 * t.binsperunit);
     p.rp = bin_rp(g.hc);
     p.warps = warps;
+    p.zero = reinterpret_cast<uint4 *>(zero);
+    p.zero_units = zero ? zero_bytes / 16 : 0;
+    const int64_t half_rows = (int64_t)2 * g.hc * g.dims;
+    p.zero_per_row = (p.zero_units + half_rows - 1) / half_rows;
     cudaError_t err;
     if ((err = ensure_dynamic_smem(k_bin_kz, smem)) != cudaSuccess)
         return err;

@@ -832,8 +832,7 @@ __global__ void __launch_bounds__(kZThreads)
 //      the lane pair, so that lane (k1, q) holds Z[k1 + 16 (ki + 16 q)];
 //   4. X[k] = E[k] + W_N^k O[k], k = 0..M, into a [kz][row] shared buffer;
 //   5. the CTA's rows leave as runs of kTRows consecutive y per kz.
-// The accumulator rows read are cleared (streaming stores after the reads),
-// so the next deposit pass needs no clear of its own.
+// The accumulator is left as it is: the kz-major binning pass clears it.
 constexpr int kTRows = 8;
 constexpr int kTThreads = kTRows * 32;
 
@@ -863,7 +862,7 @@ __device__ __forceinline__ void dft16(float2 *v)
 }
 
 __global__ void __launch_bounds__(kTThreads)
-    k_zfft_t1024(unsigned long long *acc, float2 *__restrict__ spec, int row_floats,
+    k_zfft_t1024(const unsigned long long *__restrict__ acc, float2 *__restrict__ spec, int row_floats,
                  const float2 *__restrict__ tw, const DeviceStatus *__restrict__ st)
 {
     constexpr int N = 1024, M = N / 2, R = M / 32, HC = N / 2 + 1;
@@ -876,7 +875,8 @@ __global__ void __launch_bounds__(kTThreads)
     const long long mean = st->mean_fixed;
     const float inv_scale = ldexpf(1.f, -st->fx_shift);
 
-    longlong2 *src = reinterpret_cast<longlong2 *>(acc + (size_t)(row0 + wid) * (size_t)row_floats);
+    const longlong2 *src =
+        reinterpret_cast<const longlong2 *>(acc + (size_t)(row0 + wid) * (size_t)row_floats);
     longlong2 a[R];
 #pragma unroll
     for (int m = 0; m < R; m++)
@@ -886,9 +886,6 @@ __global__ void __launch_bounds__(kTThreads)
     for (int m = 0; m < R; m++)
         v[m] = make_float2(i64_to_f32_rn(a[m].x - mean) * inv_scale,
                            i64_to_f32_rn(a[m].y - mean) * inv_scale);
-#pragma unroll
-    for (int m = 0; m < R; m++)  // the next deposit pass starts from zeros
-        __stcs(src + lane + 32 * m, make_longlong2(0, 0));
 
     dft16(v);
 #pragma unroll
@@ -933,6 +930,82 @@ __global__ void __launch_bounds__(kTThreads)
     for (int e = threadIdx.x; e < HC * kTRows; e += kTThreads) {
         const int kz = e / kTRows, r = e - kz * kTRows;
         spec[((size_t)kz * N + (size_t)x) * N + (size_t)(y0 + r)] = tb[kz * (kTRows + 1) + r];
+    }
+}
+
+// The adjoint's inverse z pass for N = 1024 (the transpose of k_zfft_t1024's
+// job): after the mode gradient and an inverse batched 2-D C2C over the kz
+// planes, the kz-major array holds, for every row (x, y), the N/2+1 values
+// X[kz] whose unnormalised C2R along z is that row of dL/drho.  One CTA takes
+// kTRows consecutive rows: their X[kz] come in as runs of kTRows consecutive y
+// per kz into a [kz][row] shared buffer; then per row (one warp)
+//   Z[k] = (X[k] + conj X[M-k]) + i W_N^{-k} (X[k] - conj X[M-k]),  k < M,
+// (Im X[0] and Im X[M] dropped, as a real transform drops them), and the
+// unnormalised inverse M-point DFT of Z, as conj(DFT(conj Z)) with the
+// forward pass's structure, gives x[2n] + i x[2n+1] = z[n]: the real row,
+// written to `out` in the padded row layout (row_floats floats per row).
+__global__ void __launch_bounds__(kTThreads)
+    k_zifft_t1024(const float2 *__restrict__ spec, float *__restrict__ out, int row_floats,
+                  const float2 *__restrict__ tw)
+{
+    constexpr int N = 1024, M = N / 2, R = M / 32, HC = N / 2 + 1;
+    extern __shared__ __align__(16) unsigned char ts[];
+    float2 *zx = reinterpret_cast<float2 *>(ts) + (threadIdx.x >> 5) * (M + M / 32);
+    float2 *tb = reinterpret_cast<float2 *>(ts) + kTRows * (M + M / 32);  // [HC][kTRows + 1]
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t row0 = (int64_t)blockIdx.x * kTRows;
+    const int x = (int)(row0 / N), y0 = (int)(row0 - (int64_t)x * N);
+    for (int e = threadIdx.x; e < HC * kTRows; e += kTThreads) {
+        const int kz = e / kTRows, r = e - kz * kTRows;
+        tb[kz * (kTRows + 1) + r] = spec[((size_t)kz * N + (size_t)x) * N + (size_t)(y0 + r)];
+    }
+    __syncthreads();
+    float2 v[R];
+#pragma unroll
+    for (int m = 0; m < R; m++) {
+        const int k = lane + 32 * m;
+        float2 a = tb[k * (kTRows + 1) + wid], b = tb[(M - k) * (kTRows + 1) + wid];
+        if (k == 0) {
+            a.y = 0.f;
+            b.y = 0.f;
+        }
+        const float2 s = make_float2(a.x + b.x, a.y - b.y);  // X[k] + conj X[M-k]
+        const float2 d = make_float2(a.x - b.x, a.y + b.y);  // X[k] - conj X[M-k]
+        const float2 w = __ldg(tw + k);
+        const float2 wd = cmul(make_float2(w.x, -w.y), d);   // W_N^{-k} d
+        v[m] = make_float2(s.x - wd.y, -(s.y + wd.x));       // conj(s + i wd)
+    }
+    dft16(v);
+#pragma unroll
+    for (int k1 = 1; k1 < R; k1++)
+        v[k1] = cmul(v[k1], __ldg(tw + ((2 * lane * k1) & (N - 1))));
+#pragma unroll
+    for (int k1 = 0; k1 < R; k1++)
+        zx[zpad(k1 * 32 + lane)] = v[k1];
+    __syncwarp();
+    const int k1g = lane >> 1, q = lane & 1;
+#pragma unroll
+    for (int i = 0; i < R; i++)
+        v[i] = zx[zpad(k1g * 32 + q + 2 * i)];
+    __syncwarp();
+    dft16(v);
+    if (q) {
+#pragma unroll
+        for (int ki = 1; ki < R; ki++)
+            v[ki] = cmul(v[ki], __ldg(tw + ((N / 32) * ki)));
+    }
+#pragma unroll
+    for (int ki = 0; ki < R; ki++)
+        v[ki] = dif_shfl(v[ki], 1, q != 0, make_float2(1.f, 0.f));
+#pragma unroll
+    for (int ki = 0; ki < R; ki++)
+        zx[zpad(k1g + 16 * (ki + 16 * q))] = make_float2(v[ki].x, -v[ki].y);  // conj: z[n]
+    __syncwarp();
+    float2 *orow = reinterpret_cast<float2 *>(out + (size_t)(row0 + wid) * (size_t)row_floats);
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const int nn = lane + 32 * j;
+        orow[nn] = zx[zpad(nn)];
     }
 }
 
@@ -1242,7 +1315,7 @@ bool zfft_kz_supported(int dims)
     return dims == 1024;
 }
 
-cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, unsigned long long *acc, const float2 *tw,
+cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, const unsigned long long *acc, const float2 *tw,
                          const DeviceStatus *dstat, cudaStream_t stream, int64_t *launches)
 {
     if (g.dims != 1024)
@@ -1255,6 +1328,23 @@ cudaError_t zfft_kz_pass(const GridGeom &g, float *grid, unsigned long long *acc
     const int64_t nrows = (int64_t)g.dims * g.dims;
     k_zfft_t1024<<<(unsigned)(nrows / kTRows), kTThreads, smem, stream>>>(
         acc, reinterpret_cast<float2 *>(grid), g.row, tw, dstat);
+    (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t zifft_kz_pass(const GridGeom &g, const float *kz_major, float *out, const float2 *tw,
+                          cudaStream_t stream, int64_t *launches)
+{
+    if (g.dims != 1024)
+        return cudaErrorNotSupported;
+    constexpr int M = 512, HC = 513;
+    const size_t smem = sizeof(float2) * ((size_t)kTRows * (M + M / 32) + (size_t)HC * (kTRows + 1));
+    cudaError_t err;
+    if ((err = ensure_dynamic_smem(k_zifft_t1024, smem)) != cudaSuccess)
+        return err;
+    const int64_t nrows = (int64_t)g.dims * g.dims;
+    k_zifft_t1024<<<(unsigned)(nrows / kTRows), kTThreads, smem, stream>>>(
+        reinterpret_cast<const float2 *>(kz_major), out, g.row, tw);
     (*launches)++;
     return cudaGetLastError();
 }

@@ -171,14 +171,17 @@ int genpk_timing_reset(genpk_ctx *ctx);
 int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
                          int *sort_ctas);
 
-/* The sorted engine's autotuner: on its first clean pass of each particle
- * density band (half octaves of particles per cell) and mass kind, the pass
- * runs once per candidate -- tiles 8^3, 16x16x8 and 16^3, each with up to 2
- * and up to 4 sort CTAs per SM -- timed with CUDA events, and the fastest is
- * kept for that band.  Every candidate writes the same grid.  This returns
- * the latest tuning's trials (at most cap, the number written): tile edges,
- * sort CTA count and milliseconds each.  No reference counterpart (the
- * reference's deposit has no tunable). */
+/* The deposit autotuner, for passes whose particle order has no spatial
+ * coherence: on the first clean pass of each particle density band (half
+ * octaves of particles per cell) and mass kind, the pass runs once per
+ * candidate -- the sorted engine with tiles 8^3, 16x16x8 and 16^3, each with
+ * up to 2 and up to 4 sort CTAs per SM, and, when the engine is automatic,
+ * the stream engine -- timed with CUDA events, and the fastest is kept for
+ * that band.  Every candidate writes the same grid.  This returns the latest
+ * tuning's trials (at most cap, the number written): tile edges (0 x 0 x 0
+ * for the stream engine), sort CTA count (0 for the stream engine) and
+ * milliseconds each.  No reference counterpart (the reference's deposit has
+ * no tunable). */
 int genpk_deposit_trials(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *tile_z,
                          int *sort_ctas, float *ms, int cap);
 

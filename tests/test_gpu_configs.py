@@ -262,11 +262,12 @@ def test_differentiable_pk_256_central_finite_differences(gp):
 
 def test_kz_major_transform_1024(gp):
     """The N = 1024 transform: a field pending in the accumulator goes through
-    the kz-major z pass (which clears the accumulator), one batched 2-D C2C
-    over the kz planes and the kz-major binning.  256^3 lattice particles on
-    the 1024^3 grid: its auto spectrum, binning the kept spectrum again, a
-    cross spectrum with a second field (which reads the spectrum back in the
-    in-place r2c layout) and the adjoint, against the FP64 oracle.  The 3-D
+    the kz-major z pass, one batched 2-D C2C over the kz planes and the
+    kz-major binning (which clears the accumulator).  256^3 lattice particles
+    on the 1024^3 grid: its auto spectrum, binning the kept spectrum again, the
+    kz-major adjoint from the kept spectrum (mode gradient, inverse 2-D C2C,
+    inverse z pass), and a cross spectrum with a second field (which reads the
+    spectrum back in the in-place r2c layout), against the FP64 oracle.  The 3-D
     cuFFT R2C path on the same particles agrees to 5e-5 (its lowest bin is
     1.8e-5 from the oracle on this sparse field, 1/64 particle per cell;
     the kz-major transform stays within 1e-5)."""
@@ -288,14 +289,20 @@ def test_kz_major_transform_1024(gp):
             p, c, k = ctx.power(0, 0, m, m)
             st = ctx.stage_times()
             again, _, _ = ctx.power(0, 0, m, m)
+            ctx.timing_reset()
+            gpos = ctx.adjoint(0, box, pos, g, m, mass=1.0)[0].cpu().numpy()  # kept spectrum
+            sta = ctx.stage_times()
+            ctx.zero(0)
+            ctx.deposit(0, box, pos, None, 1.0)
+            ctx.power(0, 0, m, m)
             ctx.deposit(1, box, other, None, 1.0)
             cross, _, _ = ctx.power(0, 1, m, m)
             auto_after, _, _ = ctx.power(0, 0, m, m)
-            gpos = ctx.adjoint(0, box, pos, g, m, mass=1.0)[0].cpu().numpy()
-            res[mode] = (p, c, again, cross, auto_after, gpos, st)
-    pk, ck, again, cross, auto_after, gk, st = res[gp.api.FFT_AUTO]
-    p3, c3, _, _, _, _, st3 = res[gp.api.FFT_CUFFT3D]
+            res[mode] = (p, c, again, cross, auto_after, gpos, st, sta)
+    pk, ck, again, cross, auto_after, gk, st, sta = res[gp.api.FFT_AUTO]
+    p3, c3, _, _, _, g3, st3, _ = res[gp.api.FFT_CUFFT3D]
     assert "zfft_kz" in st and "fft2d_kz" in st and "bin_kz" in st, st
+    assert "adj_modes_kz" in sta and "adj_fft2d_kz" in sta and "kz_to_rows" not in sta, sta
     assert "win_convert" not in st and "zfft_kz" not in st3
     assert np.array_equal(ck, c3)
     hp, ho = pos.cpu().numpy(), other.cpu().numpy()
@@ -318,3 +325,4 @@ def test_kz_major_transform_1024(gp):
     _, _, _, rpos, _, _ = O.reference_gradient_sampled(hp, box, dims, nrbins, g, sample, None, 1.0,
                                                        m_norm=m, workers=WORKERS)
     grad_close(gk[sample], rpos)
+    grad_close(g3[sample], rpos)
