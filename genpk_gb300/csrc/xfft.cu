@@ -955,9 +955,26 @@ __global__ void __launch_bounds__(kTThreads)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t row0 = (int64_t)blockIdx.x * kTRows;
     const int x = (int)(row0 / N), y0 = (int)(row0 - (int64_t)x * N);
-    for (int e = threadIdx.x; e < HC * kTRows; e += kTThreads) {
-        const int kz = e / kTRows, r = e - kz * kTRows;
-        tb[kz * (kTRows + 1) + r] = spec[((size_t)kz * N + (size_t)x) * N + (size_t)(y0 + r)];
+    {
+        // every load of this thread in flight before any store (the runs are
+        // kTRows values of one kz plane, planes N^2 values apart)
+        constexpr int PER = (HC * kTRows + kTThreads - 1) / kTThreads;
+        float2 in[PER];
+#pragma unroll
+        for (int i = 0; i < PER; i++) {
+            const int e = threadIdx.x + i * kTThreads;
+            const int kz = e / kTRows, r = e - kz * kTRows;
+            in[i] = e < HC * kTRows
+                        ? __ldg(spec + ((size_t)kz * N + (size_t)x) * N + (size_t)(y0 + r))
+                        : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < PER; i++) {
+            const int e = threadIdx.x + i * kTThreads;
+            const int kz = e / kTRows, r = e - kz * kTRows;
+            if (e < HC * kTRows)
+                tb[kz * (kTRows + 1) + r] = in[i];
+        }
     }
     __syncthreads();
     float2 v[R];
