@@ -431,7 +431,8 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
         ctx->dscr.mass_part_cap = (int)mp;
         GENPK_TRY(reset_field());
         GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
-        GENPK_CUDA(deposit_window_pass(g, a, kStreamChunk, true, ctx->dscr.mass_part, mass_ctas,
+        GENPK_CUDA(deposit_window_pass(g, a, stream_chunk(a.n, a.masses != nullptr, ctx->num_sms),
+                                       true, ctx->dscr.mass_part, mass_ctas,
                                        ctx->dscr.win_acc, false, false, ctx->num_sms,
                                        ctx->d_status, ctx->stream, &ctx->launches, nullptr,
                                        nullptr));
@@ -637,7 +638,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
     }
     const bool chunked = engine == GENPK_ENGINE_WINDOW || engine == GENPK_ENGINE_STREAM;
     if (engine == GENPK_ENGINE_STREAM)
-        chunk = kStreamChunk;
+        chunk = stream_chunk(n, masses != nullptr, ctx->num_sms);
     if (chunked && ctx->inject_chunk >= 0) {
         a.skip_chunk = ctx->inject_chunk;
         a.skip_wait = ctx->inject_clocks;
