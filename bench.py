@@ -70,9 +70,6 @@ def parse():
                     help="deposit engine (default: the library's automatic choice)")
     ap.add_argument("--fft", choices=["auto", "cufft3d"], default="auto",
                     help="forward FFT path (default: the library's choice)")
-    ap.add_argument("--box-threads", type=int, default=8,
-                    help="boxes workload: host threads, each with its own contexts (one "
-                         "stream each), the boxes dealt round-robin")
     ap.add_argument("--workload", choices=["zeldovich", "uniform", "multispecies", "boxes"],
                     default="zeldovich",
                     help="zeldovich: one species (sizes from --nside/--grid/--box); "
@@ -373,13 +370,11 @@ def box_batch(seed=21, nboxes=16, box=25000.0):
 
 def boxes(args):
     """16 independent boxes per step, each one CIC deposit + r2c + binned auto
-    spectrum on its own grid.  The boxes are dealt round-robin to
-    --box-threads host threads; each thread has one context per grid size
-    (its own stream), so the boxes' launches, syncs and result read-backs
-    overlap (the C calls release the interpreter lock).  Timed by wall clock
-    with the device synchronised on both sides: at these sizes the per-box
-    launches and read-backs are part of the cost."""
-    import threading
+    spectrum on its own grid, through one genpk_batch_power call from one host
+    thread: every box's work is issued on its own stream (largest first) and
+    the call waits once per box for the results.  Timed by wall clock with the
+    device synchronised on both sides: at these sizes the launches and the
+    result read-backs are part of the cost."""
     import torch
     import genpk_gb300 as gp
     from genpk_gb300 import synth
@@ -387,34 +382,13 @@ def boxes(args):
     batch, box = box_batch()
     mass = 1.0e-2
     nrbins = args.nrbins
-    nth = max(1, args.box_threads)
     pos = [synth.uniform(c, box, seed=sd, device="cuda") for c, g, sd in batch]
     torch.cuda.synchronize()
-    sizes = sorted({g for _, g, _ in batch})
-    ctx_sets = [{g: gp.Context(g, nrbins) for g in sizes} for _ in range(nth)]
     norms = [O.total_mass(c, None, mass) for c, _, _ in batch]
-
-    def work(t, src, out):
-        for i in range(t, len(batch), nth):
-            _, g, _ = batch[i]
-            ctx = ctx_sets[t][g]
-            ctx.zero(0)
-            ctx.deposit(0, box, src[i], None, mass)
-            out[i] = ctx.power(0, 0, norms[i], norms[i])
+    b = gp.Batch([g for _, g, _ in batch], nrbins)
 
     def step(src):
-        out = [None] * len(batch)
-        if nth == 1:
-            work(0, src, out)
-            return out
-        ths = [threading.Thread(target=work, args=(t, src, out)) for t in range(nth)]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-        if any(o is None for o in out):
-            raise RuntimeError("a box thread failed")
-        return out
+        return b.power(box, src, norms, mass=mass)
 
     def timed(src, steps):
         ts = []
@@ -428,7 +402,9 @@ def boxes(args):
 
     for _ in range(args.warmup):
         res = step(pos)
+    launches0 = b.launches
     t_dev = timed(pos, args.steps)
+    launches = (b.launches - launches0) / args.steps
     npart = sum(c for c, _, _ in batch)
     line = {"metric": "particles/s + ms per batch (16 boxes, one auto spectrum each)",
             "value": npart / t_dev, "unit": "particles/s", "n_gpus": 1,
@@ -439,10 +415,12 @@ def boxes(args):
                                    f"in [1e5, 3e7], grid 128^3 or 256^3 per box, L={box:g} "
                                    f"kpc/h, mass {mass:g}, {nrbins} bins",
                        "boxes": [{"particles": c, "grid": g} for c, g, _ in batch],
-                       "particles": npart, "host_threads": nth,
+                       "particles": npart, "host_threads": 1,
+                       "api": "genpk_batch_power (one call per batch)",
                        "timing": "wall clock per batch, device synchronised on both sides"},
-            "engines": sorted({("sorted", "window", "stream")[cs[g].last_engine - 1]
-                               for cs in ctx_sets for g in cs if cs[g].last_engine > 0})}
+            "gpu_launches": launches,
+            "engines": [("sorted", "window", "stream")[b.engine(i) - 1]
+                        for i in range(len(batch))]}
     if not args.no_e2e:
         hpos = [p.cpu().pin_memory() for p in pos]
         step(hpos)
@@ -453,17 +431,16 @@ def boxes(args):
         del hpos
     if not args.no_cpu:
         worst, exact = 0.0, True
-        for (c, g, _), p, (pw, cnt, _) in zip(batch, pos, res):
+        pw, cnt, _ = res
+        for i, ((c, g, _), p) in enumerate(zip(batch, pos)):
             pr, cr, _, _ = cpu_pipeline(p.cpu().numpy(), box, g, nrbins, mass)
             ok = cr > 0
-            worst = max(worst, float(np.max(np.abs(pw[ok] - pr[ok]) / np.abs(pr[ok]))))
-            exact = exact and bool(np.array_equal(np.asarray(cnt), cr))
+            worst = max(worst, float(np.max(np.abs(pw[i][ok] - pr[ok]) / np.abs(pr[ok]))))
+            exact = exact and bool(np.array_equal(cnt[i], cr))
         line["parity"] = {"max_bin_rel_err": worst, "counts_bit_exact": exact,
                           "oracle": "FP64 CIC (oracle port) + FP64 pocketfft r2c + binning, "
                                     "every box"}
-    for cs in ctx_sets:
-        for c in cs.values():
-            c.close()
+    b.close()
     print(json.dumps(line), flush=True)
 
 

@@ -5,7 +5,8 @@ CIC deposit -> FP32 r2c FFT (own z, y and x passes for power-of-two grids of
 shell binning, plus the adjoint of a P(k) loss, behind the C ABI in
 include/genpk_gb300.h.  See genpk_gb300.api for the Python mirror.
 """
-from .api import (Context, GenPKError, fieldize, geometry, invwindow,  # noqa: F401
+from .api import (Batch, Context, GenPKError, fieldize, geometry, invwindow,  # noqa: F401
                   powerspectrum)
 
-__all__ = ["Context", "GenPKError", "fieldize", "geometry", "invwindow", "powerspectrum"]
+__all__ = ["Batch", "Context", "GenPKError", "fieldize", "geometry", "invwindow",
+           "powerspectrum"]

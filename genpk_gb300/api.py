@@ -224,7 +224,7 @@ class Context:
     def deposit_trials(self) -> list:
         """The sorted engine's latest tuning: [(tile, sort CTAs, ms), ...]."""
         from . import native
-        cap = 8
+        cap = 10
         tx = (ctypes.c_int * cap)()
         ty = (ctypes.c_int * cap)()
         tz = (ctypes.c_int * cap)()
@@ -249,6 +249,90 @@ class Context:
         `chunk` without its bulk copy, so its bounded wait gives up
         (genpk_inject_copy_timeout)."""
         self._chk(self.lib.genpk_inject_copy_timeout(self.h, int(chunk), int(wait_clocks)))
+
+
+class Batch:
+    """Many independent boxes (grids of any sizes, one bin count) whose auto
+    spectra one call computes: genpk_batch_power issues every box's deposit,
+    transform and binning from this thread, each box on its own stream, and
+    waits once for all of them."""
+
+    def __init__(self, dims_list, nrbins: int, timing: bool = False):
+        self.lib = native.load()
+        self.dims = [int(d) for d in dims_list]
+        self.nboxes = len(self.dims)
+        self.nrbins = int(nrbins)
+        arr = (ctypes.c_int64 * self.nboxes)(*self.dims)
+        h = ctypes.c_void_p()
+        rc = self.lib.genpk_batch_create(self.nboxes, arr, self.nrbins,
+                                         GENPK_FLAG_TIMING if timing else 0, ctypes.byref(h))
+        if rc != 0:
+            msg = self.lib.genpk_batch_last_error(h).decode() if h.value else ""
+            if h.value:
+                self.lib.genpk_batch_destroy(h)
+            raise GenPKError(rc, msg or self.lib.genpk_status_string(rc).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.genpk_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def power(self, boxsize, pos_list, mass_norm, masses_list=None, mass=0.0):
+        """(power, count, keffs), each [nboxes][nrbins].  boxsize, mass and
+        mass_norm: a number for every box or one per box."""
+        nb = self.nboxes
+
+        def per_box(v):
+            return [float(x) for x in v] if np.ndim(v) else [float(v)] * nb
+
+        keep, pp, mp, n = [], [], [], []
+        for i in range(nb):
+            a, k, _ = _arg(pos_list[i], np.float32, "float32")
+            pp.append(a)
+            keep.append(k)
+            n.append((k.numel() if _is_torch(k) else k.size) // 3)
+            m = masses_list[i] if masses_list is not None else None
+            b, km, _ = _arg(m, np.float32, "float32")
+            mp.append(b)
+            keep.append(km)
+        bs = (ctypes.c_double * nb)(*per_box(boxsize))
+        ms = (ctypes.c_double * nb)(*per_box(mass))
+        mn = (ctypes.c_double * nb)(*per_box(mass_norm))
+        nn = (ctypes.c_int64 * nb)(*n)
+        pos_arr = (ctypes.c_void_p * nb)(*pp)
+        mass_arr = (ctypes.c_void_p * nb)(*mp) if masses_list is not None else None
+        p = np.zeros((nb, self.nrbins))
+        c = np.zeros((nb, self.nrbins), dtype=np.int32)
+        kf = np.zeros((nb, self.nrbins))
+        rc = self.lib.genpk_batch_power(self.h, bs, pos_arr, mass_arr, ms, nn, mn,
+                                        p.ctypes.data_as(native.c_f64p),
+                                        c.ctypes.data_as(native.c_i32p),
+                                        kf.ctypes.data_as(native.c_f64p))
+        del keep
+        if rc != 0:
+            raise GenPKError(rc, self.lib.genpk_batch_last_error(self.h).decode())
+        return p, c, kf
+
+    def engine(self, i: int) -> int:
+        """Deposit engine box i's latest pass used."""
+        return int(self.lib.genpk_last_deposit_engine(self.lib.genpk_batch_box(self.h, i)))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.genpk_batch_launches(self.h))
 
 
 # ---------------------------------------------------------------------------

@@ -105,7 +105,7 @@ struct genpk_ctx {
     Tuned tuned[kTuned];
     int ntuned = 0;
     // the latest tuning's trials, and the configuration the latest sorted pass used
-    static constexpr int kMaxTrials = 8;
+    static constexpr int kMaxTrials = 10;
     TileShape trial_tile[kMaxTrials];
     int trial_ctas[kMaxTrials] = {};
     float trial_ms[kMaxTrials] = {};
@@ -161,6 +161,20 @@ struct genpk_ctx {
     std::vector<std::vector<double>> auto_power;  // cached auto spectrum per field
     std::vector<double> auto_mass;
     std::vector<bool> auto_valid;
+
+    // results of a power request issued without waiting (genpk_batch_power):
+    // copied to pinned host memory on the stream, read when the batch collects
+    double *h_power = nullptr;
+    size_t h_power_cap = 0;
+    struct Deferred {
+        bool active = false;
+        int np = 0;
+        std::vector<int> pairs;
+        std::vector<double> mass;
+    } deferred;
+    // inside genpk_batch_power: pinned host input is read in place without
+    // waiting for the pass (the batch waits once for every box)
+    bool batch_mode = false;
 
     // adjoint scratch
     float *d_gcoef = nullptr;
@@ -372,7 +386,7 @@ constexpr int64_t kTuneMinParticles = (int64_t)1 << 16;
 // The deposit autotuner for particle orders without spatial coherence.  On
 // the first clean pass of a density band (and mass kind) it runs the pass once
 // per candidate -- the sorted engine with tiles 8^3, 16x16x8 and 16^3, each
-// with up to 2 and up to 4 sort CTAs per SM, and (with_stream) the stream
+// with up to 1, 2 and 4 sort CTAs per SM, and (with_stream) the stream
 // engine, whose reductions go straight to the accumulator -- timed with CUDA
 // events, and keeps the fastest.  (Measured on uniform random particles: the
 // stream engine is 2-2.6x faster at 1e6 particles, where the sort's fixed
@@ -386,7 +400,9 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
                 const genpk_ctx::Tuned **out)
 {
     static const TileShape tiles[] = {{8, 8, 8}, {16, 16, 8}, {16, 16, 16}};
-    static const int pers[] = {2, 4};
+    // sort CTAs per SM: fewer CTAs give each (CTA, tile) run of the scatter
+    // more particles, so its 16-byte records share sectors in the L2
+    static const int pers[] = {1, 2, 4};
     const size_t stash = 0;  // the error counters are kept in the probe buffer meanwhile
     GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)4));
     GENPK_CUDA(cudaMemcpyAsync(ctx->d_probe + stash, ctx->d_status, 2 * sizeof(long long),
@@ -1059,10 +1075,35 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
     return GENPK_OK;
 }
 
-int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
-               double *power, int *count, double *keffs)
+// The host side of a finished power request: count, keffs, the cached auto
+// spectra, the device status.
+int finish_power(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
+                 const double *power, int *count, double *keffs)
 {
-    if (np <= 0 || !pairs || !pair_mass || !power)
+    const int nrb = ctx->nrbins;
+    for (int b = 0; b < nrb; b++) {
+        if (count)
+            count[b] = (int)ctx->tables.count[(size_t)b];
+        if (keffs)
+            keffs[b] = ctx->tables.keffs[(size_t)b];
+    }
+    for (int q = 0; q < np; q++) {
+        if (pairs[2 * q] == pairs[2 * q + 1] && pair_mass[2 * q] == pair_mass[2 * q + 1]) {
+            const int f = pairs[2 * q];
+            ctx->auto_power[(size_t)f].assign(power + (size_t)q * nrb, power + (size_t)(q + 1) * nrb);
+            ctx->auto_mass[(size_t)f] = pair_mass[2 * q];
+            ctx->auto_valid[(size_t)f] = true;
+        }
+    }
+    return collect_status(ctx);
+}
+
+// deferred: issue everything, the results' copy to the context's pinned
+// buffer included, and return without waiting; power_collect finishes it.
+int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
+               double *power, int *count, double *keffs, bool deferred = false)
+{
+    if (np <= 0 || !pairs || !pair_mass || (!power && !deferred))
         return fail(ctx, GENPK_ERR_INVALID, "genpk_power_multi: bad pair arguments");
     std::vector<int> fields;
     for (int q = 0; q < 2 * np; q++) {
@@ -1182,25 +1223,44 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         q0 = q;
     }
     stage_event(ctx, "bin");
-    GENPK_CUDA(cudaMemcpyAsync(power, ctx->d_power, sizeof(double) * np * nrb,
+    double *dst = power;
+    if (deferred) {
+        const size_t need = (size_t)np * nrb;
+        if (ctx->h_power_cap < need) {
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            cudaFreeHost(ctx->h_power);
+            ctx->h_power = nullptr;
+            ctx->h_power_cap = 0;
+            GENPK_CUDA(cudaHostAlloc((void **)&ctx->h_power, sizeof(double) * need,
+                                     cudaHostAllocDefault));
+            ctx->h_power_cap = need;
+        }
+        dst = ctx->h_power;
+    }
+    GENPK_CUDA(cudaMemcpyAsync(dst, ctx->d_power, sizeof(double) * np * nrb,
                                cudaMemcpyDeviceToHost, ctx->stream));
     stage_event(ctx, "d2h");
+    if (deferred) {
+        ctx->deferred.active = true;
+        ctx->deferred.np = np;
+        ctx->deferred.pairs.assign(pairs, pairs + 2 * np);
+        ctx->deferred.mass.assign(pair_mass, pair_mass + 2 * np);
+        return GENPK_OK;
+    }
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int b = 0; b < nrb; b++) {
-        if (count)
-            count[b] = (int)ctx->tables.count[(size_t)b];
-        if (keffs)
-            keffs[b] = ctx->tables.keffs[(size_t)b];
-    }
-    for (int q = 0; q < np; q++) {
-        if (pairs[2 * q] == pairs[2 * q + 1] && pair_mass[2 * q] == pair_mass[2 * q + 1]) {
-            const int f = pairs[2 * q];
-            ctx->auto_power[(size_t)f].assign(power + (size_t)q * nrb, power + (size_t)(q + 1) * nrb);
-            ctx->auto_mass[(size_t)f] = pair_mass[2 * q];
-            ctx->auto_valid[(size_t)f] = true;
-        }
-    }
-    return collect_status(ctx);
+    return finish_power(ctx, np, pairs, pair_mass, power, count, keffs);
+}
+
+// Wait for a deferred power request and hand its results over.
+int power_collect(genpk_ctx *ctx, double *power, int *count, double *keffs)
+{
+    if (!ctx->deferred.active)
+        return fail(ctx, GENPK_ERR_STATE, "no power request is pending");
+    ctx->deferred.active = false;
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    const genpk_ctx::Deferred &d = ctx->deferred;
+    memcpy(power, ctx->h_power, sizeof(double) * (size_t)d.np * ctx->nrbins);
+    return finish_power(ctx, d.np, d.pairs.data(), d.mass.data(), power, count, keffs);
 }
 
 // Device copies of particle arrays for the adjoint when the caller passed host memory.
@@ -1271,6 +1331,7 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->d_gcoef);
     cudaFree(ctx->adj_buf);
     cudaFree(ctx->d_probe);
+    cudaFreeHost(ctx->h_power);
     for (auto &e : ctx->ev)
         if (e)
             cudaEventDestroy(e);
@@ -1404,8 +1465,10 @@ int genpk_deposit(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
         if (pm && (!masses || mm)) {
             GENPK_TRY(flush_pending(ctx));
             GENPK_TRY(run_deposit(ctx, field, boxsize, pm, mm, (float)mass, n, true));
-            // The caller may free or reuse its buffers as soon as we return.
-            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            // The caller may free or reuse its buffers as soon as we return (a
+            // batch waits for every box before it returns).
+            if (!ctx->batch_mode)
+                GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
             return GENPK_OK;
         }
     }
@@ -1796,6 +1859,124 @@ int genpk_last_deposit_engine(const genpk_ctx *ctx)
 int64_t genpk_kernel_launches(const genpk_ctx *ctx)
 {
     return ctx ? ctx->launches : -1;
+}
+
+struct genpk_batch {
+    std::vector<genpk_ctx *> box;
+    int nrbins = 0;
+    std::string err;
+};
+
+void genpk_batch_destroy(genpk_batch *b)
+{
+    if (!b)
+        return;
+    for (genpk_ctx *c : b->box)
+        genpk_ctx_destroy(c);
+    delete b;
+}
+
+int genpk_batch_create(int nboxes, const int64_t *dims, int nrbins, unsigned flags,
+                       genpk_batch **out)
+{
+    if (!out)
+        return GENPK_ERR_INVALID;
+    *out = nullptr;
+    if (nboxes < 1 || !dims || nrbins < 1)
+        return GENPK_ERR_INVALID;
+    genpk_batch *b = new genpk_batch();
+    b->nrbins = nrbins;
+    for (int i = 0; i < nboxes; i++) {
+        genpk_ctx *c = nullptr;
+        const int rc = genpk_ctx_create(dims[i], nrbins, 1, flags, &c);
+        if (rc != GENPK_OK) {
+            b->err = "box " + std::to_string(i) + ": " + (c ? genpk_last_error(c) : "") +
+                     " (" + genpk_status_string(rc) + ")";
+            genpk_ctx_destroy(c);
+            *out = b;  // keep the message readable; caller destroys
+            return rc;
+        }
+        b->box.push_back(c);
+    }
+    *out = b;
+    return GENPK_OK;
+}
+
+const char *genpk_batch_last_error(const genpk_batch *b)
+{
+    return b ? b->err.c_str() : "null batch";
+}
+
+genpk_ctx *genpk_batch_box(genpk_batch *b, int i)
+{
+    if (!b || i < 0 || i >= (int)b->box.size())
+        return nullptr;
+    return b->box[(size_t)i];
+}
+
+int64_t genpk_batch_launches(const genpk_batch *b)
+{
+    if (!b)
+        return -1;
+    int64_t k = 0;
+    for (const genpk_ctx *c : b->box)
+        k += c->launches;
+    return k;
+}
+
+int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const *pos,
+                      const float *const *masses, const double *mass, const int64_t *n,
+                      const double *mass_norm, double *power, int *count, double *keffs)
+{
+    if (!b)
+        return GENPK_ERR_INVALID;
+    const int nb = (int)b->box.size();
+    if (!boxsize || !pos || !mass || !n || !mass_norm || !power) {
+        b->err = "genpk_batch_power: null argument";
+        return GENPK_ERR_INVALID;
+    }
+    // largest boxes first: their passes start first, the small ones fill in
+    std::vector<int> order((size_t)nb);
+    for (int i = 0; i < nb; i++)
+        order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+    const int nrb = b->nrbins;
+    int first = GENPK_OK;
+    std::vector<bool> issued((size_t)nb, false);
+    auto note = [&](int i, int rc) {
+        if (rc != GENPK_OK && first == GENPK_OK) {
+            first = rc;
+            b->err = "box " + std::to_string(i) + ": " + genpk_last_error(b->box[(size_t)i]);
+        }
+    };
+    for (int i : order) {
+        genpk_ctx *c = b->box[(size_t)i];
+        cudaSetDevice(c->device);
+        c->batch_mode = true;
+        int rc = genpk_zero(c, 0);
+        if (rc == GENPK_OK)
+            rc = genpk_deposit(c, 0, boxsize[i], pos[i], masses ? masses[i] : nullptr, mass[i],
+                               n[i]);
+        if (rc == GENPK_OK) {
+            const int pr[2] = {0, 0};
+            const double pm[2] = {mass_norm[i], mass_norm[i]};
+            rc = power_impl(c, 1, pr, pm, nullptr, nullptr, nullptr, true);
+            issued[(size_t)i] = rc == GENPK_OK;
+        }
+        c->batch_mode = false;
+        note(i, rc);
+    }
+    for (int i : order) {  // every issued box is waited for, even after a failure
+        if (!issued[(size_t)i])
+            continue;
+        genpk_ctx *c = b->box[(size_t)i];
+        cudaSetDevice(c->device);
+        note(i, power_collect(c, power + (size_t)i * nrb, count ? count + (size_t)i * nrb : nullptr,
+                              keffs ? keffs + (size_t)i * nrb : nullptr));
+    }
+    if (first == GENPK_OK)
+        b->err.clear();
+    return first;
 }
 
 int genpk_inject_copy_timeout(genpk_ctx *ctx, int64_t chunk, int64_t wait_clocks)

@@ -53,6 +53,17 @@ ABI = {
     "genpk_inject_copy_timeout": (ctypes.c_int, [c_void_p, ctypes.c_int64, ctypes.c_int64]),
     "genpk_deposit_trials": (ctypes.c_int, [c_void_p, c_i32p, c_i32p, c_i32p, c_i32p, c_f32p,
                                             ctypes.c_int]),
+    "genpk_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.c_int, ctypes.c_uint,
+                                          ctypes.POINTER(c_void_p)]),
+    "genpk_batch_destroy": (None, [c_void_p]),
+    "genpk_batch_last_error": (ctypes.c_char_p, [c_void_p]),
+    "genpk_batch_power": (ctypes.c_int, [c_void_p, c_f64p, ctypes.POINTER(c_void_p),
+                                         ctypes.POINTER(c_void_p), c_f64p,
+                                         ctypes.POINTER(ctypes.c_int64), c_f64p, c_f64p, c_i32p,
+                                         c_f64p]),
+    "genpk_batch_box": (c_void_p, [c_void_p, ctypes.c_int]),
+    "genpk_batch_launches": (ctypes.c_int64, [c_void_p]),
     "genpk_power_noalloc": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_double, c_void_p, c_i32p,
                                            c_f64p, c_void_p]),

@@ -175,7 +175,7 @@ int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *ti
  * coherence: on the first clean pass of each particle density band (half
  * octaves of particles per cell) and mass kind, the pass runs once per
  * candidate -- the sorted engine with tiles 8^3, 16x16x8 and 16^3, each with
- * up to 2 and up to 4 sort CTAs per SM, and, when the engine is automatic,
+ * up to 1, 2 and 4 sort CTAs per SM, and, when the engine is automatic,
  * the stream engine -- timed with CUDA events, and the fastest is kept for
  * that band.  Every candidate writes the same grid.  This returns the latest
  * tuning's trials (at most cap, the number written): tile edges (0 x 0 x 0
@@ -225,6 +225,39 @@ int genpk_set_fft_mode(genpk_ctx *ctx, int mode);
 
 /* Number of kernels the library launched on ctx since creation. */
 int64_t genpk_kernel_launches(const genpk_ctx *ctx);
+
+/* Many independent boxes in one call -- the per-type loop of
+ * gen-pk.cpp:204-239 generalised to a batch of snapshots or boxes with
+ * different grids.  Box b has a dims[b]^3 grid; all boxes share nrbins.
+ * Every box has a context of its own (grid, accumulator, stream).  Errors as
+ * for genpk_ctx_create; genpk_batch_last_error explains them. */
+typedef struct genpk_batch genpk_batch;
+int genpk_batch_create(int nboxes, const int64_t *dims, int nrbins, unsigned flags,
+                       genpk_batch **out);
+void genpk_batch_destroy(genpk_batch *b);
+const char *genpk_batch_last_error(const genpk_batch *b);
+
+/* The auto spectrum of every box: its n[b] particles pos[b] (float[n][3]),
+ * masses[b] (float[n]) or NULL (masses itself may be NULL) for the uniform
+ * mass[b], normalised by mass_norm[b] (powerspectrum.c:102-108).  power,
+ * count and keffs are [nboxes][nrbins] host arrays (count and keffs may be
+ * NULL).  One host thread issues every box's deposit, transform and binning,
+ * largest box first, each on its box's stream, so that the boxes overlap on
+ * the GPU, then waits once per box for the results; the deposit engine of each
+ * box is chosen as genpk_deposit chooses it (and remembered for the same
+ * arrays).  Particle arrays may be host or device memory; pinned host and
+ * device arrays are read while other boxes' work runs and must stay valid
+ * until the call returns.  Returns the first failure (the message names the
+ * box); every issued box is still waited for. */
+int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const *pos,
+                      const float *const *masses, const double *mass, const int64_t *n,
+                      const double *mass_norm, double *power, int *count, double *keffs);
+
+/* Box i's context (for its stage times, engine and configuration), or NULL. */
+genpk_ctx *genpk_batch_box(genpk_batch *b, int i);
+
+/* Kernels launched by all the batch's boxes since creation. */
+int64_t genpk_batch_launches(const genpk_batch *b);
 
 /* Testing aid for the bounded device waits (no reference counterpart; the
  * reference has no device code).  The next window- or stream-engine deposit
