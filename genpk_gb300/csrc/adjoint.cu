@@ -223,6 +223,62 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Four consecutive particles per thread: three 16-byte loads of positions
+// (and one of masses), the 32 grid loads of the four particles issued
+// together, three 16-byte stores of gradients.  The one-particle kernel's
+// thread waits out a position load and then the grid loads for every
+// particle; here each wait covers four.  Needs pos, gpos (and masses, gmass)
+// on 16-byte boundaries; the last n % 4 particles go one per thread.
+__device__ __forceinline__ GatherOut gather_or_zero(const GatherParams &p, const float *__restrict__ grid,
+                                                    float x, float y, float z, float m)
+{
+    if (!finite3(x, y, z))
+        return {0.f, 0.f, 0.f, -p.dl_dm};
+    return gather_one(p, grid, x, y, z, m);
+}
+
+template <bool VARMASS>
+__global__ void __launch_bounds__(256)
+    k_gather4(GatherParams p, const float *__restrict__ grid, const float *__restrict__ pos,
+              const float *__restrict__ masses, float *__restrict__ gpos, float *__restrict__ gmass)
+{
+    const int64_t groups = p.n >> 2;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t q = tid; q < groups; q += (int64_t)gridDim.x * blockDim.x) {
+        const float4 *s = reinterpret_cast<const float4 *>(pos) + 3 * q;
+        const float4 a = __ldg(s), b = __ldg(s + 1), c = __ldg(s + 2);
+        float4 m = make_float4(p.mass, p.mass, p.mass, p.mass);
+        if (VARMASS)
+            m = __ldg(reinterpret_cast<const float4 *>(masses) + q);
+        const GatherOut o0 = gather_or_zero(p, grid, a.x, a.y, a.z, m.x);
+        const GatherOut o1 = gather_or_zero(p, grid, a.w, b.x, b.y, m.y);
+        const GatherOut o2 = gather_or_zero(p, grid, b.z, b.w, c.x, m.z);
+        const GatherOut o3 = gather_or_zero(p, grid, c.y, c.z, c.w, m.w);
+        float4 *d = reinterpret_cast<float4 *>(gpos) + 3 * q;
+        d[0] = make_float4(o0.gx, o0.gy, o0.gz, o1.gx);
+        d[1] = make_float4(o1.gy, o1.gz, o2.gx, o2.gy);
+        d[2] = make_float4(o2.gz, o3.gx, o3.gy, o3.gz);
+        if (VARMASS)
+            reinterpret_cast<float4 *>(gmass)[q] =
+                make_float4(o0.val + p.dl_dm, o1.val + p.dl_dm, o2.val + p.dl_dm, o3.val + p.dl_dm);
+    }
+    const int64_t i = 4 * groups + tid;  // the last n % 4 particles
+    if (i < p.n) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const GatherOut o = gather_or_zero(p, grid, x, y, z, VARMASS ? masses[i] : p.mass);
+        gpos[3 * i] = o.gx;
+        gpos[3 * i + 1] = o.gy;
+        gpos[3 * i + 2] = o.gz;
+        if (VARMASS)
+            gmass[i] = o.val + p.dl_dm;
+    }
+}
+
+bool aligned16(const void *ptr)
+{
+    return ((uintptr_t)ptr & 15) == 0;
+}
+
 }  // namespace
 
 cudaError_t adjoint_mode_gradient_kz(const GridGeom &g, const BinTables &t, const BinDevice &d,
@@ -283,6 +339,17 @@ cudaError_t adjoint_gather(const GridGeom &g, float units_hi, float units_lo, co
     // grid to the resident CTAs, so that the stride sweeps the particles in
     // order, cut the DRAM reads at 512^3 from 2.85 to 2.56 GB (2.15 GB of
     // positions and grid) but took 1.00 ms against 0.92.
+    const bool vec = aligned16(pos) && aligned16(grad_pos) &&
+                     (!masses || (aligned16(masses) && aligned16(grad_mass)));
+    if (vec) {
+        const int blocks4 = (int)std::min<int64_t>(std::max<int64_t>((n / 4 + 255) / 256, 1), 152 * 32);
+        if (masses)
+            k_gather4<true><<<blocks4, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);
+        else
+            k_gather4<false><<<blocks4, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);
+        (*launches)++;
+        return cudaGetLastError();
+    }
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
     if (masses)
         k_gather<true><<<blocks, 256, 0, stream>>>(p, grid, pos, masses, grad_pos, grad_mass);

@@ -151,12 +151,15 @@ def test_adjoint_device_pointers(gp):
 
 
 def test_adjoint_ragged_tile_and_unaligned_arrays(gp):
-    """A ragged particle count (not a multiple of 256 or 1024) through aligned
-    device arrays and through device arrays that start 12 bytes past a 16-byte
-    boundary: the same gradients bit for bit, and the FP64 reference
-    gradient."""
+    """A ragged particle count (not a multiple of 4, 256 or 1024) through
+    aligned device arrays (the gather's four-particles-per-thread path) and
+    through device arrays that start 12 bytes past a 16-byte boundary (one
+    particle per thread): the same gradients bit for bit, and the FP64
+    reference gradient.  Non-finite positions, one among the first particles
+    and one among the last n % 4, get zero gradients and leave the others
+    unchanged."""
     import torch
-    dims, box, nrbins, n = 32, 1000.0, 16, 3004
+    dims, box, nrbins, n = 32, 1000.0, 16, 3003
     pos, masses = make_case("uniform", dims, box, 7, nrbins, True)
     pos, masses = pos[:n].copy(), masses[:n].copy()
     m = O.total_mass(n, masses)
@@ -175,9 +178,22 @@ def test_adjoint_ragged_tile_and_unaligned_arrays(gp):
         a = ctx.adjoint(0, box, al, g, m, masses=am, recompute=True)
         b = ctx.adjoint(0, box, bp[3:], g, m, masses=bm[3:], recompute=True,
                         grad_pos=gb[3:], grad_mass=gmb[3:])
+        ctx.zero(0)
+        ctx.deposit(0, box, pos, masses)
+        ctx.power(0, 0, m, m)
+        bad = al.clone()
+        bad[5, 1] = float("nan")
+        bad[n - 1, 2] = float("inf")
+        c = ctx.adjoint(0, box, bad, g, m, masses=am)  # from the kept spectrum
     assert bp[3:].data_ptr() % 16 == 12
     assert np.array_equal(a[0].cpu().numpy(), gb[3:].reshape(n, 3).cpu().numpy())
     assert np.array_equal(a[1].cpu().numpy(), gmb[3:].cpu().numpy())
+    keep = np.ones(n, dtype=bool)
+    keep[[5, n - 1]] = False
+    cp, cm = c[0].cpu().numpy(), c[1].cpu().numpy()
+    assert np.all(cp[~keep] == 0.0) and np.all(cm[~keep] == 0.0)
+    assert np.array_equal(cp[keep], a[0].cpu().numpy()[keep])
+    assert np.array_equal(cm[keep], a[1].cpu().numpy()[keep])
     rpos, rmass, _ = O.reference_gradient(pos, box, dims, nrbins, g, masses, 0.0, m_norm=m)
     grad_close(a[0].cpu().numpy(), rpos)
     grad_close(a[1].cpu().numpy(), rmass)
