@@ -1067,7 +1067,7 @@ cudaError_t window_convert(const GridGeom &g, const unsigned long long *acc, flo
 
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
                                 bool stream_mode, double *mass_part, int mass_ctas,
-                                unsigned long long *acc, bool acc_zero, bool defer_convert,
+                                unsigned long long *acc, size_t clear_bytes, bool defer_convert,
                                 int num_sms,
                                 DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
                                 StageHook hook, void *hook_user)
@@ -1090,9 +1090,9 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
     k_window_prep<<<1, 1, 0, stream>>>(mass_part, a.masses ? mass_ctas : 0, (double)a.mass, a.n,
                                        1.0 / n3, a.field_mass, a.field_sub, dstat);
     mark("win_prep");
-    if (!acc_zero) {
-        if ((err = cudaMemsetAsync(acc, 0, sizeof(acc_t) * (size_t)g.grid.nfloat, stream)) !=
-            cudaSuccess)
+    if (clear_bytes) {
+        clear_bytes = std::min(clear_bytes, sizeof(acc_t) * (size_t)g.grid.nfloat);
+        if ((err = cudaMemsetAsync(acc, 0, clear_bytes, stream)) != cudaSuccess)
             return err;
         mark("win_clear");
     }

@@ -126,6 +126,11 @@ struct genpk_ctx {
     // the next own x pass may clear it.
     bool acc_zero = false;
     bool acc_spent = false;
+    // With acc_zero false: 0 when any of the accumulator may be non-zero, else
+    // the length of its non-zero prefix (a float grid written over a cleared
+    // accumulator: the kz-major adjoint's dL/drho, or a row-major copy of a
+    // kz-major spectrum), which is all that the next window pass clears.
+    size_t acc_dirty_bytes = 0;
     // Recent automatic engine choices and the arrays they were made for (a few:
     // one per species of a multi-species loop).  Every engine yields the same
     // grid, so reusing a choice for the same particle arrays (a loop over the
@@ -197,6 +202,22 @@ int fail(genpk_ctx *ctx, int code, const std::string &msg)
     if (ctx)
         ctx->err = msg;
     return code;
+}
+
+size_t acc_bytes(const genpk_ctx *ctx)
+{
+    return sizeof(unsigned long long) * (size_t)ctx->gg.nfloat;
+}
+
+// The accumulator's first `bytes` bytes were overwritten (used as a float
+// buffer): only they need clearing if the rest was zero.
+void acc_overwritten(genpk_ctx *ctx, size_t bytes)
+{
+    if (ctx->acc_zero)
+        ctx->acc_dirty_bytes = bytes;
+    else if (ctx->acc_dirty_bytes)
+        ctx->acc_dirty_bytes = std::max(ctx->acc_dirty_bytes, bytes);
+    ctx->acc_zero = false;
 }
 
 #define GENPK_CUDA(call)                                                                      \
@@ -449,7 +470,7 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
         GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
         GENPK_CUDA(deposit_window_pass(g, a, stream_chunk(a.n, a.masses != nullptr, ctx->num_sms),
                                        true, ctx->dscr.mass_part, mass_ctas,
-                                       ctx->dscr.win_acc, false, false, ctx->num_sms,
+                                       ctx->dscr.win_acc, acc_bytes(ctx), false, ctx->num_sms,
                                        ctx->d_status, ctx->stream, &ctx->launches, nullptr,
                                        nullptr));
         GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
@@ -457,6 +478,7 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
         float ms = 0.f;
         GENPK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         ctx->acc_zero = false;  // it holds the trial's sums
+        ctx->acc_dirty_bytes = 0;
         ctx->acc_spent = true;
         ctx->trial_tile[0] = TileShape{0, 0, 0};
         ctx->trial_ctas[0] = 0;
@@ -685,10 +707,12 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
         // accumulator: the z pass converts it on the fly.
         const bool defer = a.clean && (use_xfft(ctx) || use_kz(ctx));
         // (a pass that fails part-way must not leave the accumulator marked clear)
-        const bool acc_zero = ctx->acc_zero;
+        const size_t clear = ctx->acc_zero ? 0 : ctx->acc_dirty_bytes ? ctx->acc_dirty_bytes
+                                                                       : acc_bytes(ctx);
         ctx->acc_zero = false;
+        ctx->acc_dirty_bytes = 0;
         GENPK_CUDA(deposit_window_pass(g, a, chunk, engine == GENPK_ENGINE_STREAM, s.mass_part,
-                                       mass_ctas, s.win_acc, acc_zero, defer, ctx->num_sms,
+                                       mass_ctas, s.win_acc, clear, defer, ctx->num_sms,
                                        ctx->d_status, ctx->stream, &ctx->launches, hook, ctx));
         ctx->acc_spent = !defer;  // converted in the pass
         if (defer)
@@ -938,7 +962,7 @@ int ensure_row_major(genpk_ctx *ctx, int f)
                           ctx->stream, &ctx->launches));
     GENPK_CUDA(cudaMemcpyAsync(grid_of(ctx, f), tmp, sizeof(float) * (size_t)ctx->gg.nfloat,
                                cudaMemcpyDeviceToDevice, ctx->stream));
-    ctx->acc_zero = false;
+    acc_overwritten(ctx, sizeof(float) * (size_t)ctx->gg.nfloat);
     ctx->acc_spent = false;
     ctx->kzmajor[(size_t)f] = false;
     stage_event(ctx, "kz_to_rows");
@@ -1019,7 +1043,6 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
         GENPK_TRY(flush_acc(ctx));
     timing_touch(ctx);
     stage_event(ctx, "host");
-    const int64_t acc_bytes = (int64_t)sizeof(unsigned long long) * ctx->gg.nfloat;
     size_t i = 0;
     while (i < todo.size()) {
         size_t j = i + 1;
@@ -1051,7 +1074,7 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
             // N = 512, against 0.15 ms for the separate clear).
             const bool clear = bin && ctx->acc_spent && ctx->acc_pending < 0 && ctx->dscr.win_acc;
             GENPK_CUDA(xfft_pass(ctx->gg, base, batch, ctx->d_xtw, bin ? &fused->bin : nullptr,
-                                 clear ? ctx->dscr.win_acc : nullptr, clear ? acc_bytes : 0,
+                                 clear ? ctx->dscr.win_acc : nullptr, clear ? (int64_t)acc_bytes(ctx) : 0,
                                  ctx->num_sms, ctx->d_status, ctx->stream, &ctx->launches));
             if (clear) {
                 ctx->acc_spent = false;
@@ -1696,7 +1719,7 @@ int genpk_adjoint(genpk_ctx *ctx, int field, double boxsize, const float *pos, c
         stage_event(ctx, "adj_fft2d_kz");
         float *gbuf = reinterpret_cast<float *>(ctx->dscr.win_acc);
         GENPK_CUDA(zifft_kz_pass(ctx->gg, g, gbuf, ctx->d_xtw, ctx->stream, &ctx->launches));
-        ctx->acc_zero = false;
+        acc_overwritten(ctx, sizeof(float) * (size_t)ctx->gg.nfloat);
         ctx->acc_spent = false;
         ctx->kzmajor[(size_t)field] = false;
         g = gbuf;

@@ -156,11 +156,12 @@ cudaError_t stream_probe(const DepositGeom &g, const DepositArgs &a,
 // defer_convert (clean grids only): acc is left holding the pass, for
 // zfft_pass to read or window_convert to turn into the FP32 grid later (both
 // use the pass's mean and scale in dstat: no other pass may run before).
-// acc_zero: acc is known to hold zeros (cleared by the last transform's x
-// pass), so the pass skips its clear.
+// clear_bytes: how much of acc, from its start, the pass clears first (all
+// of it, or 0 when acc is known to hold zeros: cleared by the last
+// transform's binning pass; or the part that a float grid overwrote).
 cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int chunk,
                                 bool stream_mode, double *mass_part, int mass_ctas,
-                                unsigned long long *acc, bool acc_zero, bool defer_convert,
+                                unsigned long long *acc, size_t clear_bytes, bool defer_convert,
                                 int num_sms,
                                 DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
                                 StageHook hook, void *hook_user);
