@@ -143,6 +143,19 @@ __device__ __forceinline__ void block_mass(float msum, float mc, float mmax, dou
     }
 }
 
+// True when some lane's tile equals the previous lane's (a run of particles in
+// one tile, as spatially ordered input gives).  Without one, the lanes take
+// their tile slots with one shared atomic each: __match_any_sync over 32
+// distinct tiles (random order, the sorted engine's usual input) costs more
+// than it merges.  Slots within a tile may then come in any order; the tile
+// sums are exact integers, so the grid does not depend on it.
+__device__ __forceinline__ bool warp_has_tile_runs(uint32_t t)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, t, 1);
+    return __any_sync(0xffffffffu, lane > 0 && t != kNoTile && t == prev);
+}
+
 // Each warp walks its CTA's range in blocks of 32*kSortUnroll consecutive
 // particles (lane l takes base + l + 32u, so every load is coalesced).  The trip
 // count is warp-uniform, so warp-collective intrinsics are safe in `f`.
@@ -209,9 +222,14 @@ __global__ void __launch_bounds__(kSortThreads)
                 bad++;
             }
         }
-        const unsigned peers = __match_any_sync(0xffffffffu, t);
-        if (t != kNoTile && lane == __ffs(peers) - 1)
-            atomicAdd(&counts[t], (uint32_t)__popc(peers));
+        if (!warp_has_tile_runs(t)) {
+            if (t != kNoTile)
+                atomicAdd(&counts[t], 1u);
+        } else {
+            const unsigned peers = __match_any_sync(0xffffffffu, t);
+            if (t != kNoTile && lane == __ffs(peers) - 1)
+                atomicAdd(&counts[t], (uint32_t)__popc(peers));
+        }
     });
     __syncthreads();
     if (!GLOBAL) {
@@ -224,16 +242,45 @@ __global__ void __launch_bounds__(kSortThreads)
         atomicAdd(&st->bad_particles, (unsigned long long)bad);
 }
 
-__global__ void k_sort_colsum(const uint32_t *__restrict__ hist, int nsort, int ntiles,
-                              uint32_t *__restrict__ totals)
+// The histogram is [nsort][ntiles].  Its column sums and column prefix sums
+// go 32 tiles (one 128-byte row segment) per CTA, with the CTA rows split
+// into kColWarps contiguous blocks, one per warp: a lane's loads are
+// independent and in flight together, and a grid of 16^3 tiles at 128^3
+// (512 tiles) still spreads over 16 CTAs x 32 warps.  One thread per tile
+// walking all rows waited out nsort dependent round trips (90 us per pass at
+// 608 rows).
+constexpr int kColWarps = 32;
+
+// Sum of rows [r0, r1) of tile t's column (0 where t is out of range).
+__device__ __forceinline__ uint32_t column_block_sum(const uint32_t *hist, int ntiles, int t,
+                                                     int r0, int r1)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles)
-        return;
     uint32_t s = 0;
-    for (int c = 0; c < nsort; c++)
-        s += hist[(size_t)c * ntiles + t];
-    totals[t] = s;
+    if (t < ntiles) {
+#pragma unroll 8
+        for (int c = r0; c < r1; c++)
+            s += hist[(size_t)c * ntiles + t];
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(32 * kColWarps)
+    k_sort_colsum(const uint32_t *__restrict__ hist, int nsort, int ntiles,
+                  uint32_t *__restrict__ totals)
+{
+    __shared__ uint32_t part[kColWarps][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + lane;
+    const int rows = (nsort + kColWarps - 1) / kColWarps;
+    const int r0 = min(w * rows, nsort), r1 = min(r0 + rows, nsort);
+    part[w][lane] = column_block_sum(hist, ntiles, t, r0, r1);
+    __syncthreads();
+    if (w == 0 && t < ntiles) {
+        uint32_t s = 0;
+        for (int k = 0; k < kColWarps; k++)
+            s += part[k][lane];
+        totals[t] = s;
+    }
 }
 
 constexpr int kScanThreads = 1024;
@@ -337,18 +384,44 @@ __global__ void __launch_bounds__(kScanThreads)
     }
 }
 
-__global__ void k_sort_offsets(uint32_t *__restrict__ hist, int nsort, int ntiles,
-                               const uint32_t *__restrict__ tile_start)
+// Histogram rows -> each CTA's first slot per tile, in place: tile t's
+// column becomes tile_start[t] plus the exclusive prefix sum down the column.
+// Same blocking as k_sort_colsum: block sums, an exclusive scan of the 32
+// block sums per tile in shared memory, then each warp rewrites its block.
+__global__ void __launch_bounds__(32 * kColWarps)
+    k_sort_offsets(uint32_t *__restrict__ hist, int nsort, int ntiles,
+                   const uint32_t *__restrict__ tile_start)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t part[kColWarps][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + lane;
+    const int rows = (nsort + kColWarps - 1) / kColWarps;
+    const int r0 = min(w * rows, nsort), r1 = min(r0 + rows, nsort);
+    part[w][lane] = column_block_sum(hist, ntiles, t, r0, r1);
+    __syncthreads();
+    if (w == 0) {
+        uint32_t run = t < ntiles ? tile_start[t] : 0u;
+        for (int k = 0; k < kColWarps; k++) {
+            const uint32_t v = part[k][lane];
+            part[k][lane] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
     if (t >= ntiles)
         return;
-    uint32_t run = tile_start[t];
-    for (int c = 0; c < nsort; c++) {
-        const size_t k = (size_t)c * ntiles + t;
-        const uint32_t v = hist[k];
-        hist[k] = run;
-        run += v;
+    uint32_t run = part[w][lane];
+    for (int c = r0; c < r1; c += 8) {  // eight loads in flight, then eight stores
+        uint32_t v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            v[q] = c + q < r1 ? hist[(size_t)(c + q) * ntiles + t] : 0u;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (c + q < r1)
+                hist[(size_t)(c + q) * ntiles + t] = run;
+            run += v[q];
+        }
     }
 }
 
@@ -404,14 +477,20 @@ __global__ void __launch_bounds__(kSortThreads)
         a[0] = a[1] = a[2] = AxisQ{0, 0u, 1.f, 0.f};
         if (in && !particle_cell(p, v[0], v[1], v[2], m, a, t))
             t = kNoTile;
-        const unsigned peers = __match_any_sync(0xffffffffu, t);
-        const int leader = __ffs(peers) - 1;
-        uint32_t slot0 = 0;
-        if (t != kNoTile && lane == leader)
-            slot0 = atomicAdd(&cur[t], (uint32_t)__popc(peers));
-        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+        uint32_t slot = 0;
+        if (!warp_has_tile_runs(t)) {
+            if (t != kNoTile)
+                slot = atomicAdd(&cur[t], 1u);
+        } else {
+            const unsigned peers = __match_any_sync(0xffffffffu, t);
+            const int leader = __ffs(peers) - 1;
+            uint32_t slot0 = 0;
+            if (t != kNoTile && lane == leader)
+                slot0 = atomicAdd(&cur[t], (uint32_t)__popc(peers));
+            slot = __shfl_sync(0xffffffffu, slot0, leader) + __popc(peers & ((1u << lane) - 1u));
+        }
         if (t != kNoTile) {
-            sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = pack_particle(a, m, mx, my, mz);
+            sorted[slot] = pack_particle(a, m, mx, my, mz);
             if (p.corner) {
                 const float mm = (p.masses ? m : p.umass) * mscale;
                 f2sum u = corner_factor_q(a[0], a[1], a[2]);
@@ -865,7 +944,7 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         return err;
     if ((err = cudaMemsetAsync(&dstat->alt_sum, 0, sizeof(long long), stream)) != cudaSuccess)
         return err;
-    const int tb = 256, tgrid = (g.ntiles + tb - 1) / tb;
+    const int cgrid = (g.ntiles + 31) / 32;
     const size_t hsmem = deposit_hist_smem(g);
     if (shared_hist) {
         if ((err = ensure_dynamic_smem(k_sort_hist<false>, hsmem)) != cudaSuccess)
@@ -873,7 +952,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         k_sort_hist<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.mass_part,
                                                                        dstat);
         mark("dep_hist");
-        k_sort_colsum<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.totals);
+        k_sort_colsum<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, sort_ctas, g.ntiles,
+                                                            s.totals);
         mark("dep_colsum");
     } else {
         if ((err = cudaMemsetAsync(s.totals, 0, sizeof(uint32_t) * g.ntiles, stream)) !=
@@ -890,7 +970,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         sort_ctas, a.masses ? -1.0 : (double)a.mass, 1.0 / n3, a.field_mass, a.field_sub, dstat);
     mark("dep_scan");
     if (shared_hist) {
-        k_sort_offsets<<<tgrid, tb, 0, stream>>>(s.hist, sort_ctas, g.ntiles, s.tile_start);
+        k_sort_offsets<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, sort_ctas, g.ntiles,
+                                                             s.tile_start);
         mark("dep_offsets");
         if ((err = ensure_dynamic_smem(k_sort_scatter<false>, hsmem)) != cudaSuccess)
             return err;
