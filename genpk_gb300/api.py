@@ -153,6 +153,51 @@ class Context:
                                              k.ctypes.data_as(native.c_f64p)))
         return p, c, k
 
+    def power_step(self, boxsize, pos_list, pairs, pair_masses, masses_list=None, mass=0.0):
+        """One step of the per-species loop (genpk_power_step): species s is
+        deposited into cleared field s, then the spectra of `pairs` as
+        power_multi returns them.  Repeated identical calls on device arrays
+        replay a captured CUDA graph of the whole step."""
+        ns = len(pos_list)
+        keep, pp, mp, n = [], [], [], []
+        for s in range(ns):
+            a, k, _ = _arg(pos_list[s], np.float32, "float32")
+            pp.append(a)
+            keep.append(k)
+            n.append((k.numel() if _is_torch(k) else k.size) // 3)
+            m = masses_list[s] if masses_list is not None else None
+            b, km, _ = _arg(m, np.float32, "float32")
+            mp.append(b)
+            keep.append(km)
+        ms = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, dtype=np.float64), (ns,)))
+        nn = np.ascontiguousarray(np.asarray(n, dtype=np.int64))
+        pairs = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        pm = np.ascontiguousarray(np.asarray(pair_masses, dtype=np.float64).reshape(-1, 2))
+        npair = pairs.shape[0]
+        pos_arr = (ctypes.c_void_p * ns)(*pp)
+        mass_arr = (ctypes.c_void_p * ns)(*mp) if masses_list is not None else None
+        p = np.zeros((npair, self.nrbins))
+        c = np.zeros(self.nrbins, dtype=np.int32)
+        k = np.zeros(self.nrbins)
+        rc = self.lib.genpk_power_step(self.h, ns, float(boxsize), pos_arr, mass_arr,
+                                       ms.ctypes.data_as(native.c_f64p),
+                                       nn.ctypes.data_as(native.c_i64p), npair,
+                                       pairs.ctypes.data_as(native.c_i32p),
+                                       pm.ctypes.data_as(native.c_f64p),
+                                       p.ctypes.data_as(native.c_f64p),
+                                       c.ctypes.data_as(native.c_i32p),
+                                       k.ctypes.data_as(native.c_f64p))
+        del keep
+        self._chk(rc)
+        return p, c, k
+
+    def step_use_graph(self, on: bool = True):
+        self._chk(self.lib.genpk_power_step_use_graph(self.h, 1 if on else 0))
+
+    @property
+    def step_replays(self) -> int:
+        return int(self.lib.genpk_power_step_replays(self.h))
+
     # -- adjoint --------------------------------------------------------------
     def adjoint(self, field, boxsize, pos, dl_dp, mass_norm, masses=None, mass=0.0,
                 recompute=False, grad_pos=None, grad_mass=None):
@@ -197,9 +242,8 @@ class Context:
         return out
 
     def deposit_config(self) -> dict:
-        v = [ctypes.c_int() for _ in range(4)]
-        self._chk(self.lib.genpk_deposit_config(self.h, *[ctypes.byref(x) for x in v]))
-        return {"tile": (v[0].value, v[1].value, v[2].value), "sort_ctas": v[3].value}
+        """The sorted engine's tile and sort CTAs of the latest pass."""
+        return _deposit_config(self.lib, self.h, self._chk)
 
     def set_engine(self, engine: int):
         """Deposit engine: ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW or
@@ -222,20 +266,9 @@ class Context:
         self._chk(self.lib.genpk_set_deposit_tile(self.h, tx, ty, tz))
 
     def deposit_trials(self) -> list:
-        """The sorted engine's latest tuning: [(tile, sort CTAs, ms), ...]."""
-        from . import native
-        cap = 10
-        tx = (ctypes.c_int * cap)()
-        ty = (ctypes.c_int * cap)()
-        tz = (ctypes.c_int * cap)()
-        sc = (ctypes.c_int * cap)()
-        ms = (ctypes.c_float * cap)()
-        k = self.lib.genpk_deposit_trials(self.h, ctypes.cast(tx, native.c_i32p),
-                                          ctypes.cast(ty, native.c_i32p),
-                                          ctypes.cast(tz, native.c_i32p),
-                                          ctypes.cast(sc, native.c_i32p),
-                                          ctypes.cast(ms, native.c_f32p), cap)
-        return [((tx[i], ty[i], tz[i]), sc[i], ms[i]) for i in range(max(k, 0))]
+        """The sorted engine's latest tuning: [(tile, sort CTAs, ms), ...]
+        (tile (0, 0, 0): the stream mode's trial)."""
+        return _deposit_trials(self.lib, self.h)
 
     @property
     def launches(self) -> int:
@@ -330,9 +363,54 @@ class Batch:
         """Deposit engine box i's latest pass used."""
         return int(self.lib.genpk_last_deposit_engine(self.lib.genpk_batch_box(self.h, i)))
 
+    def deposit_config(self, i: int) -> dict:
+        """Box i's sorted-engine tile and sort CTAs of its latest pass."""
+        box = self.lib.genpk_batch_box(self.h, i)
+
+        def chk(rc):
+            if rc != 0:
+                raise GenPKError(rc, "genpk_deposit_config")
+        return _deposit_config(self.lib, box, chk)
+
+    def deposit_trials(self, i: int) -> list:
+        """Box i's latest sorted-engine tuning, as Context.deposit_trials."""
+        return _deposit_trials(self.lib, self.lib.genpk_batch_box(self.h, i))
+
     @property
     def launches(self) -> int:
         return int(self.lib.genpk_batch_launches(self.h))
+
+    def use_graph(self, on: bool = True):
+        """Capture repeated identical calls in a CUDA graph and replay it (on by
+        default); False: every call issues its kernels one by one."""
+        rc = self.lib.genpk_batch_use_graph(self.h, 1 if on else 0)
+        if rc != 0:
+            raise GenPKError(rc, "genpk_batch_use_graph")
+
+    @property
+    def graph_replays(self) -> int:
+        """Calls served by a replay of the captured graph."""
+        return int(self.lib.genpk_batch_graph_replays(self.h))
+
+
+def _deposit_config(lib, h, chk) -> dict:
+    v = [ctypes.c_int() for _ in range(4)]
+    chk(lib.genpk_deposit_config(h, *[ctypes.byref(x) for x in v]))
+    return {"tile": (v[0].value, v[1].value, v[2].value), "sort_ctas": v[3].value}
+
+
+def _deposit_trials(lib, h) -> list:
+    from . import native
+    cap = 10
+    tx = (ctypes.c_int * cap)()
+    ty = (ctypes.c_int * cap)()
+    tz = (ctypes.c_int * cap)()
+    sc = (ctypes.c_int * cap)()
+    ms = (ctypes.c_float * cap)()
+    k = lib.genpk_deposit_trials(h, ctypes.cast(tx, native.c_i32p), ctypes.cast(ty, native.c_i32p),
+                                 ctypes.cast(tz, native.c_i32p), ctypes.cast(sc, native.c_i32p),
+                                 ctypes.cast(ms, native.c_f32p), cap)
+    return [((tx[i], ty[i], tz[i]), sc[i], ms[i]) for i in range(max(k, 0))]
 
 
 # ---------------------------------------------------------------------------

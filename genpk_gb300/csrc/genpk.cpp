@@ -181,6 +181,24 @@ struct genpk_ctx {
     // waiting for the pass (the batch waits once for every box)
     bool batch_mode = false;
 
+    // genpk_power_step: a CUDA graph of the whole step, captured on the second
+    // of two identical calls and replayed while they stay identical
+    struct StepGraph {
+        bool on = true;
+        bool failed = false;
+        int attempts = 0;
+        int repeats = 0;
+        bool have_last = false;
+        std::vector<unsigned char> last;  // the previous call's arguments, serialised
+        cudaGraphExec_t exec = nullptr;
+        uint64_t digest = 0;
+        int64_t launches = 0;
+        int64_t replays = 0;
+        std::vector<int> pairs;
+        std::vector<double> mass;
+        int np = 0;
+    } step;
+
     // adjoint scratch
     float *d_gcoef = nullptr;
     float *adj_buf = nullptr;  // device staging for host pos/masses/gradients
@@ -327,11 +345,12 @@ int check_field(genpk_ctx *ctx, int f)
 // Read back and clear the device's error counters.  Only the counters: the
 // rest of the status (the latest pass's mean and scale) is still needed by a
 // pass whose conversion is deferred to the transform.
-int collect_status(genpk_ctx *ctx)
+// The error counters of a status copy already on the host; non-zero ones are
+// cleared on the device and reported.
+constexpr size_t kStatusDoubles = (sizeof(DeviceStatus) + sizeof(double) - 1) / sizeof(double);
+
+int report_status(genpk_ctx *ctx, const DeviceStatus &st)
 {
-    DeviceStatus st;
-    GENPK_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
-    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     if (st.bad_particles || st.timeouts) {
         static_assert(offsetof(DeviceStatus, timeouts) == sizeof(unsigned long long),
                       "the two counters lead DeviceStatus");
@@ -345,6 +364,14 @@ int collect_status(genpk_ctx *ctx)
                         " particle(s) with non-finite or out-of-range position/mass were skipped");
     }
     return GENPK_OK;
+}
+
+int collect_status(genpk_ctx *ctx)
+{
+    DeviceStatus st;
+    GENPK_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return report_status(ctx, st);
 }
 
 DepositGeom deposit_geom(genpk_ctx *ctx, double boxsize, TileShape tile)
@@ -1101,7 +1128,8 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
 // The host side of a finished power request: count, keffs, the cached auto
 // spectra, the device status.
 int finish_power(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
-                 const double *power, int *count, double *keffs)
+                 const double *power, int *count, double *keffs,
+                 const DeviceStatus *host_status = nullptr)
 {
     const int nrb = ctx->nrbins;
     for (int b = 0; b < nrb; b++) {
@@ -1118,7 +1146,7 @@ int finish_power(genpk_ctx *ctx, int np, const int *pairs, const double *pair_ma
             ctx->auto_valid[(size_t)f] = true;
         }
     }
-    return collect_status(ctx);
+    return host_status ? report_status(ctx, *host_status) : collect_status(ctx);
 }
 
 // deferred: issue everything, the results' copy to the context's pinned
@@ -1248,7 +1276,8 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
     stage_event(ctx, "bin");
     double *dst = power;
     if (deferred) {
-        const size_t need = (size_t)np * nrb;
+        // the spectra, then a copy of the status words
+        const size_t need = (size_t)np * nrb + kStatusDoubles;
         if (ctx->h_power_cap < need) {
             GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
             cudaFreeHost(ctx->h_power);
@@ -1262,6 +1291,9 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
     }
     GENPK_CUDA(cudaMemcpyAsync(dst, ctx->d_power, sizeof(double) * np * nrb,
                                cudaMemcpyDeviceToHost, ctx->stream));
+    if (deferred)
+        GENPK_CUDA(cudaMemcpyAsync(dst + (size_t)np * nrb, ctx->d_status, sizeof(DeviceStatus),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
     stage_event(ctx, "d2h");
     if (deferred) {
         ctx->deferred.active = true;
@@ -1282,8 +1314,77 @@ int power_collect(genpk_ctx *ctx, double *power, int *count, double *keffs)
     ctx->deferred.active = false;
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     const genpk_ctx::Deferred &d = ctx->deferred;
-    memcpy(power, ctx->h_power, sizeof(double) * (size_t)d.np * ctx->nrbins);
-    return finish_power(ctx, d.np, d.pairs.data(), d.mass.data(), power, count, keffs);
+    const size_t nv = (size_t)d.np * ctx->nrbins;
+    memcpy(power, ctx->h_power, sizeof(double) * nv);
+    DeviceStatus st;
+    memcpy(&st, ctx->h_power + nv, sizeof st);
+    return finish_power(ctx, d.np, d.pairs.data(), d.mass.data(), power, count, keffs, &st);
+}
+
+// A digest of everything in the context that decides which work a call
+// issues, and where: state flags, cached choices, buffer addresses.  A batch
+// replays a captured CUDA graph of a call only while every box's digest is
+// the one it had when the call was captured.
+uint64_t issue_digest(const genpk_ctx *ctx)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](uint64_t v) {
+        for (int k = 0; k < 8; k++) {
+            h ^= (v >> (8 * k)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    };
+    auto ptr = [&mix](const void *q) { mix((uint64_t)(uintptr_t)q); };
+    for (int s : ctx->state)
+        mix((uint64_t)s);
+    for (bool v : ctx->corner_valid)
+        mix(v);
+    for (bool v : ctx->kzmajor)
+        mix(v);
+    mix((uint64_t)ctx->acc_pending);
+    mix(ctx->acc_zero);
+    mix(ctx->acc_spent);
+    mix(ctx->acc_dirty_bytes);
+    mix((uint64_t)ctx->engine);
+    mix((uint64_t)ctx->last_engine);
+    mix((uint64_t)ctx->fft_mode);
+    mix((uint64_t)ctx->ntuned);
+    mix((uint64_t)ctx->choice_next);
+    mix(ctx->tile_fixed);
+    mix((uint64_t)ctx->inject_chunk);
+    mix(ctx->pend.active);
+    mix((uint64_t)ctx->stage_n);
+    mix(ctx->deferred.active);
+    mix(ctx->c2r_made);
+    mix(ctx->c2c_kz_made);
+    mix(ctx->r2c.size());
+    for (const void *q : {(const void *)ctx->grids, (const void *)ctx->d_field_mass,
+                          (const void *)ctx->d_status, (const void *)ctx->d_xtw, (const void *)ctx->fft_work,
+                          (const void *)ctx->dscr.hist, (const void *)ctx->dscr.tile_start,
+                          (const void *)ctx->dscr.totals, (const void *)ctx->dscr.cursor,
+                          (const void *)ctx->dscr.sorted, (const void *)ctx->dscr.faces,
+                          (const void *)ctx->dscr.halo, (const void *)ctx->dscr.mass_part,
+                          (const void *)ctx->dscr.win_acc, (const void *)ctx->d_probe,
+                          (const void *)ctx->stage_pos, (const void *)ctx->stage_mass,
+                          (const void *)ctx->d_partial, (const void *)ctx->d_power,
+                          (const void *)ctx->h_power})
+        ptr(q);
+    return h;
+}
+
+// After a failed capture the host flags may describe work that never ran:
+// back to the state that assumes nothing about the accumulator.
+void forget_issue_state(genpk_ctx *ctx)
+{
+    ctx->acc_zero = false;
+    ctx->acc_dirty_bytes = 0;
+    ctx->acc_spent = false;
+    ctx->acc_pending = -1;
+    ctx->deferred.active = false;
+    for (size_t f = 0; f < ctx->state.size(); f++) {
+        ctx->state[f] = F_GRADIENT;  // holds something other than a density or spectrum
+        ctx->kzmajor[f] = false;
+    }
 }
 
 // Device copies of particle arrays for the adjoint when the caller passed host memory.
@@ -1324,6 +1425,8 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
+    if (ctx->step.exec)
+        cudaGraphExecDestroy(ctx->step.exec);
     for (auto &kv : ctx->r2c)
         cufftDestroy(kv.second);
     if (ctx->c2r_made)
@@ -1542,6 +1645,155 @@ int genpk_power_multi(genpk_ctx *ctx, int np, const int *pairs, const double *pa
         return GENPK_ERR_INVALID;
     cudaSetDevice(ctx->device);
     return power_impl(ctx, np, pairs, pair_mass, power, count, keffs);
+}
+
+int genpk_power_step(genpk_ctx *ctx, int nspecies, double boxsize, const float *const *pos,
+                     const float *const *masses, const double *mass, const int64_t *n, int np,
+                     const int *pairs, const double *pair_mass, double *power, int *count,
+                     double *keffs)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    if (nspecies < 1 || nspecies > ctx->nfields || !pos || !mass || !n || np < 1 || !pairs ||
+        !pair_mass || !power)
+        return fail(ctx, GENPK_ERR_INVALID, "genpk_power_step: bad arguments");
+    for (int q = 0; q < 2 * np; q++)
+        if (pairs[q] < 0 || pairs[q] >= nspecies)
+            return fail(ctx, GENPK_ERR_INVALID, "genpk_power_step: pair names a field past nspecies");
+    cudaSetDevice(ctx->device);
+    genpk_ctx::StepGraph &sg = ctx->step;
+    if (ctx->deferred.active)
+        return fail(ctx, GENPK_ERR_STATE, "genpk_power_step: a batch request is pending");
+
+    std::vector<unsigned char> args;
+    auto put = [&args](const void *v, size_t bytes) {
+        const unsigned char *c = static_cast<const unsigned char *>(v);
+        args.insert(args.end(), c, c + bytes);
+    };
+    put(&nspecies, sizeof nspecies);
+    put(&boxsize, sizeof boxsize);
+    put(pos, sizeof(*pos) * nspecies);
+    for (int s = 0; s < nspecies; s++) {
+        const float *m = masses ? masses[s] : nullptr;
+        put(&m, sizeof m);
+    }
+    put(mass, sizeof(*mass) * nspecies);
+    put(n, sizeof(*n) * nspecies);
+    put(&np, sizeof np);
+    put(pairs, sizeof(*pairs) * 2 * np);
+    put(pair_mass, sizeof(*pair_mass) * 2 * np);
+    if (sg.have_last && args == sg.last) {
+        sg.repeats++;
+    } else {
+        if (sg.exec)
+            cudaGraphExecDestroy(sg.exec);
+        sg.exec = nullptr;
+        sg.last = args;
+        sg.have_last = true;
+        sg.repeats = 0;
+    }
+    if (sg.exec && issue_digest(ctx) != sg.digest) {
+        cudaGraphExecDestroy(sg.exec);  // the context was used otherwise since the capture
+        sg.exec = nullptr;
+    }
+
+    auto issue = [&]() -> int {
+        ctx->batch_mode = true;
+        int rc = GENPK_OK;
+        for (int s = 0; s < nspecies && rc == GENPK_OK; s++) {
+            rc = genpk_zero(ctx, s);
+            if (rc == GENPK_OK)
+                rc = genpk_deposit(ctx, s, boxsize, pos[s], masses ? masses[s] : nullptr, mass[s],
+                                   n[s]);
+        }
+        if (rc == GENPK_OK)
+            rc = power_impl(ctx, np, pairs, pair_mass, nullptr, nullptr, nullptr, true);
+        ctx->batch_mode = false;
+        return rc;
+    };
+
+    // As for a batch: device-resident particles, no stage events.
+    bool graphable = sg.on && !sg.failed && !(ctx->flags & GENPK_FLAG_TIMING);
+    for (int s = 0; graphable && s < nspecies; s++)
+        graphable = (n[s] == 0 || is_device_ptr(pos[s])) &&
+                    (!masses || !masses[s] || is_device_ptr(masses[s]));
+    if (graphable && !sg.exec && sg.repeats >= 1) {
+        const uint64_t before = issue_digest(ctx);
+        const int64_t launched = ctx->launches;
+        bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+        const bool began = ok;
+        if (ok)
+            ok = issue() == GENPK_OK;
+        cudaGraph_t g = nullptr;
+        if (began)
+            ok = cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess && ok;
+        const bool cuda_ok = ok;
+        sg.launches = ctx->launches - launched;
+        ctx->launches = launched;  // nothing ran yet
+        sg.np = ctx->deferred.np;
+        sg.pairs = ctx->deferred.pairs;
+        sg.mass = ctx->deferred.mass;
+        const bool pending = ctx->deferred.active;
+        ctx->deferred.active = false;
+        ok = ok && pending && issue_digest(ctx) == before;  // each replay starts where this did
+        if (ok)
+            ok = cudaGraphInstantiate(&sg.exec, g, 0) == cudaSuccess;
+        if (g)
+            cudaGraphDestroy(g);
+        if (ok) {
+            sg.digest = before;
+            sg.attempts = 0;
+        } else {
+            cudaGetLastError();
+            sg.exec = nullptr;
+            if (!cuda_ok || ++sg.attempts >= 3)
+                sg.failed = true;
+            forget_issue_state(ctx);
+        }
+    }
+    if (sg.exec) {
+        if (cudaGraphLaunch(sg.exec, ctx->stream) != cudaSuccess) {
+            cudaGraphExecDestroy(sg.exec);
+            sg.exec = nullptr;
+            return fail(ctx, GENPK_ERR_CUDA, std::string("genpk_power_step: graph launch: ") +
+                                                 cudaGetErrorString(cudaGetLastError()));
+        }
+        sg.replays++;
+        ctx->launches += sg.launches;
+        ctx->deferred.active = true;
+        ctx->deferred.np = sg.np;
+        ctx->deferred.pairs = sg.pairs;
+        ctx->deferred.mass = sg.mass;
+    } else {
+        const int rc = issue();
+        if (rc != GENPK_OK) {
+            if (ctx->deferred.active)
+                power_collect(ctx, power, count, keffs);
+            return rc;
+        }
+    }
+    return power_collect(ctx, power, count, keffs);
+}
+
+int genpk_power_step_use_graph(genpk_ctx *ctx, int on)
+{
+    if (!ctx)
+        return GENPK_ERR_INVALID;
+    genpk_ctx::StepGraph &sg = ctx->step;
+    sg.on = on != 0;
+    if (!sg.on && sg.exec) {
+        cudaGraphExecDestroy(sg.exec);
+        sg.exec = nullptr;
+    }
+    sg.failed = false;
+    sg.attempts = 0;
+    sg.repeats = 0;
+    return GENPK_OK;
+}
+
+int64_t genpk_power_step_replays(const genpk_ctx *ctx)
+{
+    return ctx ? ctx->step.replays : -1;
 }
 
 double genpk_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n)
@@ -1888,15 +2140,80 @@ struct genpk_batch {
     std::vector<genpk_ctx *> box;
     int nrbins = 0;
     std::string err;
+
+    // CUDA graph of a whole call.  A call with the same arguments as the one
+    // before is captured (every box's work, forked from `origin` onto the
+    // boxes' streams and joined back) and later identical calls replay it:
+    // one graph launch per call instead of one launch per kernel.
+    bool graph_on = true;
+    bool graph_failed = false;  // a capture failed: calls stay eager
+    int graph_attempts = 0;
+    struct Args {
+        std::vector<double> boxsize, mass, norm;
+        std::vector<const float *> pos, masses;
+        std::vector<int64_t> n;
+        bool operator==(const Args &o) const
+        {
+            return boxsize == o.boxsize && mass == o.mass && norm == o.norm && pos == o.pos &&
+                   masses == o.masses && n == o.n;
+        }
+    } last;
+    bool have_last = false;
+    int repeats = 0;  // consecutive calls with the arguments in `last`
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int64_t> graph_launches;  // per box: kernels one replay launches
+    std::vector<genpk_ctx::Deferred> graph_deferred;
+    std::vector<bool> graph_issued;
+    std::vector<uint64_t> graph_digest;  // per box, at capture
+    int64_t replays = 0;
 };
+
+namespace {
+
+void drop_graph(genpk_batch *b)
+{
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+}
+
+}  // namespace
 
 void genpk_batch_destroy(genpk_batch *b)
 {
     if (!b)
         return;
+    drop_graph(b);
+    if (b->origin)
+        cudaStreamDestroy(b->origin);
+    if (b->fork)
+        cudaEventDestroy(b->fork);
+    for (cudaEvent_t e : b->join)
+        cudaEventDestroy(e);
     for (genpk_ctx *c : b->box)
         genpk_ctx_destroy(c);
     delete b;
+}
+
+int genpk_batch_use_graph(genpk_batch *b, int on)
+{
+    if (!b)
+        return GENPK_ERR_INVALID;
+    b->graph_on = on != 0;
+    if (!b->graph_on)
+        drop_graph(b);
+    b->graph_failed = false;
+    b->graph_attempts = 0;
+    b->repeats = 0;
+    return GENPK_OK;
+}
+
+int64_t genpk_batch_graph_replays(const genpk_batch *b)
+{
+    return b ? b->replays : -1;
 }
 
 int genpk_batch_create(int nboxes, const int64_t *dims, int nrbins, unsigned flags,
@@ -1972,7 +2289,7 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
             b->err = "box " + std::to_string(i) + ": " + genpk_last_error(b->box[(size_t)i]);
         }
     };
-    for (int i : order) {
+    auto issue = [&](int i) -> int {
         genpk_ctx *c = b->box[(size_t)i];
         cudaSetDevice(c->device);
         c->batch_mode = true;
@@ -1987,7 +2304,134 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
             issued[(size_t)i] = rc == GENPK_OK;
         }
         c->batch_mode = false;
-        note(i, rc);
+        return rc;
+    };
+
+    // The arguments, for the repeat test of the graph path.
+    genpk_batch::Args args;
+    args.boxsize.assign(boxsize, boxsize + nb);
+    args.mass.assign(mass, mass + nb);
+    args.norm.assign(mass_norm, mass_norm + nb);
+    args.pos.assign(pos, pos + nb);
+    args.masses.assign((size_t)nb, nullptr);
+    if (masses)
+        args.masses.assign(masses, masses + nb);
+    args.n.assign(n, n + nb);
+    const bool same = b->have_last && args == b->last;
+    if (!same) {
+        drop_graph(b);
+        b->last = args;
+        b->have_last = true;
+        b->repeats = 0;
+    } else {
+        b->repeats++;
+    }
+    // One device, no stage events (a replay does not re-record them), and
+    // particles in device memory: host input goes through host-side copies
+    // into staging buffers, which a replay would not repeat.
+    bool graphable = b->graph_on && !b->graph_failed;
+    for (int i = 0; graphable && i < nb; i++) {
+        const genpk_ctx *c = b->box[(size_t)i];
+        graphable = c->device == b->box[0]->device && !(c->flags & GENPK_FLAG_TIMING) &&
+                    (n[i] == 0 || is_device_ptr(pos[i])) &&
+                    (!masses || !masses[i] || is_device_ptr(masses[i]));
+    }
+    if (b->exec) {
+        for (int i = 0; i < nb; i++)
+            if (issue_digest(b->box[(size_t)i]) != b->graph_digest[(size_t)i] ||
+                b->box[(size_t)i]->deferred.active) {
+                drop_graph(b);  // a box was used on its own since the capture
+                break;
+            }
+    }
+    if (graphable && !b->exec && b->repeats >= 1) {
+        // Capture this call: every box's work, forked from `origin`.
+        cudaSetDevice(b->box[0]->device);
+        bool ok = true;
+        if (!b->origin)
+            ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+        while (ok && (int)b->join.size() < nb) {
+            cudaEvent_t e;
+            ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+            if (ok)
+                b->join.push_back(e);
+        }
+        std::vector<uint64_t> before((size_t)nb);
+        std::vector<int64_t> launched((size_t)nb);
+        for (int i = 0; i < nb; i++) {
+            before[(size_t)i] = issue_digest(b->box[(size_t)i]);
+            launched[(size_t)i] = b->box[(size_t)i]->launches;
+        }
+        ok = ok && cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+        bool began = ok;
+        ok = ok && cudaEventRecord(b->fork, b->origin) == cudaSuccess;
+        for (int i = 0; ok && i < nb; i++)
+            ok = cudaStreamWaitEvent(b->box[(size_t)i]->stream, b->fork, 0) == cudaSuccess;
+        for (int i : order)
+            if (ok)
+                ok = issue(i) == GENPK_OK;
+        for (int i = 0; ok && i < nb; i++)
+            ok = cudaEventRecord(b->join[(size_t)i], b->box[(size_t)i]->stream) == cudaSuccess &&
+                 cudaStreamWaitEvent(b->origin, b->join[(size_t)i], 0) == cudaSuccess;
+        cudaGraph_t g = nullptr;
+        if (began)
+            ok = cudaStreamEndCapture(b->origin, &g) == cudaSuccess && ok;
+        const bool cuda_ok = ok;
+        b->graph_launches.assign((size_t)nb, 0);
+        b->graph_deferred.assign((size_t)nb, genpk_ctx::Deferred{});
+        for (int i = 0; i < nb; i++) {
+            genpk_ctx *c = b->box[(size_t)i];
+            b->graph_launches[(size_t)i] = c->launches - launched[(size_t)i];
+            c->launches = launched[(size_t)i];  // nothing ran yet
+            b->graph_deferred[(size_t)i] = c->deferred;
+            c->deferred.active = false;
+        }
+        // The call must leave every box as it found it, so that each replay
+        // starts from the state the capture started from.
+        for (int i = 0; ok && i < nb; i++)
+            ok = issue_digest(b->box[(size_t)i]) == before[(size_t)i];
+        if (ok)
+            ok = cudaGraphInstantiate(&b->exec, g, 0) == cudaSuccess;
+        if (ok)
+            b->graph_attempts = 0;
+        if (g)
+            cudaGraphDestroy(g);
+        b->graph_issued = issued;
+        b->graph_digest = before;
+        if (!ok) {
+            // Nothing ran: run the call eagerly from a state that assumes
+            // nothing.  A call that did not leave the boxes as it found them
+            // may do so the next time (a first pass allocates, tunes, clears);
+            // a CUDA error during capture ends the graph path.
+            cudaGetLastError();
+            b->exec = nullptr;
+            if (!cuda_ok || ++b->graph_attempts >= 3)
+                b->graph_failed = true;
+            for (genpk_ctx *c : b->box)
+                forget_issue_state(c);
+            std::fill(issued.begin(), issued.end(), false);
+        }
+    }
+    if (b->exec) {
+        cudaSetDevice(b->box[0]->device);
+        if (cudaGraphLaunch(b->exec, b->origin) != cudaSuccess ||
+            cudaStreamSynchronize(b->origin) != cudaSuccess) {
+            b->err = std::string("genpk_batch_power: graph replay failed: ") +
+                     cudaGetErrorString(cudaGetLastError());
+            drop_graph(b);
+            return GENPK_ERR_CUDA;
+        }
+        b->replays++;
+        for (int i = 0; i < nb; i++) {
+            genpk_ctx *c = b->box[(size_t)i];
+            c->launches += b->graph_launches[(size_t)i];
+            c->deferred = b->graph_deferred[(size_t)i];
+        }
+        issued = b->graph_issued;
+    } else {
+        for (int i : order)
+            note(i, issue(i));
     }
     for (int i : order) {  // every issued box is waited for, even after a failure
         if (!issued[(size_t)i])

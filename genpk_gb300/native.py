@@ -16,6 +16,7 @@ _COMPAT = None
 c_f32p = ctypes.POINTER(ctypes.c_float)
 c_f64p = ctypes.POINTER(ctypes.c_double)
 c_i32p = ctypes.POINTER(ctypes.c_int)
+c_i64p = ctypes.POINTER(ctypes.c_int64)
 c_void_p = ctypes.c_void_p
 
 # name -> (restype, argtypes); exactly the functions include/genpk_gb300.h declares.
@@ -64,6 +65,13 @@ ABI = {
                                          c_f64p]),
     "genpk_batch_box": (c_void_p, [c_void_p, ctypes.c_int]),
     "genpk_batch_launches": (ctypes.c_int64, [c_void_p]),
+    "genpk_batch_use_graph": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "genpk_power_step": (ctypes.c_int, [c_void_p, ctypes.c_int, ctypes.c_double, c_void_p,
+                                        c_void_p, c_f64p, c_i64p, ctypes.c_int, c_i32p, c_f64p,
+                                        c_f64p, c_i32p, c_f64p]),
+    "genpk_power_step_use_graph": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "genpk_power_step_replays": (ctypes.c_int64, [c_void_p]),
+    "genpk_batch_graph_replays": (ctypes.c_int64, [c_void_p]),
     "genpk_power_noalloc": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_double, c_void_p, c_i32p,
                                            c_f64p, c_void_p]),

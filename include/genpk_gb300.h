@@ -115,6 +115,29 @@ int genpk_power(genpk_ctx *ctx, int field_a, int field_b, double mass_a, double 
 int genpk_power_multi(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
                       double *power, int *count, double *keffs);
 
+/* One whole step of the per-species loop: fields 0..nspecies-1 are cleared,
+ * species s (n[s] particles pos[s], masses[s] or the uniform mass[s]) is
+ * deposited into field s, and the spectra pairs[2*np] (field indices below
+ * nspecies, normalisation masses pair_mass[2*np]) come back as
+ * genpk_power_multi returns them.  The gen-pk loop of gen-pk.cpp:204-356 (one
+ * fieldize per type, the FFTs, powerspectrum per auto and cross pair) in one
+ * call.  Repeated calls with the same arguments (the same arrays, counts,
+ * masses and pairs; the arrays' contents may change) replay a CUDA graph of
+ * the whole step, captured on the second such call, when every array is in
+ * device memory and the context has no GENPK_FLAG_TIMING: the same results
+ * bit for bit, one launch per step.  Any other use of the context between
+ * steps drops the graph (the next identical step captures it again). */
+int genpk_power_step(genpk_ctx *ctx, int nspecies, double boxsize, const float *const *pos,
+                     const float *const *masses, const double *mass, const int64_t *n, int np,
+                     const int *pairs, const double *pair_mass, double *power, int *count,
+                     double *keffs);
+
+/* Graphs for genpk_power_step on (1, the default) or off (0; drops one). */
+int genpk_power_step_use_graph(genpk_ctx *ctx, int on);
+
+/* genpk_power_step calls served by a graph replay, or -1 for a null ctx. */
+int64_t genpk_power_step_replays(const genpk_ctx *ctx);
+
 /* The reference's inverse CIC window, fieldize.cpp:125-133 (host function). */
 double genpk_invwindow(int64_t kx, int64_t ky, int64_t kz, int64_t n);
 
@@ -243,7 +266,8 @@ const char *genpk_batch_last_error(const genpk_batch *b);
  * count and keffs are [nboxes][nrbins] host arrays (count and keffs may be
  * NULL).  One host thread issues every box's deposit, transform and binning,
  * largest box first, each on its box's stream, so that the boxes overlap on
- * the GPU, then waits once per box for the results; the deposit engine of each
+ * the GPU, then waits once per box for the results (a repeated call replays a
+ * captured CUDA graph of all of it: genpk_batch_use_graph); the deposit engine of each
  * box is chosen as genpk_deposit chooses it (and remembered for the same
  * arrays).  Particle arrays may be host or device memory; pinned host and
  * device arrays are read while other boxes' work runs and must stay valid
@@ -256,8 +280,27 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
 /* Box i's context (for its stage times, engine and configuration), or NULL. */
 genpk_ctx *genpk_batch_box(genpk_batch *b, int i);
 
-/* Kernels launched by all the batch's boxes since creation. */
+/* Kernels launched by all the batch's boxes since creation (a graph replay
+ * counts the kernels it launches). */
 int64_t genpk_batch_launches(const genpk_batch *b);
+
+/* CUDA graph of a whole call (on by default).  The second of two
+ * consecutive genpk_batch_power calls with the same arguments (the same
+ * arrays, counts, box sizes and masses; the arrays' contents may change) is
+ * captured: every box's work is forked from one stream onto the boxes'
+ * streams and joined back.  Later identical calls replay the graph with one
+ * launch; results are identical to the eager path's, bit for bit.  A call
+ * with other arguments runs eagerly and drops the graph, and so does any use
+ * of a box's context on its own between calls.  The capture is kept only if
+ * the call leaves every box's state as it found it; otherwise the call runs
+ * eagerly and a later identical call tries again (three tries; a CUDA error
+ * during capture ends the graph path).  Boxes created with GENPK_FLAG_TIMING
+ * always run eagerly (stage events are not re-recorded by a replay).
+ * on = 0 turns graphs off (and drops one), 1 turns them back on. */
+int genpk_batch_use_graph(genpk_batch *b, int on);
+
+/* Calls served by a graph replay since creation, or -1 for a null batch. */
+int64_t genpk_batch_graph_replays(const genpk_batch *b);
 
 /* Testing aid for the bounded device waits (no reference counterpart; the
  * reference has no device code).  The next window- or stream-engine deposit

@@ -83,3 +83,70 @@ def test_batch_reports_a_failing_box_and_stays_usable(gp):
         assert e.value.status == 5 and "box 1" in str(e.value)
         p, c, _ = b.power(box, [good, good], m, mass=1.0)
     assert np.array_equal(p[0], p[1])
+
+
+def test_batch_graph_replay_matches_eager_calls(gp):
+    """Repeated identical calls: the second is captured as one CUDA graph and
+    later ones replay it.  Every replay gives the eager path's spectra bit for
+    bit, also after the positions change in place (a replay reads the arrays'
+    current contents), after a new array (eager again, then a new capture) and
+    after a box's context is used on its own (the graph is dropped)."""
+    import torch
+    from genpk_gb300 import synth
+    box, nrbins = 1000.0, 20
+    dims = [64, 32, 128, 64]
+    pos = [torch.from_numpy(synth.zeldovich(64, box, seed=31)).cuda(),
+           torch.from_numpy(synth.uniform(50_000, box, seed=32)).cuda(),
+           torch.from_numpy(synth.uniform(3_000_000, box, seed=33)).cuda(),
+           torch.from_numpy(synth.uniform(400_000, box, seed=34)).cuda()]
+    masses = [None, None, None,
+              torch.from_numpy(np.random.default_rng(35).lognormal(0.0, 0.4, 400_000)
+                               .astype(np.float32)).cuda()]
+    mass = [1.0, 0.5, 2.0, 0.0]
+
+    def norms():
+        return [O.total_mass(len(p), None if m is None else m.cpu().numpy(), mu)
+                for p, m, mu in zip(pos, masses, mass)]
+
+    def same(a, b):
+        return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+    with gp.Batch(dims, nrbins) as g, gp.Batch(dims, nrbins) as e:
+        e.use_graph(False)
+        ref = e.power(box, pos, norms(), masses_list=masses, mass=mass)
+        outs = [g.power(box, pos, norms(), masses_list=masses, mass=mass) for _ in range(2)]
+        l0 = g.launches  # (the first call's tuning trials and probes are not steady state)
+        outs += [g.power(box, pos, norms(), masses_list=masses, mass=mass) for _ in range(3)]
+        r5 = g.graph_replays
+        assert r5 == 4, r5  # call 2 is captured and replayed, calls 3-5 replay
+        assert e.graph_replays == 0
+        assert all(same(o, ref) for o in outs)
+        per_call = (g.launches - l0) / 3
+        le = e.launches
+        e.power(box, pos, norms(), masses_list=masses, mass=mass)
+        assert per_call == e.launches - le  # a replay counts the kernels it launches
+
+        # new contents, same arrays (and the same normalising masses, which are
+        # arguments): replayed, equal to the eager path
+        nm = norms()
+        with torch.no_grad():
+            pos[2].mul_(0.5)
+            masses[3].mul_(1.5)
+        r = g.power(box, pos, nm, masses_list=masses, mass=mass)
+        assert g.graph_replays == r5 + 1
+        assert same(r, e.power(box, pos, nm, masses_list=masses, mass=mass))
+
+        # a new array for box 1: eager, then captured again on the next repeat
+        pos[1] = torch.from_numpy(synth.uniform(60_000, box, seed=36)).cuda()
+        refn = e.power(box, pos, norms(), masses_list=masses, mass=mass)
+        for k in range(3):
+            assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
+        assert g.graph_replays == r5 + 3  # eager, captured + replayed, replayed
+
+        # box 0's context used on its own: the graph is dropped, the call eager
+        lib = g.lib
+        assert lib.genpk_zero(lib.genpk_batch_box(g.h, 0), 0) == 0
+        assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
+        assert g.graph_replays == r5 + 3
+        assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
+        assert g.graph_replays == r5 + 4
