@@ -77,7 +77,30 @@ def parse():
                          "512^3 grid, 3 auto + 3 cross spectra per step; boxes: 16 boxes of "
                          "uniform particles, counts log-uniform in [1e5, 3e7], grids 128^3 or "
                          "256^3, one auto spectrum each per step")
+    ap.add_argument("--profile-timed", action="store_true",
+                    help="open the CUDA profiler range (cudaProfilerStart/Stop) around the timed "
+                         "steps only, for `ncu --profile-from-start off`: set-up, tuning and "
+                         "warm-up launches stay out of a launch list")
     return ap.parse_args()
+
+
+class ProfiledRange:
+    """cudaProfilerStart/Stop around a block when enabled (no effect otherwise)."""
+
+    def __init__(self, on):
+        self.on = on
+
+    def __enter__(self):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
 
 
 def peaks():
@@ -251,14 +274,48 @@ def particle_mass(args):
     return 1.0e-2 if args.workload == "uniform" else 1.0
 
 
+L2_BYTES = 129 * 2 ** 20  # GB300 L2 (queried on the device where torch reports it)
+
+
+def l2_bytes():
+    try:
+        import torch
+        return int(getattr(torch.cuda.get_device_properties(0), "L2_cache_size", L2_BYTES))
+    except Exception:
+        return L2_BYTES
+
+
+def needs_l2_flush(npart):
+    """Positions smaller than twice the L2 would be served from it on the next
+    step: such runs write a buffer larger than the L2 between steps."""
+    return npart * 12 < 2 * l2_bytes()
+
+
 def config_dict(args, npart):
     kind = ("uniform random particles (mass 1e-2)" if args.workload == "uniform"
             else "Zel'dovich lattice particles")
+    l2 = (f"L2 flushed between steps (a {2 * l2_bytes() / 1e6:.0f} MB buffer written outside "
+          f"the stage events; {npart * 12 / 1e9:.3f} GB of positions per step)"
+          if needs_l2_flush(npart)
+          else f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions per step)")
     return {"workload": (f"{kind}, {args.nside}^3 particles, L={args.box:g} kpc/h, "
                          f"FP32 {args.grid}^3 grid, {args.nrbins} log-k bins, auto spectrum"),
             "particles": npart, "grid": args.grid, "nrbins": args.nrbins, "boxsize": args.box,
-            "l2": f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions per step)",
-            "parallelism": "replicas (one independent box per GPU)"}
+            "l2": l2, "parallelism": "replicas (one independent box per GPU)"}
+
+
+def tuning_record(cfg, trials, engine):
+    """The deposit engine a context used and, for the sorted engine, its tile,
+    sort CTAs and the autotuner's timed trials."""
+    label = lambda t: "stream" if t == (0, 0, 0) else "x".join(str(v) for v in t)
+    rec = {"engine": engine}
+    if engine == "sorted":
+        rec["tile"] = label(cfg["tile"])
+        rec["sort_ctas"] = cfg["sort_ctas"]
+    if trials:
+        rec["trials_ms"] = [[label(t) + ("" if t == (0, 0, 0) else f"/{c}"), round(float(ms), 4)]
+                            for t, c, ms in trials]
+    return rec
 
 
 # ---------------------------------------------------------------------------
@@ -306,11 +363,12 @@ def multispecies(args):
     torch.cuda.synchronize()
     dev_ms, stages = [], {}
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        p, c, st = step()
-        dev_ms.append(sum(st.values()))
-        for key, v in st.items():
-            stages[key] = stages.get(key, 0.0) + v
+    with ProfiledRange(args.profile_timed):
+        for _ in range(args.steps):
+            p, c, st = step()
+            dev_ms.append(sum(st.values()))
+            for key, v in st.items():
+                stages[key] = stages.get(key, 0.0) + v
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ms_step = float(np.mean(dev_ms))
@@ -322,11 +380,30 @@ def multispecies(args):
             "data": "synthetic: Zel'dovich DM and gas on the GPU, lognormal stars (numpy)",
             "config": {"workload": "DM 256^3 + gas 256^3 + 1.2e7 stars, 512^3 grid, "
                                    f"{nrbins} bins, 3 auto + 3 cross spectra",
-                       "particles": npart, "grid": n, "nrbins": nrbins, "boxsize": box},
+                       "particles": npart, "grid": n, "nrbins": nrbins, "boxsize": box,
+                       "l2": f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions and "
+                             "three 1.08 GB grids per step)"},
             "wall_ms_per_step": wall / args.steps * 1e3,
             "stages_ms": {k: round(v / args.steps, 5) for k, v in stages.items()},
             "deposit_engines": "per species, automatic"}
     ctx.close()
+    # The same step through genpk_power_step on a context without stage events:
+    # repeated identical steps replay one captured CUDA graph of the whole step.
+    # Wall clock per step (each call returns with the spectra on the host).
+    gctx = gp.Context(n, nrbins, nfields=3)
+    gctx.set_fft_mode({"auto": 0, "cufft3d": 1}[args.fft])
+    spec_pos, spec_m, spec_mu = [dm, gas, stars], [None, None, smass_d], [1.0, 0.19, 0.0]
+    for _ in range(max(args.warmup, 3)):
+        gctx.power_step(box, spec_pos, pairs, pm, masses_list=spec_m, mass=spec_mu)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pg, cg, _ = gctx.power_step(box, spec_pos, pairs, pm, masses_list=spec_m, mass=spec_mu)
+    g_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    line["graph_step"] = {"api": "genpk_power_step (one call per step)",
+                          "wall_ms_per_step": g_ms, "graph_replays": gctx.step_replays,
+                          "same_as_calls": bool(np.array_equal(pg, p) and np.array_equal(cg, c))}
+    gctx.close()
     if not args.no_cpu:
         # every bin of the 6 spectra against the FP64 oracle (deposit, r2c, binning)
         import scipy.fft as sfft
@@ -403,7 +480,8 @@ def boxes(args):
     for _ in range(args.warmup):
         res = step(pos)
     launches0 = b.launches
-    t_dev = timed(pos, args.steps)
+    with ProfiledRange(args.profile_timed):
+        t_dev = timed(pos, args.steps)
     launches = (b.launches - launches0) / args.steps
     npart = sum(c for c, _, _ in batch)
     line = {"metric": "particles/s + ms per batch (16 boxes, one auto spectrum each)",
@@ -416,11 +494,22 @@ def boxes(args):
                                    f"kpc/h, mass {mass:g}, {nrbins} bins",
                        "boxes": [{"particles": c, "grid": g} for c, g, _ in batch],
                        "particles": npart, "host_threads": 1,
-                       "api": "genpk_batch_power (one call per batch)",
+                       "l2": f"inputs larger than L2 ({npart * 12 / 1e9:.2f} GB of positions "
+                             f"per batch, every box read once per step)",
+                       "api": "genpk_batch_power (one call per batch; from the second "
+                              "identical call on, one replay of a captured CUDA graph)",
                        "timing": "wall clock per batch, device synchronised on both sides"},
             "gpu_launches": launches,
             "engines": [("sorted", "window", "stream")[b.engine(i) - 1]
                         for i in range(len(batch))]}
+    line["deposit_tuning"] = [tuning_record(b.deposit_config(i), b.deposit_trials(i),
+                                            line["engines"][i]) for i in range(len(batch))]
+    line["graph_replays"] = b.graph_replays
+    b.use_graph(False)  # the same batch issued kernel by kernel, for comparison
+    for _ in range(2):
+        step(pos)
+    line["eager_ms_per_step"] = timed(pos, args.steps) * 1e3
+    b.use_graph(True)
     if not args.no_e2e:
         hpos = [p.cpu().pin_memory() for p in pos]
         step(hpos)
@@ -471,7 +560,12 @@ def main():
     ctx.set_engine({"auto": 0, "sorted": 1, "window": 2, "stream": 3}[args.engine])
     ctx.set_fft_mode({"auto": 0, "cufft3d": 1}[args.fft])
 
-    def step(src):
+    flush = (torch.empty(2 * l2_bytes(), dtype=torch.uint8, device="cuda")
+             if needs_l2_flush(npart) else None)
+
+    def step(src, flush_l2=True):
+        if flush is not None and flush_l2:  # (host input is read over the link anyway)
+            flush.fill_(1)
         ctx.timing_reset()
         ctx.zero(0)
         ctx.deposit(0, box, src, None, mass)
@@ -493,11 +587,12 @@ def main():
     launches0 = ctx.launches
     t0 = time.perf_counter()
     dev_ms, stages = [], {}
-    for _ in range(args.steps):
-        p, c, st = step(dpos)
-        dev_ms.append(sum(st.values()))
-        for key, v in st.items():
-            stages[key] = stages.get(key, 0.0) + v
+    with ProfiledRange(args.profile_timed):
+        for _ in range(args.steps):
+            p, c, st = step(dpos)
+            dev_ms.append(sum(st.values()))
+            for key, v in st.items():
+                stages[key] = stages.get(key, 0.0) + v
     barrier()
     wall = time.perf_counter() - t0
     launches = ctx.launches - launches0
@@ -550,7 +645,8 @@ def main():
             "wall_ms_per_step": wall / args.steps * 1e3,
             "stages_ms": {k: round(v, 5) for k, v in stages.items()},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
-            "deposit_engine": engine}
+            "deposit_engine": engine,
+            "deposit_tuning": tuning_record(ctx.deposit_config(), ctx.deposit_trials(), engine)}
 
     # end to end through the C ABI from pinned host memory (before the adjoint
     # section: after it, the host-link reads of a newly pinned buffer were
@@ -558,12 +654,12 @@ def main():
     if not args.no_e2e:
         hpos = dpos.cpu().pin_memory()
         for _ in range(2):
-            step(hpos)
+            step(hpos, flush_l2=False)
         torch.cuda.synchronize()
         e2e_t = []
         for _ in range(max(3, min(args.steps, 20))):
             t1 = time.perf_counter()
-            step(hpos)
+            step(hpos, flush_l2=False)
             e2e_t.append(time.perf_counter() - t1)
         e_ms = max_over_ranks(float(np.mean(e2e_t)) * 1e3, world)
         line["e2e"] = {"value": job_throughput(npart, world, e_ms), "unit": "particles/s",
