@@ -430,6 +430,9 @@ int density_band(const genpk_ctx *ctx, int64_t n)
 }
 
 constexpr int64_t kTuneMinParticles = (int64_t)1 << 16;
+// Timed runs per candidate (the fastest counts): single runs of a small pass
+// varied by 10-20 %, enough to flip close choices from run to run.
+constexpr int kTuneReps = 2;
 
 // The deposit autotuner for particle orders without spatial coherence.  On
 // the first clean pass of a density band (and mass kind) it runs the pass once
@@ -493,17 +496,22 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
         size_t mp = (size_t)ctx->dscr.mass_part_cap;
         GENPK_TRY(grow(ctx, &ctx->dscr.mass_part, &mp, (size_t)mass_ctas));
         ctx->dscr.mass_part_cap = (int)mp;
-        GENPK_TRY(reset_field());
-        GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
-        GENPK_CUDA(deposit_window_pass(g, a, stream_chunk(a.n, a.masses != nullptr, ctx->num_sms),
-                                       true, ctx->dscr.mass_part, mass_ctas,
-                                       ctx->dscr.win_acc, acc_bytes(ctx), false, ctx->num_sms,
-                                       ctx->d_status, ctx->stream, &ctx->launches, nullptr,
-                                       nullptr));
-        GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
-        GENPK_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        GENPK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        float ms = 1e30f;
+        for (int rep = 0; rep < kTuneReps; rep++) {
+            GENPK_TRY(reset_field());
+            GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
+            GENPK_CUDA(deposit_window_pass(g, a,
+                                           stream_chunk(a.n, a.masses != nullptr, ctx->num_sms),
+                                           true, ctx->dscr.mass_part, mass_ctas,
+                                           ctx->dscr.win_acc, acc_bytes(ctx), false, ctx->num_sms,
+                                           ctx->d_status, ctx->stream, &ctx->launches, nullptr,
+                                           nullptr));
+            GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
+            GENPK_CUDA(cudaEventSynchronize(e1));
+            float t = 0.f;
+            GENPK_CUDA(cudaEventElapsedTime(&t, e0, e1));
+            ms = std::min(ms, t);
+        }
         ctx->acc_zero = false;  // it holds the trial's sums
         ctx->acc_dirty_bytes = 0;
         ctx->acc_spent = true;
@@ -525,14 +533,18 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
                 continue;
             last_ctas = ctas;
             GENPK_TRY(grow_sorted_scratch(ctx, g, a.n, ctas));
-            GENPK_TRY(reset_field());
-            GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
-            GENPK_CUDA(deposit_pass(g, a, ctx->dscr, ctx->d_status, ctas, ctx->stream,
-                                    &ctx->launches, nullptr, nullptr));
-            GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
-            GENPK_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            GENPK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            float ms = 1e30f;
+            for (int rep = 0; rep < kTuneReps; rep++) {
+                GENPK_TRY(reset_field());
+                GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
+                GENPK_CUDA(deposit_pass(g, a, ctx->dscr, ctx->d_status, ctas, ctx->stream,
+                                        &ctx->launches, nullptr, nullptr));
+                GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
+                GENPK_CUDA(cudaEventSynchronize(e1));
+                float t = 0.f;
+                GENPK_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                ms = std::min(ms, t);
+            }
             if (ctx->ntrials < genpk_ctx::kMaxTrials) {
                 ctx->trial_tile[ctx->ntrials] = t;
                 ctx->trial_ctas[ctx->ntrials] = ctas;
