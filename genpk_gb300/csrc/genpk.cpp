@@ -99,7 +99,7 @@ struct genpk_ctx {
         bool with_stream = false;         // the stream engine was among the trials
         int engine = GENPK_ENGINE_SORTED;  // the faster: SORTED (tile, per_sm) or STREAM
         TileShape tile{16, 16, 16};
-        int per_sm = 4;
+        int per_sm = 1;
     };
     static constexpr int kTuned = 16;
     Tuned tuned[kTuned];
@@ -452,8 +452,9 @@ int tune_sorted(genpk_ctx *ctx, int f, double boxsize, const DepositArgs &a, boo
 {
     static const TileShape tiles[] = {{8, 8, 8}, {16, 16, 8}, {16, 16, 16}};
     // sort CTAs per SM: fewer CTAs give each (CTA, tile) run of the scatter
-    // more particles, so its 16-byte records share sectors in the L2
-    static const int pers[] = {1, 2, 4};
+    // more particles, so its 16-byte records share sectors in the L2; more
+    // shorten a CTA's range (two waves of 1024-thread CTAs)
+    static const int pers[] = {1, 2};
     const size_t stash = 0;  // the error counters are kept in the probe buffer meanwhile
     GENPK_TRY(grow(ctx, &ctx->d_probe, &ctx->probe_cap, (size_t)4));
     GENPK_CUDA(cudaMemcpyAsync(ctx->d_probe + stash, ctx->d_status, 2 * sizeof(long long),
@@ -758,7 +759,7 @@ int run_deposit(genpk_ctx *ctx, int f, double boxsize, const float *pos, const f
             ctx->acc_pending = f;
     } else {
         TileShape tile = ctx->tile;
-        int per_sm = 4;
+        int per_sm = 1;
         if (tuned) {
             tile = tuned->tile;
             per_sm = tuned->per_sm;

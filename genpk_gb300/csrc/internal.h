@@ -108,7 +108,7 @@ bool deposit_tile_supported(int tx, int ty, int tz);
 TileShape deposit_default_tile(int dims, int64_t n);
 // Sort CTAs of a pass: up to max_per_sm per SM (fewer where the per-CTA tile
 // histogram leaves no room), and no more than one per 4096 particles.
-int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms, int max_per_sm = 4);
+int deposit_sort_ctas(const DepositGeom &g, int64_t n, int num_sms, int max_per_sm = 1);
 size_t deposit_hist_smem(const DepositGeom &g);
 // True when the per-CTA tile histogram fits in shared memory (else the pass
 // uses global counters).

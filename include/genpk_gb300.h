@@ -196,9 +196,9 @@ int genpk_deposit_config(const genpk_ctx *ctx, int *tile_x, int *tile_y, int *ti
 
 /* The deposit autotuner, for passes whose particle order has no spatial
  * coherence: on the first clean pass of each particle density band (half
- * octaves of particles per cell) and mass kind, the pass runs once per
+ * octaves of particles per cell) and mass kind, the pass runs twice per
  * candidate -- the sorted engine with tiles 8^3, 16x16x8 and 16^3, each with
- * up to 1, 2 and 4 sort CTAs per SM, and, when the engine is automatic,
+ * 1 and 2 sort CTAs per SM, and, when the engine is automatic,
  * the stream engine -- timed with CUDA events, and the fastest is kept for
  * that band.  Every candidate writes the same grid.  This returns the latest
  * tuning's trials (at most cap, the number written): tile edges (0 x 0 x 0
