@@ -143,10 +143,25 @@ def test_batch_graph_replay_matches_eager_calls(gp):
             assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
         assert g.graph_replays == r5 + 3  # eager, captured + replayed, replayed
 
+        # a non-finite position written into box 2's array after the capture:
+        # the replay reports it for that box, and the batch stays usable
+        with torch.no_grad():
+            keep = pos[2][7, 0].item()
+            pos[2][7, 0] = float("nan")
+        r0 = g.graph_replays
+        with pytest.raises(gp.api.GenPKError) as err:
+            g.power(box, pos, norms(), masses_list=masses, mass=mass)
+        assert err.value.status == 5 and "box 2" in err.value.message
+        assert g.graph_replays == r0 + 1
+        with torch.no_grad():
+            pos[2][7, 0] = keep
+        assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
+        assert g.graph_replays == r0 + 2
+
         # box 0's context used on its own: the graph is dropped, the call eager
         lib = g.lib
         assert lib.genpk_zero(lib.genpk_batch_box(g.h, 0), 0) == 0
         assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
-        assert g.graph_replays == r5 + 3
+        assert g.graph_replays == r0 + 2
         assert same(g.power(box, pos, norms(), masses_list=masses, mass=mass), refn)
-        assert g.graph_replays == r5 + 4
+        assert g.graph_replays == r0 + 3
