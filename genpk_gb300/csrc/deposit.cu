@@ -93,12 +93,12 @@ struct SortParams {
 };
 
 // Threads of a sort CTA (a CTA's particle range does not depend on them).
-// The histogram pass runs 1024 per CTA: at one CTA per SM (the long per-tile
-// runs that let the scatter's 16-byte records share L2 sectors) its 32 warps
-// cover the loads' latency (0.20 -> 0.14 ms for 27 M particles on 256^3).  The
-// scatter keeps 512: with 1024 it took 0.65 ms against 0.59.
+// 1024 per CTA: at one CTA per SM (the long per-tile runs that let the
+// scatter's 16-byte records share L2 sectors) 32 warps cover the loads'
+// latency.  Against 512, timed in one run: the histogram pass 0.20 -> 0.14 ms
+// for 27 M random particles on 256^3, the scatter 1.17 -> 1.00 ms on the 512^3
+// lattice, the 16-box batch 6.1 -> 5.4 ms.
 constexpr int kSortThreads = 1024;
-constexpr int kScatterThreads = 512;
 constexpr int kSortUnroll = 4;
 constexpr uint32_t kNoTile = 0xffffffffu;
 
@@ -459,7 +459,7 @@ __device__ __forceinline__ uint4 pack_particle(const AxisQ a[3], float m, uint32
 // (deterministic: fixed per-thread order, integer sums across warps).  The last log-k bin holds only
 // this mode, so its value must not carry the FP32 grid's rounding noise.
 template <bool GLOBAL>
-__global__ void __launch_bounds__(kScatterThreads)
+__global__ void __launch_bounds__(kSortThreads)
     k_sort_scatter(SortParams p, uint32_t *__restrict__ offs, uint4 *__restrict__ sorted,
                    DeviceStatus *st)
 {
@@ -981,10 +981,10 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         mark("dep_offsets");
         if ((err = ensure_dynamic_smem(k_sort_scatter<false>, hsmem)) != cudaSuccess)
             return err;
-        k_sort_scatter<false><<<sort_ctas, kScatterThreads, hsmem, stream>>>(sp, s.hist, s.sorted,
+        k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted,
                                                                          dstat);
     } else {
-        k_sort_scatter<true><<<sort_ctas, kScatterThreads, 0, stream>>>(sp, s.cursor, s.sorted,
+        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.cursor, s.sorted,
                                                                        dstat);
     }
     mark("dep_scatter");
