@@ -566,6 +566,7 @@ def main():
     def step(src, flush_l2=True):
         if flush is not None and flush_l2:  # (host input is read over the link anyway)
             flush.fill_(1)
+            torch.cuda.synchronize()  # the library's stream does not wait for torch's
         ctx.timing_reset()
         ctx.zero(0)
         ctx.deposit(0, box, src, None, mass)

@@ -1385,20 +1385,43 @@ uint64_t issue_digest(const genpk_ctx *ctx)
     return h;
 }
 
-// After a failed capture the host flags may describe work that never ran:
-// back to the state that assumes nothing about the accumulator.
-void forget_issue_state(genpk_ctx *ctx)
-{
-    ctx->acc_zero = false;
-    ctx->acc_dirty_bytes = 0;
-    ctx->acc_spent = false;
-    ctx->acc_pending = -1;
-    ctx->deferred.active = false;
-    for (size_t f = 0; f < ctx->state.size(); f++) {
-        ctx->state[f] = F_GRADIENT;  // holds something other than a density or spectrum
-        ctx->kzmajor[f] = false;
+// The host-side record of what the device holds, which issuing a call
+// updates as if its work had run.  A capture that fails runs nothing, so the
+// record taken before it is put back.
+struct IssueState {
+    std::vector<int> state;
+    std::vector<bool> corner_valid, kzmajor, auto_valid;
+    std::vector<double> auto_mass;
+    std::vector<std::vector<double>> auto_power;
+    int acc_pending = -1;
+    bool acc_zero = false, acc_spent = false;
+    size_t acc_dirty_bytes = 0;
+    int last_engine = 0;
+    genpk_ctx::Deferred deferred;
+
+    explicit IssueState(const genpk_ctx *c)
+        : state(c->state), corner_valid(c->corner_valid), kzmajor(c->kzmajor),
+          auto_valid(c->auto_valid), auto_mass(c->auto_mass), auto_power(c->auto_power),
+          acc_pending(c->acc_pending), acc_zero(c->acc_zero), acc_spent(c->acc_spent),
+          acc_dirty_bytes(c->acc_dirty_bytes), last_engine(c->last_engine), deferred(c->deferred)
+    {
     }
-}
+    void restore(genpk_ctx *c) const
+    {
+        c->state = state;
+        c->corner_valid = corner_valid;
+        c->kzmajor = kzmajor;
+        c->auto_valid = auto_valid;
+        c->auto_mass = auto_mass;
+        c->auto_power = auto_power;
+        c->acc_pending = acc_pending;
+        c->acc_zero = acc_zero;
+        c->acc_spent = acc_spent;
+        c->acc_dirty_bytes = acc_dirty_bytes;
+        c->last_engine = last_engine;
+        c->deferred = deferred;
+    }
+};
 
 // Device copies of particle arrays for the adjoint when the caller passed host memory.
 int adj_stage(genpk_ctx *ctx, size_t floats)
@@ -1732,6 +1755,7 @@ int genpk_power_step(genpk_ctx *ctx, int nspecies, double boxsize, const float *
                     (!masses || !masses[s] || is_device_ptr(masses[s]));
     if (graphable && !sg.exec && sg.repeats >= 1) {
         const uint64_t before = issue_digest(ctx);
+        const IssueState saved(ctx);
         const int64_t launched = ctx->launches;
         bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
         const bool began = ok;
@@ -1761,7 +1785,7 @@ int genpk_power_step(genpk_ctx *ctx, int nspecies, double boxsize, const float *
             sg.exec = nullptr;
             if (!cuda_ok || ++sg.attempts >= 3)
                 sg.failed = true;
-            forget_issue_state(ctx);
+            saved.restore(ctx);  // nothing ran
         }
     }
     if (sg.exec) {
@@ -2372,9 +2396,11 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
         }
         std::vector<uint64_t> before((size_t)nb);
         std::vector<int64_t> launched((size_t)nb);
+        std::vector<IssueState> saved;
         for (int i = 0; i < nb; i++) {
             before[(size_t)i] = issue_digest(b->box[(size_t)i]);
             launched[(size_t)i] = b->box[(size_t)i]->launches;
+            saved.emplace_back(b->box[(size_t)i]);
         }
         ok = ok && cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed) == cudaSuccess;
         bool began = ok;
@@ -2413,16 +2439,16 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
         b->graph_issued = issued;
         b->graph_digest = before;
         if (!ok) {
-            // Nothing ran: run the call eagerly from a state that assumes
-            // nothing.  A call that did not leave the boxes as it found them
-            // may do so the next time (a first pass allocates, tunes, clears);
-            // a CUDA error during capture ends the graph path.
+            // Nothing ran: put back each box's record of its device state and
+            // run the call eagerly.  A call that did not leave the boxes as it
+            // found them may do so the next time (a first pass allocates,
+            // tunes, clears); a CUDA error during capture ends the graph path.
             cudaGetLastError();
             b->exec = nullptr;
             if (!cuda_ok || ++b->graph_attempts >= 3)
                 b->graph_failed = true;
-            for (genpk_ctx *c : b->box)
-                forget_issue_state(c);
+            for (int i = 0; i < nb; i++)
+                saved[(size_t)i].restore(b->box[(size_t)i]);
             std::fill(issued.begin(), issued.end(), false);
         }
     }
