@@ -155,7 +155,12 @@ struct genpk_ctx {
     float *stage_mass = nullptr;
     int64_t stage_cap = 0;
     int64_t stage_n = 0;
-    int64_t stage_limit = (int64_t)1 << 28;
+    // Staged host particles merge into one pass up to this count (16 bytes each
+    // on the device: 17 GB at 2^30, one pass for a whole 1024^3 snapshot; four
+    // passes of 2^28 cost four accumulator clears and conversions and lost the
+    // kz-major transform).  Where the device cannot hold that much, the staged
+    // pass is deposited early instead (ensure_stage).
+    int64_t stage_limit = (int64_t)1 << 30;
     Pending pend;
 
     // binning
@@ -813,18 +818,37 @@ int flush_staged(genpk_ctx *ctx)
                        p.mass, n);
 }
 
+// Room in the staging area for `need` particles (the staged ones included).
+// The area grows by doubling up to stage_limit; where the device has no room
+// for that, it grows to `need` exactly, and where it has no room for that
+// either, the staged pass is deposited first and the area sized for the new
+// chunk alone.
 int ensure_stage(genpk_ctx *ctx, int64_t need)
 {
     if (ctx->stage_cap >= need)
         return GENPK_OK;
-    int64_t cap = std::max<int64_t>(need, std::min<int64_t>(ctx->stage_limit, 2 * ctx->stage_cap));
+    int64_t want = std::max<int64_t>(need, std::min<int64_t>(ctx->stage_limit, 2 * ctx->stage_cap));
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     float *np = nullptr, *nm = nullptr;
-    GENPK_CUDA(cudaMalloc(&np, sizeof(float) * 3 * (size_t)cap));
-    if (cudaMalloc(&nm, sizeof(float) * (size_t)cap) != cudaSuccess) {
+    for (;;) {
+        if (cudaMalloc(&np, sizeof(float) * 3 * (size_t)want) == cudaSuccess &&
+            cudaMalloc(&nm, sizeof(float) * (size_t)want) == cudaSuccess)
+            break;
         cudaGetLastError();
         cudaFree(np);
-        return fail(ctx, GENPK_ERR_NOMEM, "staging allocation failed");
+        np = nullptr;
+        if (want > need) {
+            want = need;
+        } else if (ctx->stage_n > 0) {
+            need -= ctx->stage_n;
+            GENPK_TRY(flush_staged(ctx));
+            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (ctx->stage_cap >= need)
+                return GENPK_OK;
+            want = need;
+        } else {
+            return fail(ctx, GENPK_ERR_NOMEM, "staging allocation failed");
+        }
     }
     if (ctx->stage_n > 0) {
         GENPK_CUDA(cudaMemcpyAsync(np, ctx->stage_pos, sizeof(float) * 3 * ctx->stage_n,
@@ -837,7 +861,7 @@ int ensure_stage(genpk_ctx *ctx, int64_t need)
     cudaFree(ctx->stage_mass);
     ctx->stage_pos = np;
     ctx->stage_mass = nm;
-    ctx->stage_cap = cap;
+    ctx->stage_cap = want;
     return GENPK_OK;
 }
 
@@ -1176,6 +1200,9 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
     }
     const int nrb = ctx->nrbins;
     GENPK_TRY(grow(ctx, &ctx->d_power, &ctx->power_cap, (size_t)np * nrb));
+    // Staged host chunks become their pass first, so that the choice of
+    // transform below sees the field as the density it is.
+    GENPK_TRY(flush_staged(ctx));
     // A single auto spectrum of a field still to be transformed: bin it inside
     // the x-axis FFT pass.
     FusedAuto fa;

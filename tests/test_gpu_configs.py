@@ -298,6 +298,17 @@ def test_kz_major_transform_1024(gp):
             ctx.deposit(1, box, other, None, 1.0)
             cross, _, _ = ctx.power(0, 1, m, m)
             auto_after, _, _ = ctx.power(0, 0, m, m)
+            if mode == gp.api.FFT_AUTO:
+                # the same particles from host memory in two chunks: staged,
+                # deposited as one pass, and transformed kz-major as well
+                hp = pos.cpu().numpy()
+                ctx.zero(0)
+                ctx.deposit(0, box, hp[: n // 2], None, 1.0)
+                ctx.deposit(0, box, hp[n // 2:], None, 1.0)
+                ctx.timing_reset()
+                p_host, _, _ = ctx.power(0, 0, m, m)
+                assert "zfft_kz" in ctx.stage_times()
+                assert np.array_equal(p_host, p)
             res[mode] = (p, c, again, cross, auto_after, gpos, st, sta)
     pk, ck, again, cross, auto_after, gk, st, sta = res[gp.api.FFT_AUTO]
     p3, c3, _, _, _, g3, st3, _ = res[gp.api.FFT_CUFFT3D]
