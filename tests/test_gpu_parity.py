@@ -173,7 +173,7 @@ def test_small_and_odd_grids(gp, dims):
         grid_close(ctx.read_field(0), ref_grid)
         p, c, k = ctx.power(0, 0, m, m)
     assert np.array_equal(c, cr)
-    bins_close(p, pr, c, rtol=2e-5)
+    bins_close(p, pr, c)  # 1e-5; the largest seen is 2.8e-7
 
 
 def test_deposit_is_bit_reproducible_across_tiles_and_pointer_kinds(gp):
