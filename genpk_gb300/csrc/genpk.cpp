@@ -166,16 +166,17 @@ struct genpk_ctx {
     // binning
     double *d_partial = nullptr;
     size_t partial_cap = 0;
-    double *d_power = nullptr;
-    size_t power_cap = 0;
+    // The results: mapped pinned host memory that the finalize kernel writes in
+    // place (the spectra, then a copy of the status words), so no copy back
+    // follows the binning.  res_dev is its device address.
+    double *res_host = nullptr;
+    double *res_dev = nullptr;
+    size_t res_cap = 0;  // doubles
     std::vector<std::vector<double>> auto_power;  // cached auto spectrum per field
     std::vector<double> auto_mass;
     std::vector<bool> auto_valid;
 
-    // results of a power request issued without waiting (genpk_batch_power):
-    // copied to pinned host memory on the stream, read when the batch collects
-    double *h_power = nullptr;
-    size_t h_power_cap = 0;
+    // a power request issued without waiting (genpk_batch_power, genpk_power_step)
     struct Deferred {
         bool active = false;
         int np = 0;
@@ -307,6 +308,21 @@ int grow(genpk_ctx *ctx, T **ptr, size_t *cap, size_t need)
     }
     GENPK_CUDA(cudaMalloc((void **)ptr, sizeof(T) * need));
     *cap = need;
+    return GENPK_OK;
+}
+
+// Room for `need` doubles of results in mapped pinned host memory.
+int grow_res(genpk_ctx *ctx, size_t need)
+{
+    if (ctx->res_cap >= need)
+        return GENPK_OK;
+    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->res_host);
+    ctx->res_host = ctx->res_dev = nullptr;
+    ctx->res_cap = 0;
+    GENPK_CUDA(cudaHostAlloc((void **)&ctx->res_host, sizeof(double) * need, cudaHostAllocMapped));
+    GENPK_CUDA(cudaHostGetDevicePointer((void **)&ctx->res_dev, ctx->res_host, 0));
+    ctx->res_cap = need;
     return GENPK_OK;
 }
 
@@ -1186,8 +1202,10 @@ int finish_power(genpk_ctx *ctx, int np, const int *pairs, const double *pair_ma
     return host_status ? report_status(ctx, *host_status) : collect_status(ctx);
 }
 
-// deferred: issue everything, the results' copy to the context's pinned
-// buffer included, and return without waiting; power_collect finishes it.
+int power_collect(genpk_ctx *ctx, double *power, int *count, double *keffs);
+
+// deferred: issue everything and return without waiting; power_collect
+// finishes it (the results land in the context's mapped host buffer).
 int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass,
                double *power, int *count, double *keffs, bool deferred = false)
 {
@@ -1199,7 +1217,8 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         fields.push_back(pairs[q]);
     }
     const int nrb = ctx->nrbins;
-    GENPK_TRY(grow(ctx, &ctx->d_power, &ctx->power_cap, (size_t)np * nrb));
+    GENPK_TRY(grow_res(ctx, (size_t)np * nrb + kStatusDoubles));
+    DeviceStatus *st_out = reinterpret_cast<DeviceStatus *>(ctx->res_dev + (size_t)np * nrb);
     // Staged host chunks become their pass first, so that the choice of
     // transform below sees the field as the density it is.
     GENPK_TRY(flush_staged(ctx));
@@ -1260,7 +1279,8 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         const int ctas =
             fa.kz_ctas > 0 ? fa.kz_ctas : xfft_bin_ctas(ctx->dims, 1, ctx->num_sms);
         GENPK_CUDA(finalize_power(ctx->d_partial, ctas, nrb, ctx->bdev.count, pair_mass[0],
-                                  pair_mass[1], ctx->d_power, ctx->stream, &ctx->launches));
+                                  pair_mass[1], ctx->res_dev, ctx->stream, &ctx->launches,
+                                  ctx->d_status, st_out));
     }
     // Pairs are binned in groups whose fields fit one kernel instantiation.
     int q0 = fa.done ? np : 0;
@@ -1308,42 +1328,20 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
             return fail(ctx, GENPK_ERR_UNSUPPORTED, "nrbins too large for the binning kernel");
         GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap,
                        (size_t)ctas * bin_pair_slots(l.nfields, l.npairs) * nrb));
+        const bool last = q >= np;  // the last finalize also copies the status words
         GENPK_CUDA(bin_spectra(ctx->gg, ctx->tables, ctx->bdev, l, ctx->d_partial,
-                               ctx->d_power + (size_t)q0 * nrb, ctas, warps, smem, ctx->stream,
-                               &ctx->launches));
+                               ctx->res_dev + (size_t)q0 * nrb, ctas, warps, smem, ctx->stream,
+                               &ctx->launches, ctx->d_status, last ? st_out : nullptr));
         q0 = q;
     }
     stage_event(ctx, "bin");
-    double *dst = power;
-    if (deferred) {
-        // the spectra, then a copy of the status words
-        const size_t need = (size_t)np * nrb + kStatusDoubles;
-        if (ctx->h_power_cap < need) {
-            GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-            cudaFreeHost(ctx->h_power);
-            ctx->h_power = nullptr;
-            ctx->h_power_cap = 0;
-            GENPK_CUDA(cudaHostAlloc((void **)&ctx->h_power, sizeof(double) * need,
-                                     cudaHostAllocDefault));
-            ctx->h_power_cap = need;
-        }
-        dst = ctx->h_power;
-    }
-    GENPK_CUDA(cudaMemcpyAsync(dst, ctx->d_power, sizeof(double) * np * nrb,
-                               cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->deferred.active = true;
+    ctx->deferred.np = np;
+    ctx->deferred.pairs.assign(pairs, pairs + 2 * np);
+    ctx->deferred.mass.assign(pair_mass, pair_mass + 2 * np);
     if (deferred)
-        GENPK_CUDA(cudaMemcpyAsync(dst + (size_t)np * nrb, ctx->d_status, sizeof(DeviceStatus),
-                                   cudaMemcpyDeviceToHost, ctx->stream));
-    stage_event(ctx, "d2h");
-    if (deferred) {
-        ctx->deferred.active = true;
-        ctx->deferred.np = np;
-        ctx->deferred.pairs.assign(pairs, pairs + 2 * np);
-        ctx->deferred.mass.assign(pair_mass, pair_mass + 2 * np);
         return GENPK_OK;
-    }
-    GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
-    return finish_power(ctx, np, pairs, pair_mass, power, count, keffs);
+    return power_collect(ctx, power, count, keffs);
 }
 
 // Wait for a deferred power request and hand its results over.
@@ -1355,9 +1353,9 @@ int power_collect(genpk_ctx *ctx, double *power, int *count, double *keffs)
     GENPK_CUDA(cudaStreamSynchronize(ctx->stream));
     const genpk_ctx::Deferred &d = ctx->deferred;
     const size_t nv = (size_t)d.np * ctx->nrbins;
-    memcpy(power, ctx->h_power, sizeof(double) * nv);
+    memcpy(power, ctx->res_host, sizeof(double) * nv);
     DeviceStatus st;
-    memcpy(&st, ctx->h_power + nv, sizeof st);
+    memcpy(&st, ctx->res_host + nv, sizeof st);
     return finish_power(ctx, d.np, d.pairs.data(), d.mass.data(), power, count, keffs, &st);
 }
 
@@ -1406,8 +1404,7 @@ uint64_t issue_digest(const genpk_ctx *ctx)
                           (const void *)ctx->dscr.halo, (const void *)ctx->dscr.mass_part,
                           (const void *)ctx->dscr.win_acc, (const void *)ctx->d_probe,
                           (const void *)ctx->stage_pos, (const void *)ctx->stage_mass,
-                          (const void *)ctx->d_partial, (const void *)ctx->d_power,
-                          (const void *)ctx->h_power})
+                          (const void *)ctx->d_partial, (const void *)ctx->res_dev})
         ptr(q);
     return h;
 }
@@ -1516,11 +1513,11 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
     cudaFree(ctx->stage_pos);
     cudaFree(ctx->stage_mass);
     cudaFree(ctx->d_partial);
-    cudaFree(ctx->d_power);
+
     cudaFree(ctx->d_gcoef);
     cudaFree(ctx->adj_buf);
     cudaFree(ctx->d_probe);
-    cudaFreeHost(ctx->h_power);
+    cudaFreeHost(ctx->res_host);
     for (auto &e : ctx->ev)
         if (e)
             cudaEventDestroy(e);

@@ -303,11 +303,14 @@ int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms
              size_t *smem);
 
 // Runs the binning kernel and the finalize kernel; writes out_power[np][nrbins]
-// on the device.  partial must hold ctas*npairs*nrbins doubles.
+// (device memory, or mapped host memory the kernel writes in place).
+// partial must hold ctas*npairs*nrbins doubles.
 // power[b] = sum over the CTA partials / (ma * mb * count[b]) (count 0: 0).
+// With st_out, the finalize kernel also copies the status words *st_in there.
 cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const double *count,
                            double ma, double mb, double *out, cudaStream_t stream,
-                           int64_t *launches);
+                           int64_t *launches, const DeviceStatus *st_in = nullptr,
+                           DeviceStatus *st_out = nullptr);
 // Binning of one kz-major spectrum S[kz][x][y] (after zfft_kz_pass and the
 // batched 2-D C2C): the auto pair's partial sums, one FP64 histogram per CTA
 // (partial: ctas * nrbins doubles), for finalize_power.  When `zero` is not
@@ -321,7 +324,8 @@ cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevi
                             cudaStream_t stream, int64_t *launches);
 cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
                         const BinLaunch &l, double *partial, double *out_power, int ctas,
-                        int warps, size_t smem, cudaStream_t stream, int64_t *launches);
+                        int warps, size_t smem, cudaStream_t stream, int64_t *launches,
+                        const DeviceStatus *st_in = nullptr, DeviceStatus *st_out = nullptr);
 
 // ---------------------------------------------------------------------------
 // Adjoint

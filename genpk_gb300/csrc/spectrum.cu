@@ -515,8 +515,11 @@ constexpr int kFinalizeThreads = 256;
 
 __global__ void __launch_bounds__(kFinalizeThreads)
     k_bin_finalize(const double *__restrict__ partial, int ctas, int nrbins,
-                   const double *__restrict__ count, NormParams mn, double *__restrict__ power)
+                   const double *__restrict__ count, NormParams mn, double *__restrict__ power,
+                   const DeviceStatus *__restrict__ st_in, DeviceStatus *__restrict__ st_out)
 {
+    if (st_out && blockIdx.x == 0 && threadIdx.x == 0)
+        *st_out = *st_in;  // the pass's status words, beside the results
     __shared__ double sh[kFinalizeThreads];
     const int k = blockIdx.x;
     const int s = k / nrbins, b = k - s * nrbins;
@@ -602,7 +605,8 @@ int bin_ctas(const GridGeom &g, int nrbins, int npairs, int nfields, int num_sms
 
 cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &d,
                         const BinLaunch &l, double *partial, double *out_power, int ctas,
-                        int warps, size_t smem, cudaStream_t stream, int64_t *launches)
+                        int warps, size_t smem, cudaStream_t stream, int64_t *launches,
+                        const DeviceStatus *st_in, DeviceStatus *st_out)
 {
     const Shape s = pick_shape(l.nfields, l.npairs);
     BinParams p;
@@ -652,7 +656,7 @@ cudaError_t bin_spectra(const GridGeom &g, const BinTables &t, const BinDevice &
     }
     const int k = l.npairs * t.nrbins;
     k_bin_finalize<<<k, kFinalizeThreads, 0, stream>>>(partial, ctas, t.nrbins, d.count, mn,
-                                                        out_power);
+                                                        out_power, st_in, st_out);
     (*launches)++;
     return cudaGetLastError();
 }
@@ -702,7 +706,7 @@ cudaError_t bin_spectrum_kz(const GridGeom &g, const BinTables &t, const BinDevi
 
 cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const double *count,
                            double ma, double mb, double *out, cudaStream_t stream,
-                           int64_t *launches)
+                           int64_t *launches, const DeviceStatus *st_in, DeviceStatus *st_out)
 {
     NormParams mn;
     mn.npc = 1;
@@ -712,7 +716,7 @@ cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const do
         mn.src[q] = 0;
     }
     k_bin_finalize<<<nrbins, kFinalizeThreads, 0, stream>>>(partial, ctas, nrbins, count, mn,
-                                                            out);
+                                                            out, st_in, st_out);
     (*launches)++;
     return cudaGetLastError();
 }
