@@ -367,6 +367,7 @@ __global__ void __launch_bounds__(kScanThreads)
         // once per 2^4 adds) and 64-bit cell sums hold 2^35 full-mass particles.
         const float mref = uniform_mass >= 0.0 ? (float)fabs(uniform_mass)
                                                : __uint_as_float(st->max_mass_bits);
+        st->max_mass_bits = 0u;  // read: zero again for the next pass
         int s = 0;
         if (mref > 0.f && isfinite(mref))
             s = 27 - ilogbf(mref);
@@ -802,10 +803,12 @@ __global__ void __launch_bounds__(256)
 
 // The corner mode k = (N/2, N/2, N/2) of an even grid is sum (-1)^(x+y+z) rho(x):
 // this pass's exact share, in mass units, joins the grid's running value.  (The
-// subtracted mean contributes nothing: the signs balance on an even grid.)
-__global__ void k_pass_finish(const DeviceStatus *__restrict__ st, double *field_corner)
+// subtracted mean contributes nothing: the signs balance on an even grid.)  The
+// sum is zeroed for the next pass here, so no pass has to clear it first.
+__global__ void k_pass_finish(DeviceStatus *__restrict__ st, double *field_corner)
 {
     *field_corner += ldexp((double)st->alt_sum, -(st->fx_shift + 4));
+    st->alt_sum = 0;
 }
 
 int ilog2(int v)
@@ -949,11 +952,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     const bool shared_hist = deposit_shared_hist(g);
     const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
     cudaError_t err;
-    if ((err = cudaMemsetAsync(&dstat->max_mass_bits, 0, sizeof(unsigned), stream)) !=
-        cudaSuccess)
-        return err;
-    if ((err = cudaMemsetAsync(&dstat->alt_sum, 0, sizeof(long long), stream)) != cudaSuccess)
-        return err;
+    // (max_mass_bits and alt_sum are zero here: the pass that used them last
+    // zeroed them, in k_sort_scan / k_window_prep and the finishing kernels)
     const int cgrid = (g.ntiles + 31) / 32;
     const size_t hsmem = deposit_hist_smem(g);
     if (shared_hist) {

@@ -77,7 +77,55 @@ struct WinParams {
     // clocks; -1 for none.
     int64_t skip_chunk;
     long long skip_wait;
+    // A uniform mass's pass constants, computed on the host (host_prep = 1) as
+    // k_window_prep computes them; thread 0 of CTA 0 stores them in the status
+    // words and adds the pass to the grid's running sums.  Else (host_prep = 0)
+    // k_window_prep ran before the pass.
+    int host_prep;
+    int fx_shift;
+    double pass_mass;
+    long long mean_fixed;
+    double *field_mass, *field_sub;
 };
+
+// The pass constants of k_window_prep, on the host for a uniform mass (the
+// same IEEE operations in the same order: the same bits).
+struct PassConsts {
+    double mass;
+    int fx_shift;
+    long long mean_fixed;
+};
+
+__host__ __device__ inline PassConsts pass_consts(double m, float mref, double inv_cells)
+{
+    int s = 0;
+    if (mref > 0.f && isfinite(mref))
+        s = 27 - ilogbf(mref);
+    s = max(-100, min(100, s));
+    const double mf = m * inv_cells * ldexp(1.0, s);
+    long long mean_fixed;
+    const double amf = fabs(mf);
+    if (amf >= 16777216.0) {
+        const double q = ldexp(1.0, ilogb(amf) - 23);
+        mean_fixed = (long long)(rint(mf / q) * q);
+    } else {
+        mean_fixed = llrint(mf);
+    }
+    return {m, s, mean_fixed};
+}
+
+// Thread 0 of CTA 0: the host-computed constants into the status words and
+// the grid's running sums (a uniform-mass pass without k_window_prep).
+__device__ __forceinline__ void store_host_prep(const WinParams &p, DeviceStatus *st)
+{
+    if (p.host_prep && blockIdx.x == 0 && threadIdx.x == 0) {
+        st->pass_mass = p.pass_mass;
+        st->fx_shift = p.fx_shift;
+        st->mean_fixed = p.mean_fixed;
+        *p.field_mass += p.pass_mass;
+        *p.field_sub += ldexp((double)p.mean_fixed, -p.fx_shift);
+    }
+}
 
 // Clocks a bounded wait spins before it gives up: about a second.
 constexpr long long kWaitClocks = 1ll << 31;
@@ -416,12 +464,14 @@ __global__ void __launch_bounds__(kWinThreads, 1)
 
     // Weights in 2^-s mass units, s = 154 - emax (common.cuh pair_w / z_mass /
     // corner_w, as the sorted engine computes them).
-    const int emax = 154 - st->fx_shift;
+    store_host_prep(p, st);
+    const int fxs = p.host_prep ? p.fx_shift : st->fx_shift;
+    const int emax = 154 - fxs;
     const unsigned ubits = __float_as_uint(p.umass);
     const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
     const int uef = (int)((ubits >> 23) & 0xffu);
     const bool uneg = (ubits >> 31) != 0u;
-    const float mscale = ldexpf(1.f, st->fx_shift + 4);
+    const float mscale = ldexpf(1.f, fxs + 4);
 
     f2sum alt = {0.f, 0.f};
     unsigned bad = 0, timeouts = 0;
@@ -619,12 +669,14 @@ __global__ void __launch_bounds__(kWinThreads, 1)
     }
     __syncthreads();
 
-    const int emax = 154 - st->fx_shift;
+    store_host_prep(p, st);
+    const int fxs = p.host_prep ? p.fx_shift : st->fx_shift;
+    const int emax = 154 - fxs;
     const unsigned ubits = __float_as_uint(p.umass);
     const unsigned umant = (ubits & 0x7fffffu) | 0x800000u;
     const int uef = (int)((ubits >> 23) & 0xffu);
     const bool uneg = (ubits >> 31) != 0u;
-    const float mscale = ldexpf(1.f, st->fx_shift + 4);
+    const float mscale = ldexpf(1.f, fxs + 4);
 
     f2sum alt = {0.f, 0.f};
     unsigned bad = 0, timeouts = 0;
@@ -847,25 +899,14 @@ __global__ void k_window_prep(const double *__restrict__ mass_part, int nparts, 
         for (int c = 0; c < nparts; c++)
             m += mass_part[c];
         mref = __uint_as_float(st->max_mass_bits);
+        st->max_mass_bits = 0u;  // read: zero again for the next pass
     }
-    int s = 0;
-    if (mref > 0.f && isfinite(mref))
-        s = 27 - ilogbf(mref);
-    s = max(-100, min(100, s));
-    const double mf = m * inv_cells * ldexp(1.0, s);
-    long long mean_fixed;
-    const double amf = fabs(mf);
-    if (amf >= 16777216.0) {
-        const double q = ldexp(1.0, ilogb(amf) - 23);
-        mean_fixed = (long long)(rint(mf / q) * q);
-    } else {
-        mean_fixed = llrint(mf);
-    }
-    st->pass_mass = m;
-    st->fx_shift = s;
-    st->mean_fixed = mean_fixed;
-    *field_mass += m;
-    *field_sub += ldexp((double)mean_fixed, -s);
+    const PassConsts k = pass_consts(m, mref, inv_cells);
+    st->pass_mass = k.mass;
+    st->fx_shift = k.fx_shift;
+    st->mean_fixed = k.mean_fixed;
+    *field_mass += k.mass;
+    *field_sub += ldexp((double)k.mean_fixed, -k.fx_shift);
 }
 
 // Accumulator minus the mean, rounded once to FP32 and stored (clean grid) or
@@ -917,9 +958,10 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void k_window_finish(const DeviceStatus *__restrict__ st, double *field_corner)
+__global__ void k_window_finish(DeviceStatus *__restrict__ st, double *field_corner)
 {
     *field_corner += ldexp((double)st->alt_sum, -(st->fx_shift + 4));
+    st->alt_sum = 0;  // zero for the next pass
 }
 
 // Probe: for up to `samples` evenly spread chunks, the window volume in cells
@@ -1020,6 +1062,11 @@ WinParams make_win_params(const DepositGeom &g, const DepositArgs &a, int chunk)
                  : 0;
     p.skip_chunk = a.skip_chunk;
     p.skip_wait = a.skip_wait;
+    p.host_prep = 0;
+    p.fx_shift = 0;
+    p.pass_mass = 0.0;
+    p.mean_fixed = 0;
+    p.field_mass = p.field_sub = nullptr;
     return p;
 }
 
@@ -1078,25 +1125,36 @@ cudaError_t deposit_window_pass(const DepositGeom &g, const DepositArgs &a, int 
             hook(hook_user, name);
     };
     cudaError_t err;
-    if ((err = cudaMemsetAsync(&dstat->max_mass_bits, 0, sizeof(unsigned), stream)) != cudaSuccess)
-        return err;
-    if ((err = cudaMemsetAsync(&dstat->alt_sum, 0, sizeof(long long), stream)) != cudaSuccess)
-        return err;
+    // (max_mass_bits and alt_sum are zero here: the pass that used them last
+    // zeroed them, in k_window_prep / k_sort_scan and the finishing kernels)
     const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
+    WinParams p = make_win_params(g, a, chunk);
     if (a.masses) {
         k_mass_reduce<<<mass_ctas, 256, 0, stream>>>(a.masses, a.n, mass_part, dstat);
         mark("win_mass");
     }
-    k_window_prep<<<1, 1, 0, stream>>>(mass_part, a.masses ? mass_ctas : 0, (double)a.mass, a.n,
-                                       1.0 / n3, a.field_mass, a.field_sub, dstat);
-    mark("win_prep");
+    if (a.masses || p.nchunks == 0) {
+        k_window_prep<<<1, 1, 0, stream>>>(mass_part, a.masses ? mass_ctas : 0, (double)a.mass,
+                                           a.n, 1.0 / n3, a.field_mass, a.field_sub, dstat);
+        mark("win_prep");
+    } else {
+        // a uniform mass: the constants need nothing from the device, and the
+        // deposit kernel stores them (one launch fewer per pass)
+        const double umass = (double)a.mass;
+        const PassConsts k = pass_consts((double)a.n * umass, (float)fabs(umass), 1.0 / n3);
+        p.host_prep = 1;
+        p.fx_shift = k.fx_shift;
+        p.pass_mass = k.mass;
+        p.mean_fixed = k.mean_fixed;
+        p.field_mass = a.field_mass;
+        p.field_sub = a.field_sub;
+    }
     if (clear_bytes) {
         clear_bytes = std::min(clear_bytes, sizeof(acc_t) * (size_t)g.grid.nfloat);
         if ((err = cudaMemsetAsync(acc, 0, clear_bytes, stream)) != cudaSuccess)
             return err;
         mark("win_clear");
     }
-    const WinParams p = make_win_params(g, a, chunk);
     if (p.nchunks > 0) {
         const unsigned ctas = (unsigned)std::min<int64_t>(p.nchunks, num_sms);
         // stream mode: the two chunk buffers only
