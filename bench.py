@@ -505,6 +505,8 @@ def boxes(args):
     line["deposit_tuning"] = [tuning_record(b.deposit_config(i), b.deposit_trials(i),
                                             line["engines"][i]) for i in range(len(batch))]
     line["graph_replays"] = b.graph_replays
+    # the host's launches per timed call: one graph launch once the call is replayed
+    line["host_launches_per_step"] = 1 if b.graph_replays >= args.steps else launches
     b.use_graph(False)  # the same batch issued kernel by kernel, for comparison
     for _ in range(2):
         step(pos)
