@@ -77,6 +77,10 @@ def parse():
                          "512^3 grid, 3 auto + 3 cross spectra per step; boxes: 16 boxes of "
                          "uniform particles, counts log-uniform in [1e5, 3e7], grids 128^3 or "
                          "256^3, one auto spectrum each per step")
+    ap.add_argument("--order", choices=["lattice", "morton", "random"], default="lattice",
+                    help="particle order of the Zel'dovich workload: lattice (x slowest), "
+                         "morton (a space-filling curve, as snapshots are often written) or "
+                         "random (shuffled)")
     ap.add_argument("--profile-timed", action="store_true",
                     help="open the CUDA profiler range (cudaProfilerStart/Stop) around the timed "
                          "steps only, for `ncu --profile-from-start off`: set-up, tuning and "
@@ -261,13 +265,40 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def morton_order(nside, device):
+    """Permutation of an nside^3 lattice (x slowest) into Morton (Z-curve) order
+    of the lattice cells: blocks of 2^k cells stay together, as in snapshots
+    written in a space-filling-curve order."""
+    import torch
+    i = torch.arange(nside ** 3, device=device, dtype=torch.int64)
+    x, y, z = i // (nside * nside), (i // nside) % nside, i % nside
+    code = torch.zeros_like(i)
+    for b in range(max(1, (nside - 1).bit_length())):
+        code |= ((x >> b) & 1) << (3 * b + 2)
+        code |= ((y >> b) & 1) << (3 * b + 1)
+        code |= ((z >> b) & 1) << (3 * b)
+    return torch.argsort(code)
+
+
 def positions(args, seed, device="cpu"):
-    """nside^3 particles: a Zel'dovich lattice (lattice order), or i.i.d.
-    uniform positions in [0, box) (the 128^3 Gadget-snapshot configuration)."""
+    """nside^3 particles: a Zel'dovich lattice (lattice order, or reordered by
+    --order), or i.i.d. uniform positions in [0, box) (the 128^3
+    Gadget-snapshot configuration)."""
     from genpk_gb300 import synth
     if args.workload == "uniform":
         return synth.uniform(args.nside ** 3, args.box, seed=seed, device=device)
-    return synth.zeldovich(args.nside, args.box, seed=seed, device=device)
+    pos = synth.zeldovich(args.nside, args.box, seed=seed, device=device)
+    if args.order == "lattice":
+        return pos
+    import torch
+    t = pos if isinstance(pos, torch.Tensor) else torch.from_numpy(pos)
+    if args.order == "morton":
+        perm = morton_order(args.nside, t.device)
+    else:
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        perm = torch.randperm(args.nside ** 3, generator=g).to(t.device)
+    out = t[perm].contiguous()
+    return out if isinstance(pos, torch.Tensor) else out.numpy()
 
 
 def particle_mass(args):
@@ -293,7 +324,8 @@ def needs_l2_flush(npart):
 
 def config_dict(args, npart):
     kind = ("uniform random particles (mass 1e-2)" if args.workload == "uniform"
-            else "Zel'dovich lattice particles")
+            else "Zel'dovich lattice particles" + ("" if args.order == "lattice"
+                                                   else f" in {args.order} order"))
     l2 = (f"L2 flushed between steps (a {2 * l2_bytes() / 1e6:.0f} MB buffer written outside "
           f"the stage events; {npart * 12 / 1e9:.3f} GB of positions per step)"
           if needs_l2_flush(npart)
