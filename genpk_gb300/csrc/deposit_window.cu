@@ -546,9 +546,26 @@ __global__ void __launch_bounds__(kWinThreads, 1)
             if (ef == 0)  // zero or subnormal mass deposits nothing
                 continue;
             const int dsh = max(emax - ef, 0);
-            const AxisQ ax = split_q28(x, p.uh, p.ul, p.dims);
-            const AxisQ ay = split_q28(y, p.uh, p.ul, p.dims);
-            const AxisQ az = split_q28(z, p.uh, p.ul, p.dims);
+            // The stream kernel's fast split where 1 <= |x N/L| < 2^22 cells on
+            // every axis (the same cells and fractions as split_q28).
+            const float xh = __fmul_rn(x, p.uh), yh = __fmul_rn(y, p.uh), zh = __fmul_rn(z, p.uh);
+            AxisQ ax, ay, az;
+            if (fabsf(xh) >= 1.f && fabsf(xh) < kFastSplitMax && fabsf(yh) >= 1.f &&
+                fabsf(yh) < kFastSplitMax && fabsf(zh) >= 1.f && fabsf(zh) < kFastSplitMax) {
+                ax = split_q28_unwrapped(x, xh, p.uh, p.ul);
+                ay = split_q28_unwrapped(y, yh, p.uh, p.ul);
+                az = split_q28_unwrapped(z, zh, p.uh, p.ul);
+                if (max((unsigned)ax.cell, max((unsigned)ay.cell, (unsigned)az.cell)) >=
+                    (unsigned)p.dims) {
+                    ax.cell = wrap_cell(ax.cell, p.dims);
+                    ay.cell = wrap_cell(ay.cell, p.dims);
+                    az.cell = wrap_cell(az.cell, p.dims);
+                }
+            } else {
+                ax = split_q28(x, p.uh, p.ul, p.dims);
+                ay = split_q28(y, p.uh, p.ul, p.dims);
+                az = split_q28(z, p.uh, p.ul, p.dims);
+            }
             if (CORNER) {
                 f2sum v = corner_factor_q(ax, ay, az);
                 if (VARMASS) {
