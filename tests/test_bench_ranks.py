@@ -97,3 +97,26 @@ def test_box_batch_is_seeded_and_in_range():
     b, _ = bench.box_batch()
     assert a == b and len(a) == 16 and box == 25000.0
     assert all(1e5 <= c <= 3e7 and g in (128, 256) for c, g, _ in a)
+
+
+def test_particle_orders_are_permutations_of_the_lattice():
+    """--order morton and --order random reorder the same particles: a Morton
+    code sorts (x, y, z) with the bits interleaved, and both orders hold every
+    lattice particle once (the deposit does not depend on the order)."""
+    import argparse
+    import numpy as np
+    import torch
+    sys.path.insert(0, ROOT)
+    import bench
+    perm = bench.morton_order(8, "cpu").numpy()
+    assert np.array_equal(np.sort(perm), np.arange(8 ** 3))
+    x, y, z = perm // 64, (perm // 8) % 8, perm % 8
+    assert list(zip(x[:8], y[:8], z[:8])) == [(0, 0, 0), (0, 0, 1), (0, 1, 0), (0, 1, 1),
+                                              (1, 0, 0), (1, 0, 1), (1, 1, 0), (1, 1, 1)]
+    base = dict(workload="zeldovich", nside=16, box=1000.0)
+    lattice = bench.positions(argparse.Namespace(order="lattice", **base), seed=3)
+    for order in ("morton", "random"):
+        other = bench.positions(argparse.Namespace(order=order, **base), seed=3)
+        assert other.shape == lattice.shape and not np.array_equal(other, lattice)
+        key = lambda a: a[np.lexsort(a.T[::-1])]
+        assert np.array_equal(key(other), key(lattice))
