@@ -917,3 +917,38 @@ def test_state_and_argument_errors(gp):
         assert not p.any()
         with pytest.raises(gp.GenPKError):
             ctx.set_tile(7, 7, 7)
+
+
+def test_empty_inputs(gp):
+    """Empty particle arrays (host and device): a grid that receives none has
+    a zero spectrum with the full mode counts; a batch with an empty box gives
+    zeros for it and the other box's spectrum unchanged, through the eager,
+    captured and replayed calls; a species step with an empty species gives
+    zero auto and cross spectra for it."""
+    import torch
+    from genpk_gb300 import synth
+    box, nrbins, n = 1000.0, 16, 100_000
+    empty_h = np.zeros((0, 3), np.float32)
+    empty_d = torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+    hp = synth.uniform(n, box, seed=5)
+    full = torch.from_numpy(hp).cuda()
+    m = O.total_mass(n, None, 1.0)
+    pr, cr, _ = O.pk(hp, box, 32, nrbins, None, 1.0, m_norm=m)
+    with gp.Context(32, nrbins) as ctx:
+        ctx.deposit(0, box, empty_h, None, 1.0)
+        ctx.deposit(0, box, empty_d, None, 1.0)
+        p, c, _ = ctx.power(0, 0, 1.0, 1.0)
+    assert not p.any() and np.array_equal(c, cr)
+    with gp.Context(32, nrbins) as ctx:
+        ctx.deposit(0, box, full, None, 1.0)
+        alone, _, _ = ctx.power(0, 0, m, m)
+    with gp.Batch([32, 32], nrbins) as b:
+        for _ in range(3):  # eager, captured and replayed, replayed
+            pw, cw, _ = b.power(box, [empty_d, full], [1.0, m], mass=1.0)
+            assert not pw[0].any() and np.array_equal(pw[1], alone)
+            assert np.array_equal(cw[0], cr) and np.array_equal(cw[1], cr)
+    with gp.Context(32, nrbins, nfields=2) as ctx:
+        ps, cs, _ = ctx.power_step(box, [full, empty_d], [(0, 0), (1, 1), (0, 1)],
+                                   [(m, m), (1.0, 1.0), (m, 1.0)], mass=[1.0, 1.0])
+    assert not ps[1].any() and not ps[2].any() and np.array_equal(cs, cr)
+    bins_close(ps[0], pr, cr)
