@@ -45,12 +45,13 @@ METRIC = ("particles/s + ms/spectrum at 512^3 grid vs FP64 oracle; "
           "fwd+adjoint/fwd time ratio")
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # dram__bytes_read.sum + dram__bytes_write.sum of one deposit-kernel launch,
-# from ncu captures of the default workload (512^3 Zel'dovich particles onto a
-# 512^3 grid, uniform mass), keyed by (kernel, particles per side, grid): the
-# positions (1.61 GB) and the 64-bit accumulator's lines read, the accumulator
-# written.  Reported only for that workload.
+# from ncu captures of Zel'dovich lattices in lattice order (uniform mass),
+# keyed by (kernel, particles per side, grid): the positions and the 64-bit
+# accumulator's lines read, the accumulator written.  Reported only for those
+# workloads.
 NCU_TRAFFIC = {("k_stream_deposit", 512, 512): 2.691e9 + 1.036e9,
-               ("k_window_deposit", 512, 512): 2.692e9 + 1.052e9}
+               ("k_window_deposit", 512, 512): 2.692e9 + 1.052e9,
+               ("k_stream_deposit", 256, 256): 337.3e6 + 92.7e6}
 
 
 def parse():
@@ -650,8 +651,8 @@ def main():
         stage = "win_deposit" if engine == "window" else "stream_deposit"
         t_k = stages.get(stage, 0.0) * 1e-3
         kname = "k_window_deposit" if engine == "window" else "k_stream_deposit"
-        ncu = NCU_TRAFFIC.get((kname, nside, n))
-        traffic = ncu
+        lattice = args.workload == "zeldovich" and args.order == "lattice"
+        traffic = NCU_TRAFFIC.get((kname, nside, n)) if lattice else None
     else:
         t_k = t_pass
         kname = "deposit pass (sorted engine: all its kernels)"
