@@ -22,6 +22,10 @@ from . import native
 GENPK_FLAG_TIMING = 0x1
 ENGINE_AUTO, ENGINE_SORTED, ENGINE_WINDOW, ENGINE_STREAM = 0, 1, 2, 3
 FFT_AUTO, FFT_CUFFT3D = 0, 1
+GENPK_BATCH_PER_BOX, GENPK_BATCH_GROUPED, GENPK_BATCH_AUTO = 0, 1, 2
+_BATCH_MODES = {False: GENPK_BATCH_PER_BOX, "per_box": GENPK_BATCH_PER_BOX,
+                True: GENPK_BATCH_GROUPED, "grouped": GENPK_BATCH_GROUPED,
+                "auto": GENPK_BATCH_AUTO}
 
 
 class GenPKError(RuntimeError):
@@ -391,6 +395,51 @@ class Batch:
     def graph_replays(self) -> int:
         """Calls served by a replay of the captured graph."""
         return int(self.lib.genpk_batch_graph_replays(self.h))
+
+    def set_mode(self, mode):
+        """True or "grouped": boxes of one grid size share each kernel launch of
+        a grouped sorted-engine pass, one batched transform and one binning x
+        pass (GENPK_BATCH_GROUPED); False or "per_box": every box has its own
+        passes; "auto" (the default): the faster of the two, from timed trial
+        calls."""
+        rc = self.lib.genpk_batch_set_mode(self.h, _BATCH_MODES[mode])
+        if rc != 0:
+            raise GenPKError(rc, "genpk_batch_set_mode")
+
+    @property
+    def last_mode(self) -> str:
+        """How the latest call ran: "per_box" or "grouped" (None before a call)."""
+        m = int(self.lib.genpk_batch_last_mode(self.h))
+        return {GENPK_BATCH_PER_BOX: "per_box", GENPK_BATCH_GROUPED: "grouped"}.get(m)
+
+    def auto_times(self) -> dict:
+        """The auto mode's timed trial calls (ms) and its choice (None while the
+        trials run)."""
+        a, g = ctypes.c_double(), ctypes.c_double()
+        c = int(self.lib.genpk_batch_auto_times(self.h, ctypes.byref(a), ctypes.byref(g)))
+        return {"per_box_ms": a.value, "grouped_ms": g.value,
+                "choice": {GENPK_BATCH_PER_BOX: "per_box",
+                           GENPK_BATCH_GROUPED: "grouped"}.get(c)}
+
+    def groups(self) -> list:
+        """The groups of the latest grouped call: for each, its boxes, grid size,
+        tuned tile and sort CTAs, tuning trials and kernel launches."""
+        out = []
+        for g in range(max(int(self.lib.genpk_batch_groups(self.h)), 0)):
+            nb = ctypes.c_int()
+            boxes = (ctypes.c_int * 32)()
+            h = self.lib.genpk_batch_group(self.h, g, ctypes.byref(nb),
+                                           ctypes.cast(boxes, native.c_i32p))
+
+            def chk(rc):
+                if rc != 0:
+                    raise GenPKError(rc, "genpk_deposit_config")
+            out.append({"boxes": [boxes[i] for i in range(nb.value)],
+                        "dims": self.dims[boxes[0]],
+                        "config": _deposit_config(self.lib, h, chk),
+                        "trials": _deposit_trials(self.lib, h),
+                        "launches": int(self.lib.genpk_kernel_launches(h))})
+        return out
 
 
 def _deposit_config(lib, h, chk) -> dict:

@@ -30,6 +30,12 @@
 //                     (up to 7) lower neighbours hold for it, in a fixed order,
 //                     and stores (sum - mean) as FP32.
 //
+// A grouped pass runs the same kernels once for several boxes of one grid size
+// (a batch of uneven boxes): the sort CTAs are shared out over the boxes'
+// particles, the per-tile kernels take the box from blockIdx.y, the scan and
+// the finish one CTA or thread per box.  Record slots are global across the
+// boxes (box b's tile starts are offset by its first record).
+//
 // No global float atomics are involved and no grid memset is needed: every real
 // cell is written exactly once per pass.  Subtracting the pass mean (in fixed
 // point, before the single rounding) keeps the FP32 r2c accurate; it changes
@@ -90,6 +96,44 @@ struct SortParams {
     int ntiles;
     float umass;     // uniform mass when masses == nullptr
     int corner;      // accumulate the exact (N/2,N/2,N/2) mode (even grids)
+};
+
+// Where a sort CTA's particles come from: the one box of a pass, or the boxes
+// of a grouped pass (CTAs [cta0[b], cta0[b+1]) read box b; an empty box has
+// none).  Both are passed by value in the kernel parameters.
+struct OneBox {
+    SortParams p;
+    __device__ __forceinline__ int box_of(int) const { return 0; }
+    __device__ __forceinline__ SortParams params(int) const { return p; }
+    __device__ __forceinline__ int first_cta(int) const { return 0; }
+};
+
+struct BoxGroup {
+    int nbox;
+    int cta0[kMaxGroupBoxes + 1];
+    SortParams p[kMaxGroupBoxes];
+    __device__ __forceinline__ int box_of(int blk) const
+    {
+        int b = 0;
+        while (b + 1 < nbox && blk >= cta0[b + 1])
+            b++;
+        return b;
+    }
+    __device__ __forceinline__ SortParams params(int b) const { return p[b]; }
+    __device__ __forceinline__ int first_cta(int b) const { return cta0[b]; }
+};
+
+// Sort-CTA rows of each box in the histogram (k_sort_colsum, k_sort_offsets:
+// box = blockIdx.y), and what the scan needs per box (box = blockIdx.x):
+// its rows, uniform mass (< 0: the particles carry masses) and first record.
+struct BoxRows {
+    int first[kMaxGroupBoxes + 1];
+};
+
+struct ScanBoxes {
+    int first[kMaxGroupBoxes + 1];
+    double umass[kMaxGroupBoxes];
+    long long rec0[kMaxGroupBoxes];
 };
 
 // Threads of a sort CTA (a CTA's particle range does not depend on them).
@@ -162,13 +206,13 @@ __device__ __forceinline__ bool warp_has_tile_runs(uint32_t t)
     return __any_sync(0xffffffffu, lane > 0 && t != kNoTile && t == prev);
 }
 
-// Each warp walks its CTA's range in blocks of 32*kSortUnroll consecutive
+// Each warp walks its CTA's range (CTA `cta` of its box) in blocks of 32*kSortUnroll consecutive
 // particles (lane l takes base + l + 32u, so every load is coalesced).  The trip
 // count is warp-uniform, so warp-collective intrinsics are safe in `f`.
 template <typename F>
-__device__ __forceinline__ void for_each_warp_batch(const SortParams &p, F &&f)
+__device__ __forceinline__ void for_each_warp_batch(const SortParams &p, int cta, F &&f)
 {
-    const int64_t b = (int64_t)blockIdx.x * p.chunk;
+    const int64_t b = (int64_t)cta * p.chunk;
     const int64_t e = min(p.n, b + p.chunk);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (int64_t base = b + (int64_t)warp * 32 * kSortUnroll; base < e;
@@ -198,22 +242,26 @@ __device__ __forceinline__ void for_each_warp_batch(const SortParams &p, F &&f)
 // straight into global totals (GLOBAL = true, for grids with many tiles).
 // Lanes of a warp that fall in the same tile are merged first
 // (__match_any_sync), so spatially ordered input costs one atomic per warp.
-template <bool GLOBAL>
+template <bool GLOBAL, class Src>
 __global__ void __launch_bounds__(kSortThreads)
-    k_sort_hist(SortParams p, uint32_t *__restrict__ out, double *__restrict__ mass_part,
-                DeviceStatus *st)
+    k_sort_hist(const __grid_constant__ Src src, uint32_t *__restrict__ out,
+                double *__restrict__ mass_part, DeviceStatus *st)
 {
     extern __shared__ uint32_t sh_hist[];
+    const int box = src.box_of(blockIdx.x);
+    const SortParams p = src.params(box);
+    const int cta = blockIdx.x - src.first_cta(box);
+    st += box;
     if (!GLOBAL) {
         for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
             sh_hist[i] = 0u;
         __syncthreads();
     }
-    uint32_t *counts = GLOBAL ? out : sh_hist;
+    uint32_t *counts = GLOBAL ? out + (size_t)box * p.ntiles : sh_hist;
     const int lane = threadIdx.x & 31;
     float msum = 0.f, mc = 0.f, mmax = 0.f;
     unsigned bad = 0;
-    for_each_warp_batch(p, [&](bool in, const float *v, float m) {
+    for_each_warp_batch(p, cta, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
         if (in) {
             AxisQ a[3];
@@ -271,14 +319,18 @@ __device__ __forceinline__ uint32_t column_block_sum(const uint32_t *hist, int n
 }
 
 __global__ void __launch_bounds__(32 * kColWarps)
-    k_sort_colsum(const uint32_t *__restrict__ hist, int nsort, int ntiles,
-                  uint32_t *__restrict__ totals)
+    k_sort_colsum(const uint32_t *__restrict__ hist, const __grid_constant__ BoxRows rows,
+                  int ntiles, uint32_t *__restrict__ totals)
 {
     __shared__ uint32_t part[kColWarps][33];
+    const int box = blockIdx.y;
+    const int nsort = rows.first[box + 1] - rows.first[box];
+    hist += (size_t)rows.first[box] * ntiles;
+    totals += (size_t)box * ntiles;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int t = blockIdx.x * 32 + lane;
-    const int rows = (nsort + kColWarps - 1) / kColWarps;
-    const int r0 = min(w * rows, nsort), r1 = min(r0 + rows, nsort);
+    const int per_warp = (nsort + kColWarps - 1) / kColWarps;
+    const int r0 = min(w * per_warp, nsort), r1 = min(r0 + per_warp, nsort);
     part[w][lane] = column_block_sum(hist, ntiles, t, r0, r1);
     __syncthreads();
     if (w == 0 && t < ntiles) {
@@ -291,19 +343,32 @@ __global__ void __launch_bounds__(32 * kColWarps)
 
 constexpr int kScanThreads = 1024;
 
-// Exclusive scan of tile totals (one CTA) and the per-pass constants.
-// uniform_mass >= 0 means every particle weighs uniform_mass.
+// Exclusive scan of tile totals (one CTA per box) and the per-pass constants.
+// A box's tile starts begin at its first record.  uniform_mass >= 0 means
+// every particle of the box weighs uniform_mass.
 __global__ void __launch_bounds__(kScanThreads)
     k_sort_scan(const uint32_t *__restrict__ totals, int ntiles, uint32_t *__restrict__ tile_start,
-                uint32_t *__restrict__ cursor, const double *__restrict__ mass_part, int nsort,
-                double uniform_mass, double inv_cells, double *field_mass, double *field_sub,
-                DeviceStatus *st)
+                uint32_t *__restrict__ cursor, const double *__restrict__ mass_part,
+                const __grid_constant__ ScanBoxes boxes, double inv_cells, double *field_mass,
+                double *field_sub, DeviceStatus *st)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     __shared__ uint32_t carry;
     __shared__ double sh_m[kScanThreads / 32];
+    const int box = blockIdx.x;
+    const int nsort = boxes.first[box + 1] - boxes.first[box];
+    const double uniform_mass = boxes.umass[box];
+    const uint32_t rec0 = (uint32_t)boxes.rec0[box];
+    totals += (size_t)box * ntiles;
+    tile_start += (size_t)box * (ntiles + 1);
+    if (cursor)
+        cursor += (size_t)box * ntiles;
+    mass_part += boxes.first[box];
+    field_mass += box;
+    field_sub += box;
+    st += box;
     if (threadIdx.x == 0)
-        carry = 0;
+        carry = rec0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int base = 0; base < ntiles; base += kScanThreads) {
@@ -359,7 +424,7 @@ __global__ void __launch_bounds__(kScanThreads)
             m = s;
         }
     } else {
-        m = (double)carry * uniform_mass;
+        m = (double)(carry - rec0) * uniform_mass;
     }
     if (threadIdx.x == 0) {
         // Scale: the largest |mass| maps into [2^27, 2^28) units of 2^-s, so one
@@ -396,14 +461,18 @@ __global__ void __launch_bounds__(kScanThreads)
 // Same blocking as k_sort_colsum: block sums, an exclusive scan of the 32
 // block sums per tile in shared memory, then each warp rewrites its block.
 __global__ void __launch_bounds__(32 * kColWarps)
-    k_sort_offsets(uint32_t *__restrict__ hist, int nsort, int ntiles,
+    k_sort_offsets(uint32_t *__restrict__ hist, const __grid_constant__ BoxRows rows, int ntiles,
                    const uint32_t *__restrict__ tile_start)
 {
     __shared__ uint32_t part[kColWarps][33];
+    const int box = blockIdx.y;
+    const int nsort = rows.first[box + 1] - rows.first[box];
+    hist += (size_t)rows.first[box] * ntiles;
+    tile_start += (size_t)box * (ntiles + 1);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int t = blockIdx.x * 32 + lane;
-    const int rows = (nsort + kColWarps - 1) / kColWarps;
-    const int r0 = min(w * rows, nsort), r1 = min(r0 + rows, nsort);
+    const int per_warp = (nsort + kColWarps - 1) / kColWarps;
+    const int r0 = min(w * per_warp, nsort), r1 = min(r0 + per_warp, nsort);
     part[w][lane] = column_block_sum(hist, ntiles, t, r0, r1);
     __syncthreads();
     if (w == 0) {
@@ -459,26 +528,30 @@ __device__ __forceinline__ uint4 pack_particle(const AxisQ a[3], float m, uint32
 // is rounded to an integer of 2^-(s+4) mass units and summed in 64-bit integers
 // (deterministic: fixed per-thread order, integer sums across warps).  The last log-k bin holds only
 // this mode, so its value must not carry the FP32 grid's rounding noise.
-template <bool GLOBAL>
+template <bool GLOBAL, class Src>
 __global__ void __launch_bounds__(kSortThreads)
-    k_sort_scatter(SortParams p, uint32_t *__restrict__ offs, uint4 *__restrict__ sorted,
-                   DeviceStatus *st)
+    k_sort_scatter(const __grid_constant__ Src src, uint32_t *__restrict__ offs,
+                   uint4 *__restrict__ sorted, DeviceStatus *st)
 {
     extern __shared__ uint32_t sh_cur[];
+    const int box = src.box_of(blockIdx.x);
+    const SortParams p = src.params(box);
+    const int cta = blockIdx.x - src.first_cta(box);
+    st += box;
     if (!GLOBAL) {
         const uint32_t *row = offs + (size_t)blockIdx.x * p.ntiles;
         for (int i = threadIdx.x; i < p.ntiles; i += blockDim.x)
             sh_cur[i] = row[i];
         __syncthreads();
     }
-    uint32_t *cur = GLOBAL ? offs : sh_cur;
+    uint32_t *cur = GLOBAL ? offs + (size_t)box * p.ntiles : sh_cur;
     const uint32_t mx = (1u << p.lx) - 1u, my = (1u << p.ly) - 1u, mz = (1u << p.lz) - 1u;
     const int lane = threadIdx.x & 31;
     // Corner terms in 2^-(s+4) mass units (|term| < 2^32), summed per thread as
     // a float pair and converted to an integer once per warp.
     const float mscale = ldexpf(1.f, st->fx_shift + 4);
     f2sum alt = {0.f, 0.f};
-    for_each_warp_batch(p, [&](bool in, const float *v, float m) {
+    for_each_warp_batch(p, cta, [&](bool in, const float *v, float m) {
         uint32_t t = kNoTile;
         AxisQ a[3];
         a[0] = a[1] = a[2] = AxisQ{0, 0u, 1.f, 0.f};
@@ -497,7 +570,8 @@ __global__ void __launch_bounds__(kSortThreads)
             slot = __shfl_sync(0xffffffffu, slot0, leader) + __popc(peers & ((1u << lane) - 1u));
         }
         if (t != kNoTile) {
-            sorted[slot] = pack_particle(a, m, mx, my, mz);
+            // (the mass word carries a uniform mass too, for grouped passes)
+            sorted[slot] = pack_particle(a, p.masses ? m : p.umass, mx, my, mz);
             if (p.corner) {
                 const float mm = (p.masses ? m : p.umass) * mscale;
                 f2sum u = corner_factor_q(a[0], a[1], a[2]);
@@ -652,17 +726,27 @@ __device__ __forceinline__ long long acc_get(const unsigned *lo, const unsigned 
     return (long long)(((unsigned long long)hi[idx] << 32) | lo[idx]);
 }
 
+// Tile blockIdx.x of box blockIdx.y (grid_stride floats between the boxes' grids).
 template <int TX, int TY, int TZ, bool VARMASS, bool CLEAN>
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_deposit(TileParams p, const uint4 *__restrict__ sorted,
                    const uint32_t *__restrict__ tile_start, DeviceStatus *__restrict__ st,
                    float *__restrict__ grid, long long *__restrict__ faces,
-                   long long *__restrict__ halo)
+                   long long *__restrict__ halo, int64_t grid_stride)
 {
     using L = TileLayout<TX, TY, TZ>;
     extern __shared__ unsigned acc_words[];
     unsigned *lo = acc_words, *hi = acc_words + L::NACC;
     const int t = blockIdx.x;
+    {
+        const int box = blockIdx.y;
+        const int ntiles = p.ntx * p.nty * p.ntz;
+        tile_start += (size_t)box * (ntiles + 1);
+        st += box;
+        grid += (size_t)box * (size_t)grid_stride;
+        faces += (size_t)box * ntiles * L::NFACE;
+        halo += (size_t)box * ntiles * L::NHALO;
+    }
     int tx, ty, tz;
     tile_coords(p, t, tx, ty, tz);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
@@ -755,10 +839,18 @@ template <int TX, int TY, int TZ, bool CLEAN>
 __global__ void __launch_bounds__(256)
     k_face_gather(TileParams p, const long long *__restrict__ faces,
                   const long long *__restrict__ halo, DeviceStatus *__restrict__ st,
-                  float *__restrict__ grid)
+                  float *__restrict__ grid, int64_t grid_stride)
 {
     using L = TileLayout<TX, TY, TZ>;
     const int t = blockIdx.x;
+    {
+        const int box = blockIdx.y;
+        const int ntiles = p.ntx * p.nty * p.ntz;
+        st += box;
+        grid += (size_t)box * (size_t)grid_stride;
+        faces += (size_t)box * ntiles * L::NFACE;
+        halo += (size_t)box * ntiles * L::NHALO;
+    }
     int tx, ty, tz;
     tile_coords(p, t, tx, ty, tz);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
@@ -805,10 +897,20 @@ __global__ void __launch_bounds__(256)
 // this pass's exact share, in mass units, joins the grid's running value.  (The
 // subtracted mean contributes nothing: the signs balance on an even grid.)  The
 // sum is zeroed for the next pass here, so no pass has to clear it first.
-__global__ void k_pass_finish(DeviceStatus *__restrict__ st, double *field_corner)
+// One thread per box; a grouped pass also hands each box's count of skipped
+// particles to bad_out and zeroes it.
+__global__ void k_pass_finish(DeviceStatus *__restrict__ st, double *field_corner, int nbox,
+                              unsigned long long *bad_out)
 {
-    *field_corner += ldexp((double)st->alt_sum, -(st->fx_shift + 4));
-    st->alt_sum = 0;
+    const int b = threadIdx.x;
+    if (b >= nbox)
+        return;
+    field_corner[b] += ldexp((double)st[b].alt_sum, -(st[b].fx_shift + 4));
+    st[b].alt_sum = 0;
+    if (bad_out) {
+        bad_out[b] = st[b].bad_particles;
+        st[b].bad_particles = 0;
+    }
 }
 
 int ilog2(int v)
@@ -819,8 +921,21 @@ int ilog2(int v)
     return l;
 }
 
+// What the tile kernels of a pass write: nbox grids from `grid` on, with
+// their corner sums and (grouped passes) skipped-particle counts.
+struct TileTarget {
+    float *grid;
+    int64_t grid_stride;
+    int nbox;
+    float mass;  // uniform mass when !var
+    bool var;    // records carry the masses
+    bool clean;
+    double *field_corner;
+    unsigned long long *bad_out;
+};
+
 template <int TX, int TY, int TZ>
-cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, DepositScratch &s,
+cudaError_t launch_tile_kernels(const DepositGeom &g, const TileTarget &a, DepositScratch &s,
                                 DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
                                 StageHook hook, void *hook_user)
 {
@@ -834,7 +949,8 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
     tp.ntz = g.ntz;
     tp.mass = a.mass;
     const size_t smem = 2 * sizeof(unsigned) * L::NACC;
-    const bool var = a.masses != nullptr;
+    const bool var = a.var;
+    const dim3 tiles((unsigned)g.ntiles, (unsigned)a.nbox);
     cudaError_t err;
 #define GENPK_TILE_LAUNCH(V, C)                                                                \
     do {                                                                                       \
@@ -842,8 +958,8 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
         err = ensure_dynamic_smem(kern, smem);                                                 \
         if (err != cudaSuccess)                                                                \
             return err;                                                                        \
-        kern<<<g.ntiles, kTileThreads, smem, stream>>>(tp, s.sorted, s.tile_start, dstat,      \
-                                                      a.grid, s.faces, s.halo);                \
+        kern<<<tiles, kTileThreads, smem, stream>>>(tp, s.sorted, s.tile_start, dstat, a.grid, \
+                                                   s.faces, s.halo, a.grid_stride);            \
     } while (0)
     if (var && a.clean)
         GENPK_TILE_LAUNCH(true, true);
@@ -860,19 +976,55 @@ cudaError_t launch_tile_kernels(const DepositGeom &g, const DepositArgs &a, Depo
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
     if (a.clean)
-        k_face_gather<TX, TY, TZ, true><<<g.ntiles, 256, 0, stream>>>(tp, s.faces, s.halo, dstat,
-                                                                      a.grid);
+        k_face_gather<TX, TY, TZ, true><<<tiles, 256, 0, stream>>>(tp, s.faces, s.halo, dstat,
+                                                                   a.grid, a.grid_stride);
     else
-        k_face_gather<TX, TY, TZ, false><<<g.ntiles, 256, 0, stream>>>(tp, s.faces, s.halo,
-                                                                       dstat, a.grid);
+        k_face_gather<TX, TY, TZ, false><<<tiles, 256, 0, stream>>>(tp, s.faces, s.halo, dstat,
+                                                                    a.grid, a.grid_stride);
     (*launches)++;
     if (hook)
         hook(hook_user, "dep_faces");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    k_pass_finish<<<1, 1, 0, stream>>>(dstat, a.field_corner);
+    k_pass_finish<<<1, ((a.nbox + 31) / 32) * 32, 0, stream>>>(dstat, a.field_corner, a.nbox,
+                                                               a.bad_out);
     (*launches)++;
     return cudaGetLastError();
+}
+
+cudaError_t launch_tile_pass(const DepositGeom &g, const TileTarget &t, DepositScratch &s,
+                             DeviceStatus *dstat, cudaStream_t stream, int64_t *launches,
+                             StageHook hook, void *hook_user)
+{
+    if (g.tx == 8)
+        return launch_tile_kernels<8, 8, 8>(g, t, s, dstat, stream, launches, hook, hook_user);
+    if (g.tz == 8)
+        return launch_tile_kernels<16, 16, 8>(g, t, s, dstat, stream, launches, hook, hook_user);
+    return launch_tile_kernels<16, 16, 16>(g, t, s, dstat, stream, launches, hook, hook_user);
+}
+
+SortParams sort_params(const DepositGeom &g, const float *pos, const float *masses, float mass,
+                       int64_t n, float uh, float ul, int ctas)
+{
+    SortParams sp;
+    sp.pos = pos;
+    sp.masses = masses;
+    sp.n = n;
+    sp.chunk = ctas > 0 ? (n + ctas - 1) / ctas : 1;
+    if (sp.chunk < 1)
+        sp.chunk = 1;
+    sp.dims = g.grid.dims;
+    sp.uh = uh;
+    sp.ul = ul;
+    sp.lx = ilog2(g.tx);
+    sp.ly = ilog2(g.ty);
+    sp.lz = ilog2(g.tz);
+    sp.nty = g.nty;
+    sp.ntz = g.ntz;
+    sp.ntiles = g.ntiles;
+    sp.umass = mass;
+    sp.corner = (g.grid.dims % 2 == 0) ? 1 : 0;
+    return sp;
 }
 
 }  // namespace
@@ -931,24 +1083,13 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
         if (hook)
             hook(hook_user, name);
     };
-    SortParams sp;
-    sp.pos = a.pos;
-    sp.masses = a.masses;
-    sp.n = a.n;
-    sp.chunk = (a.n + sort_ctas - 1) / sort_ctas;
-    if (sp.chunk < 1)
-        sp.chunk = 1;
-    sp.dims = g.grid.dims;
-    sp.uh = g.units_hi;
-    sp.ul = g.units_lo;
-    sp.lx = ilog2(g.tx);
-    sp.ly = ilog2(g.ty);
-    sp.lz = ilog2(g.tz);
-    sp.nty = g.nty;
-    sp.ntz = g.ntz;
-    sp.ntiles = g.ntiles;
-    sp.umass = a.mass;
-    sp.corner = (g.grid.dims % 2 == 0) ? 1 : 0;
+    const OneBox src{sort_params(g, a.pos, a.masses, a.mass, a.n, g.units_hi, g.units_lo,
+                                 sort_ctas)};
+    BoxRows rows = {};
+    rows.first[1] = sort_ctas;
+    ScanBoxes sb = {};
+    sb.first[1] = sort_ctas;
+    sb.umass[0] = a.masses ? -1.0 : (double)a.mass;
     const bool shared_hist = deposit_shared_hist(g);
     const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
     cudaError_t err;
@@ -957,48 +1098,130 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     const int cgrid = (g.ntiles + 31) / 32;
     const size_t hsmem = deposit_hist_smem(g);
     if (shared_hist) {
-        if ((err = ensure_dynamic_smem(k_sort_hist<false>, hsmem)) != cudaSuccess)
+        if ((err = ensure_dynamic_smem(k_sort_hist<false, OneBox>, hsmem)) != cudaSuccess)
             return err;
-        k_sort_hist<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.mass_part,
+        k_sort_hist<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(src, s.hist, s.mass_part,
                                                                        dstat);
         mark("dep_hist");
-        k_sort_colsum<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, sort_ctas, g.ntiles,
-                                                            s.totals);
+        k_sort_colsum<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, rows, g.ntiles, s.totals);
         mark("dep_colsum");
     } else {
         if ((err = cudaMemsetAsync(s.totals, 0, sizeof(uint32_t) * g.ntiles, stream)) !=
             cudaSuccess)
             return err;
-        k_sort_hist<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.totals, s.mass_part,
+        k_sort_hist<true><<<sort_ctas, kSortThreads, 0, stream>>>(src, s.totals, s.mass_part,
                                                                   dstat);
         mark("dep_hist");
     }
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    k_sort_scan<<<1, kScanThreads, 0, stream>>>(
-        s.totals, g.ntiles, s.tile_start, shared_hist ? nullptr : s.cursor, s.mass_part,
-        sort_ctas, a.masses ? -1.0 : (double)a.mass, 1.0 / n3, a.field_mass, a.field_sub, dstat);
+    k_sort_scan<<<1, kScanThreads, 0, stream>>>(s.totals, g.ntiles, s.tile_start,
+                                                shared_hist ? nullptr : s.cursor, s.mass_part, sb,
+                                                1.0 / n3, a.field_mass, a.field_sub, dstat);
     mark("dep_scan");
     if (shared_hist) {
-        k_sort_offsets<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, sort_ctas, g.ntiles,
+        k_sort_offsets<<<cgrid, 32 * kColWarps, 0, stream>>>(s.hist, rows, g.ntiles,
                                                              s.tile_start);
         mark("dep_offsets");
-        if ((err = ensure_dynamic_smem(k_sort_scatter<false>, hsmem)) != cudaSuccess)
+        if ((err = ensure_dynamic_smem(k_sort_scatter<false, OneBox>, hsmem)) != cudaSuccess)
             return err;
-        k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(sp, s.hist, s.sorted,
+        k_sort_scatter<false><<<sort_ctas, kSortThreads, hsmem, stream>>>(src, s.hist, s.sorted,
                                                                          dstat);
     } else {
-        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(sp, s.cursor, s.sorted,
+        k_sort_scatter<true><<<sort_ctas, kSortThreads, 0, stream>>>(src, s.cursor, s.sorted,
                                                                        dstat);
     }
     mark("dep_scatter");
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    if (g.tx == 8)
-        return launch_tile_kernels<8, 8, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
-    if (g.tz == 8)
-        return launch_tile_kernels<16, 16, 8>(g, a, s, dstat, stream, launches, hook, hook_user);
-    return launch_tile_kernels<16, 16, 16>(g, a, s, dstat, stream, launches, hook, hook_user);
+    const TileTarget t{a.grid, 0, 1, a.mass, a.masses != nullptr, a.clean, a.field_corner,
+                       nullptr};
+    return launch_tile_pass(g, t, s, dstat, stream, launches, hook, hook_user);
+}
+
+GroupLayout deposit_group_layout(int nbox, const GroupBox *boxes, int sort_ctas)
+{
+    GroupLayout lay = {};
+    lay.nbox = nbox;
+    int64_t total = 0;
+    for (int b = 0; b < nbox; b++)
+        total += boxes[b].n;
+    int c = 0;
+    int64_t r = 0;
+    for (int b = 0; b < nbox; b++) {
+        const int64_t n = boxes[b].n;
+        int k = 0;
+        if (n > 0) {
+            const double share = (double)sort_ctas * (double)n / (double)total;
+            k = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::llround(share),
+                                                            (n + 4095) / 4096));
+        }
+        lay.cta0[b] = c;
+        lay.rec0[b] = r;
+        c += k;
+        r += n;
+    }
+    lay.cta0[nbox] = c;
+    lay.rec0[nbox] = r;
+    return lay;
+}
+
+cudaError_t deposit_group_pass(const DepositGeom &g, const GroupLayout &lay, const GroupBox *boxes,
+                               float *grid0, int64_t grid_stride, double *field_mass0,
+                               double *field_sub0, double *field_corner0, DepositScratch &s,
+                               DeviceStatus *st0, unsigned long long *bad_out, cudaStream_t stream,
+                               int64_t *launches)
+{
+    const int nbox = lay.nbox;
+    if (nbox < 1 || nbox > kMaxGroupBoxes || !deposit_shared_hist(g) ||
+        lay.rec0[nbox] > (int64_t)0xfffffffeLL)
+        return cudaErrorInvalidValue;
+    BoxGroup src = {};
+    BoxRows rows = {};
+    ScanBoxes sb = {};
+    src.nbox = nbox;
+    for (int b = 0; b <= nbox; b++) {
+        src.cta0[b] = lay.cta0[b];
+        rows.first[b] = lay.cta0[b];
+        sb.first[b] = lay.cta0[b];
+    }
+    for (int b = 0; b < nbox; b++) {
+        const GroupBox &x = boxes[b];
+        src.p[b] = sort_params(g, x.pos, x.masses, x.mass, x.n, x.units_hi, x.units_lo,
+                               lay.cta0[b + 1] - lay.cta0[b]);
+        sb.umass[b] = x.masses ? -1.0 : (double)x.mass;
+        sb.rec0[b] = (long long)lay.rec0[b];
+    }
+    const int ctas = lay.cta0[nbox];
+    const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
+    const int cgrid = (g.ntiles + 31) / 32;
+    const size_t hsmem = deposit_hist_smem(g);
+    cudaError_t err;
+    if (ctas > 0) {
+        if ((err = ensure_dynamic_smem(k_sort_hist<false, BoxGroup>, hsmem)) != cudaSuccess)
+            return err;
+        k_sort_hist<false><<<ctas, kSortThreads, hsmem, stream>>>(src, s.hist, s.mass_part, st0);
+        (*launches)++;
+    }
+    k_sort_colsum<<<dim3(cgrid, nbox), 32 * kColWarps, 0, stream>>>(s.hist, rows, g.ntiles,
+                                                                     s.totals);
+    k_sort_scan<<<nbox, kScanThreads, 0, stream>>>(s.totals, g.ntiles, s.tile_start, nullptr,
+                                                   s.mass_part, sb, 1.0 / n3, field_mass0,
+                                                   field_sub0, st0);
+    k_sort_offsets<<<dim3(cgrid, nbox), 32 * kColWarps, 0, stream>>>(s.hist, rows, g.ntiles,
+                                                                      s.tile_start);
+    *launches += 3;
+    if (ctas > 0) {
+        if ((err = ensure_dynamic_smem(k_sort_scatter<false, BoxGroup>, hsmem)) != cudaSuccess)
+            return err;
+        k_sort_scatter<false><<<ctas, kSortThreads, hsmem, stream>>>(src, s.hist, s.sorted, st0);
+        (*launches)++;
+    }
+    if ((err = cudaGetLastError()) != cudaSuccess)
+        return err;
+    // every box's records carry its mass bits, so the tile kernels read them
+    const TileTarget t{grid0, grid_stride, nbox, 0.f, true, true, field_corner0, bad_out};
+    return launch_tile_pass(g, t, s, st0, stream, launches, nullptr, nullptr);
 }
 
 }  // namespace genpk

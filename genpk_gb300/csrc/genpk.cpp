@@ -15,6 +15,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <map>
 #include <string>
@@ -1054,7 +1056,7 @@ int ensure_row_major(genpk_ctx *ctx, int f)
 // N = 1024 (kz_ctas > 0) the field pending in the accumulator takes the
 // kz-major transform and is binned in that order (fused->done := true).
 struct FusedAuto {
-    int field;
+    int field;  // the binned field (the first of bin.fields consecutive ones)
     XfftBin bin;
     bool done;
     int kz_ctas = 0, kz_warps = 0;
@@ -1147,7 +1149,7 @@ int to_spectrum(genpk_ctx *ctx, const std::vector<int> &need, FusedAuto *fused =
                 GENPK_CUFFT(cufftExecR2C(h, (cufftReal *)base, (cufftComplex *)base));
                 stage_event(ctx, "fft");
             }
-            const bool bin = fused && batch == 1 && todo[i] == fused->field;
+            const bool bin = fused && batch == fused->bin.fields && todo[i] == fused->field;
             // The accumulator's clear, once its pass has been used, rides on a
             // binning x pass, whose bin walk leaves HBM bandwidth idle; the plain
             // x pass is faster and became HBM-bound with it (0.19 -> 0.36 ms at
@@ -1241,6 +1243,28 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
         fa.bin.partial = ctx->d_partial;
         fused = &fa;
     }
+    // The auto spectra of consecutive fields still to be transformed in one
+    // batch (a batch's grouped boxes): each binned inside the x pass, one
+    // histogram per field.
+    bool autos = np > 1 && use_xfft(ctx) && xfft_bin_supported(ctx->dims, nrb) &&
+                 (ctx->acc_pending < pairs[0] || ctx->acc_pending >= pairs[0] + np);
+    for (int q = 0; autos && q < np; q++)
+        autos = pairs[2 * q] == pairs[0] + q && pairs[2 * q + 1] == pairs[2 * q] &&
+                pair_mass[2 * q] == pair_mass[2 * q + 1] &&
+                ctx->state[(size_t)pairs[2 * q]] == F_DENSITY;
+    if (autos) {
+        const int ctas = xfft_bin_ctas(ctx->dims, np, ctx->num_sms);
+        GENPK_TRY(grow(ctx, &ctx->d_partial, &ctx->partial_cap, (size_t)ctas * np * nrb));
+        fa.field = pairs[0];
+        fa.bin.nrbins = nrb;
+        fa.bin.bpu_half = (float)(0.5 * ctx->tables.binsperunit);
+        fa.bin.thr = ctx->bdev.thr;
+        fa.bin.iw = ctx->bdev.iw;
+        fa.bin.corner = ctx->d_field_mass + 2 * ctx->nfields + pairs[0];
+        fa.bin.partial = ctx->d_partial;
+        fa.bin.fields = np;
+        fused = &fa;
+    }
     const bool auto1 = np == 1 && pairs[0] == pairs[1] && pair_mass[0] == pair_mass[1];
     if (!fused && auto1 && use_kz(ctx) && ctx->state[(size_t)pairs[0]] == F_DENSITY) {
         const int ctas = bin_kz_ctas(ctx->gg, nrb, ctx->num_sms, &fa.kz_warps, &fa.kz_smem);
@@ -1275,7 +1299,14 @@ int power_impl(genpk_ctx *ctx, int np, const int *pairs, const double *pair_mass
     if (!fa.done)  // every other binning reads the in-place r2c layout
         for (int f : fields)
             GENPK_TRY(ensure_row_major(ctx, f));
-    if (fa.done) {
+    if (fa.done && fa.bin.fields > 1) {
+        std::vector<double> m((size_t)np);
+        for (int q = 0; q < np; q++)
+            m[(size_t)q] = pair_mass[2 * q];
+        GENPK_CUDA(finalize_powers(ctx->d_partial, xfft_bin_ctas(ctx->dims, np, ctx->num_sms), nrb,
+                                   np, ctx->bdev.count, m.data(), ctx->res_dev, ctx->stream,
+                                   &ctx->launches, ctx->d_status, st_out));
+    } else if (fa.done) {
         const int ctas =
             fa.kz_ctas > 0 ? fa.kz_ctas : xfft_bin_ctas(ctx->dims, 1, ctx->num_sms);
         GENPK_CUDA(finalize_power(ctx->d_partial, ctas, nrb, ctx->bdev.count, pair_mass[0],
@@ -1453,6 +1484,8 @@ int adj_stage(genpk_ctx *ctx, size_t floats)
     return grow(ctx, &ctx->adj_buf, &ctx->adj_cap, floats);
 }
 
+int ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genpk_ctx **out);
+
 }  // namespace
 
 extern "C" {
@@ -1528,11 +1561,27 @@ void genpk_ctx_destroy(genpk_ctx *ctx)
 
 int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genpk_ctx **out)
 {
+    if (nfields > GENPK_MAX_FIELDS) {
+        if (out)
+            *out = nullptr;
+        return GENPK_ERR_INVALID;
+    }
+    return ctx_create(dims, nrbins, nfields, flags, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+// genpk_ctx_create without the public field limit: a batch's grouped boxes
+// are the fields of one internal context (up to kMaxGroupBoxes).
+int ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genpk_ctx **out)
+{
     if (!out)
         return GENPK_ERR_INVALID;
     *out = nullptr;
     if (dims < 2 || dims > 4096 || nrbins < 1 || nrbins > 65536 || nfields < 1 ||
-        nfields > GENPK_MAX_FIELDS)
+        nfields > std::max(GENPK_MAX_FIELDS, kMaxGroupBoxes))
         return GENPK_ERR_INVALID;
     genpk_ctx *ctx = new genpk_ctx();
     ctx->dims = dims;
@@ -1600,6 +1649,10 @@ int genpk_ctx_create(int64_t dims, int nrbins, int nfields, unsigned flags, genp
     *out = ctx;
     return GENPK_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int genpk_zero(genpk_ctx *ctx, int field)
 {
@@ -2199,13 +2252,42 @@ int64_t genpk_kernel_launches(const genpk_ctx *ctx)
 
 struct genpk_batch {
     std::vector<genpk_ctx *> box;
+    std::vector<int64_t> dims;
     int nrbins = 0;
+    unsigned flags = 0;
     std::string err;
+    int mode = GENPK_BATCH_AUTO;
+    int last_mode = -1;  // the way the latest call ran
+    // GENPK_BATCH_AUTO: for calls of one shape (particle counts and mass
+    // kinds), one untimed call each way (they tune), then one timed call each
+    // way; later calls take the faster way.
+    struct AutoChoice {
+        std::vector<int64_t> key;
+        int phase = 0;
+        double ms[2] = {0.0, 0.0};
+        int choice = GENPK_BATCH_PER_BOX;
+    } au;
+
+    // Grouped mode: the boxes of one grid size are the fields of one context
+    // and share each kernel launch of a grouped sorted-engine pass.
+    struct Group {
+        genpk_ctx *ctx = nullptr;
+        std::vector<int> boxes;                  // field f holds box boxes[f]
+        DeviceStatus *d_st = nullptr;            // per box: the pass's status words
+        unsigned long long *bad_host = nullptr;  // mapped: skipped particles per box
+        unsigned long long *bad_dev = nullptr;
+        bool tuned = false;
+        std::vector<int64_t> tuned_n;  // the particle counts it was tuned for
+        TileShape tile = {16, 16, 16};
+        int per_sm = 1;
+    };
+    std::vector<Group> groups;
 
     // CUDA graph of a whole call.  A call with the same arguments as the one
-    // before is captured (every box's work, forked from `origin` onto the
-    // boxes' streams and joined back) and later identical calls replay it:
-    // one graph launch per call instead of one launch per kernel.
+    // before is captured (every unit's work -- a box, or a group of boxes --
+    // forked from `origin` onto the units' streams and joined back) and later
+    // identical calls replay it: one graph launch per call instead of one
+    // launch per kernel.
     bool graph_on = true;
     bool graph_failed = false;  // a capture failed: calls stay eager
     int graph_attempts = 0;
@@ -2225,10 +2307,11 @@ struct genpk_batch {
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
     cudaGraphExec_t exec = nullptr;
-    std::vector<int64_t> graph_launches;  // per box: kernels one replay launches
+    bool graph_grouped = false;           // the graph is of a grouped call
+    std::vector<int64_t> graph_launches;  // per unit: kernels one replay launches
     std::vector<genpk_ctx::Deferred> graph_deferred;
     std::vector<bool> graph_issued;
-    std::vector<uint64_t> graph_digest;  // per box, at capture
+    std::vector<uint64_t> graph_digest;  // per unit, at capture
     int64_t replays = 0;
 };
 
@@ -2239,6 +2322,252 @@ void drop_graph(genpk_batch *b)
     if (b->exec)
         cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
+}
+
+void destroy_groups(genpk_batch *b)
+{
+    for (genpk_batch::Group &g : b->groups) {
+        genpk_ctx_destroy(g.ctx);
+        cudaFree(g.d_st);
+        cudaFreeHost(g.bad_host);
+    }
+    b->groups.clear();
+}
+
+// The groups of the grouped mode: boxes of one grid size, in the order of
+// their first box, at most kMaxGroupBoxes to a group.
+int make_groups(genpk_batch *b)
+{
+    if (!b->groups.empty())
+        return GENPK_OK;
+    const int nb = (int)b->box.size();
+    std::vector<bool> taken((size_t)nb, false);
+    for (int i = 0; i < nb; i++) {
+        if (taken[(size_t)i])
+            continue;
+        genpk_batch::Group g;
+        for (int j = i; j < nb && (int)g.boxes.size() < kMaxGroupBoxes; j++)
+            if (!taken[(size_t)j] && b->dims[(size_t)j] == b->dims[(size_t)i]) {
+                g.boxes.push_back(j);
+                taken[(size_t)j] = true;
+            }
+        const int nf = (int)g.boxes.size();
+        int rc = ctx_create(b->dims[(size_t)i], b->nrbins, nf, b->flags & ~GENPK_FLAG_TIMING,
+                            &g.ctx);
+        std::string why = rc != GENPK_OK && g.ctx ? genpk_last_error(g.ctx) : "";
+        if (rc == GENPK_OK) {
+            cudaError_t e = cudaMalloc(&g.d_st, sizeof(DeviceStatus) * (size_t)nf);
+            if (e == cudaSuccess)
+                e = cudaMemset(g.d_st, 0, sizeof(DeviceStatus) * (size_t)nf);
+            if (e == cudaSuccess)
+                e = cudaHostAlloc((void **)&g.bad_host, sizeof(unsigned long long) * (size_t)nf,
+                                  cudaHostAllocMapped);
+            if (e == cudaSuccess)
+                e = cudaHostGetDevicePointer((void **)&g.bad_dev, g.bad_host, 0);
+            if (e != cudaSuccess) {
+                rc = e == cudaErrorMemoryAllocation ? GENPK_ERR_NOMEM : GENPK_ERR_CUDA;
+                why = cudaGetErrorString(e);
+                cudaGetLastError();
+            }
+        }
+        b->groups.push_back(g);
+        if (rc != GENPK_OK) {
+            b->err = "group of box " + std::to_string(i) + ": " + why + " (" +
+                     genpk_status_string(rc) + ")";
+            destroy_groups(b);
+            return rc;
+        }
+    }
+    return GENPK_OK;
+}
+
+// Whether a call can run grouped: valid arguments (the per-box path reports
+// the others, box by box), device-resident particles, grids whose tile
+// histograms fit in shared memory, fewer than 2^32 particles per group.
+bool groupable(const genpk_batch *b, const double *boxsize, const float *const *pos,
+               const float *const *masses, const double *mass, const int64_t *n)
+{
+    const int nb = (int)b->box.size();
+    for (int i = 0; i < nb; i++) {
+        if (n[i] < 0 || (n[i] > 0 && !pos[i]) || !(boxsize[i] > 0.0) ||
+            !std::isfinite(boxsize[i]) || (!(masses && masses[i]) && !std::isfinite(mass[i])))
+            return false;
+        if (n[i] > 0 && !is_device_ptr(pos[i]))
+            return false;
+        if (masses && masses[i] && n[i] > 0 && !is_device_ptr(masses[i]))
+            return false;
+        if (b->box[(size_t)i]->flags & GENPK_FLAG_TIMING)
+            return false;
+        DepositGeom g = deposit_geom(b->box[(size_t)i], 1.0, TileShape{16, 16, 16});
+        if (!deposit_shared_hist(g))
+            return false;
+    }
+    std::vector<int64_t> total;
+    std::vector<int64_t> key;
+    for (int i = 0; i < nb; i++) {
+        size_t k = 0;
+        while (k < key.size() && key[k] != b->dims[(size_t)i])
+            k++;
+        if (k == key.size()) {
+            key.push_back(b->dims[(size_t)i]);
+            total.push_back(0);
+        }
+        total[k] += n[i];
+    }
+    for (int64_t t : total)
+        if (t > 0xfffffffeLL)
+            return false;
+    return true;
+}
+
+// Scratch of a grouped pass in the group context's sorted-engine buffers.
+int grow_group_scratch(genpk_ctx *ctx, const DepositGeom &g, const GroupLayout &lay)
+{
+    DepositScratch &s = ctx->dscr;
+    const int nb = lay.nbox;
+    const int ctas = lay.cta0[nb];
+    GENPK_TRY(grow(ctx, &s.hist, &s.hist_cap, std::max<size_t>(1, (size_t)ctas * g.ntiles)));
+    GENPK_TRY(grow(ctx, &s.tile_start, &s.tile_start_cap, (size_t)nb * (g.ntiles + 1)));
+    GENPK_TRY(grow(ctx, &s.totals, &s.tile_cap, (size_t)nb * g.ntiles + 1));
+    GENPK_TRY(grow(ctx, &s.sorted, &s.sorted_cap, (size_t)std::max<int64_t>(lay.rec0[nb], 1)));
+    size_t nface = 0, nhalo = 0;
+    deposit_scratch_sizes(g, &nface, &nhalo);
+    GENPK_TRY(grow(ctx, &s.faces, &s.faces_cap, nface * nb));
+    GENPK_TRY(grow(ctx, &s.halo, &s.halo_cap, nhalo * nb));
+    size_t mp = (size_t)s.mass_part_cap;
+    GENPK_TRY(grow(ctx, &s.mass_part, &mp, (size_t)std::max(ctas, 1)));
+    s.mass_part_cap = (int)mp;
+    return GENPK_OK;
+}
+
+// One grouped pass of every box of group g into its field (which must be
+// clean, with zero field sums).
+int group_pass(genpk_batch::Group &g, const std::vector<GroupBox> &gb, TileShape tile, int per_sm)
+{
+    genpk_ctx *ctx = g.ctx;
+    int64_t total = 0;
+    for (const GroupBox &x : gb)
+        total += x.n;
+    const DepositGeom geo = deposit_geom(ctx, 1.0, tile);
+    const int ctas = deposit_sort_ctas(geo, std::max<int64_t>(total, 1), ctx->num_sms, per_sm);
+    const GroupLayout lay = deposit_group_layout((int)gb.size(), gb.data(), ctas);
+    GENPK_TRY(grow_group_scratch(ctx, geo, lay));
+    GENPK_CUDA(deposit_group_pass(geo, lay, gb.data(), ctx->grids, ctx->gg.nfloat, ctx->d_field_mass,
+                                  ctx->d_field_mass + ctx->nfields, ctx->d_field_mass + 2 * ctx->nfields,
+                                  ctx->dscr, g.d_st, g.bad_dev, ctx->stream, &ctx->launches));
+    ctx->last_tile = tile;
+    ctx->last_sort_ctas = lay.cta0[lay.nbox];
+    ctx->last_engine = GENPK_ENGINE_SORTED;
+    return GENPK_OK;
+}
+
+// The group's tile shape and sort CTAs per SM, timed as tune_sorted times
+// the single-box candidates (the best of kTuneReps passes each); the trials
+// are kept in the group context (genpk_deposit_trials).
+int tune_group(genpk_batch::Group &g, const std::vector<GroupBox> &gb)
+{
+    static const TileShape tiles[] = {{8, 8, 8}, {16, 16, 8}, {16, 16, 16}};
+    static const int pers[] = {1, 2};
+    genpk_ctx *ctx = g.ctx;
+    int64_t total = 0;
+    for (const GroupBox &x : gb)
+        total += x.n;
+    cudaEvent_t e0, e1;
+    GENPK_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(ctx, GENPK_ERR_CUDA, "tune_group: cudaEventCreate failed");
+    }
+    struct Ev {
+        cudaEvent_t a, b;
+        ~Ev() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } ev{e0, e1};
+    const size_t sums = sizeof(double) * 3 * (size_t)ctx->nfields;
+    float best_ms = 1e30f;
+    ctx->ntrials = 0;
+    for (const TileShape &t : tiles) {
+        const DepositGeom geo = deposit_geom(ctx, 1.0, t);
+        if (!deposit_shared_hist(geo))
+            continue;
+        int last_ctas = -1;
+        for (int per : pers) {
+            const int ctas = deposit_sort_ctas(geo, std::max<int64_t>(total, 1), ctx->num_sms, per);
+            if (ctas == last_ctas)
+                continue;
+            last_ctas = ctas;
+            float ms = 1e30f;
+            for (int rep = 0; rep < kTuneReps; rep++) {
+                GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass, 0, sums, ctx->stream));
+                GENPK_CUDA(cudaEventRecord(e0, ctx->stream));
+                GENPK_TRY(group_pass(g, gb, t, per));
+                GENPK_CUDA(cudaEventRecord(e1, ctx->stream));
+                GENPK_CUDA(cudaEventSynchronize(e1));
+                float x = 0.f;
+                GENPK_CUDA(cudaEventElapsedTime(&x, e0, e1));
+                ms = std::min(ms, x);
+            }
+            if (ctx->ntrials < genpk_ctx::kMaxTrials) {
+                ctx->trial_tile[ctx->ntrials] = t;
+                ctx->trial_ctas[ctx->ntrials] = ctas;
+                ctx->trial_ms[ctx->ntrials] = ms;
+                ctx->ntrials++;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                g.tile = t;
+                g.per_sm = per;
+            }
+        }
+    }
+    GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass, 0, sums, ctx->stream));
+    g.tuned = true;
+    return GENPK_OK;
+}
+
+// Issues group g's work: every box deposited into its field by one grouped
+// pass, then the auto spectra of all the fields (one batched transform of
+// their x-planes, one x pass, binning of up to four fields per launch), to be
+// collected by power_collect.
+int group_issue(genpk_batch::Group &g, const double *boxsize, const float *const *pos,
+                const float *const *masses, const double *mass, const int64_t *n,
+                const double *mass_norm)
+{
+    genpk_ctx *ctx = g.ctx;
+    const int nf = (int)g.boxes.size();
+    cudaSetDevice(ctx->device);
+    std::vector<GroupBox> gb((size_t)nf);
+    std::vector<int64_t> counts((size_t)nf);
+    for (int f = 0; f < nf; f++) {
+        const int i = g.boxes[(size_t)f];
+        const double units = (double)ctx->dims / boxsize[i];
+        GroupBox &x = gb[(size_t)f];
+        x.n = n[i];
+        x.pos = n[i] > 0 ? pos[i] : nullptr;
+        x.masses = masses && n[i] > 0 ? masses[i] : nullptr;
+        x.mass = (float)mass[i];
+        x.units_hi = (float)units;
+        x.units_lo = (float)(units - (double)x.units_hi);
+        counts[(size_t)f] = n[i];
+        ctx->state[(size_t)f] = F_CLEAN;
+        ctx->auto_valid[(size_t)f] = false;
+        ctx->kzmajor[(size_t)f] = false;
+        ctx->corner_valid[(size_t)f] = false;
+    }
+    GENPK_CUDA(cudaMemsetAsync(ctx->d_field_mass, 0, sizeof(double) * 3 * (size_t)ctx->nfields,
+                               ctx->stream));
+    if (!g.tuned || g.tuned_n != counts) {
+        GENPK_TRY(tune_group(g, gb));
+        g.tuned_n = counts;
+    }
+    GENPK_TRY(group_pass(g, gb, g.tile, g.per_sm));
+    std::vector<int> pairs((size_t)2 * nf);
+    std::vector<double> pm((size_t)2 * nf);
+    for (int f = 0; f < nf; f++) {
+        ctx->state[(size_t)f] = F_DENSITY;
+        pairs[(size_t)2 * f] = pairs[(size_t)2 * f + 1] = f;
+        pm[(size_t)2 * f] = pm[(size_t)2 * f + 1] = mass_norm[g.boxes[(size_t)f]];
+    }
+    return power_impl(ctx, nf, pairs.data(), pm.data(), nullptr, nullptr, nullptr, true);
 }
 
 }  // namespace
@@ -2256,6 +2585,7 @@ void genpk_batch_destroy(genpk_batch *b)
         cudaEventDestroy(e);
     for (genpk_ctx *c : b->box)
         genpk_ctx_destroy(c);
+    destroy_groups(b);
     delete b;
 }
 
@@ -2277,6 +2607,44 @@ int64_t genpk_batch_graph_replays(const genpk_batch *b)
     return b ? b->replays : -1;
 }
 
+int genpk_batch_set_mode(genpk_batch *b, int mode)
+{
+    if (!b || (mode != GENPK_BATCH_PER_BOX && mode != GENPK_BATCH_GROUPED &&
+               mode != GENPK_BATCH_AUTO))
+        return GENPK_ERR_INVALID;
+    if (mode != b->mode) {
+        drop_graph(b);
+        b->repeats = 0;
+        b->have_last = false;
+        b->au = genpk_batch::AutoChoice{};
+    }
+    b->mode = mode;
+    return GENPK_OK;
+}
+
+int genpk_batch_last_mode(const genpk_batch *b)
+{
+    return b ? b->last_mode : -1;
+}
+
+int genpk_batch_groups(const genpk_batch *b)
+{
+    return b ? (int)b->groups.size() : -1;
+}
+
+genpk_ctx *genpk_batch_group(genpk_batch *b, int g, int *nboxes, int *boxes)
+{
+    if (!b || g < 0 || g >= (int)b->groups.size())
+        return nullptr;
+    const genpk_batch::Group &gr = b->groups[(size_t)g];
+    if (nboxes)
+        *nboxes = (int)gr.boxes.size();
+    if (boxes)
+        for (size_t f = 0; f < gr.boxes.size(); f++)
+            boxes[f] = gr.boxes[f];
+    return gr.ctx;
+}
+
 int genpk_batch_create(int nboxes, const int64_t *dims, int nrbins, unsigned flags,
                        genpk_batch **out)
 {
@@ -2287,6 +2655,8 @@ int genpk_batch_create(int nboxes, const int64_t *dims, int nrbins, unsigned fla
         return GENPK_ERR_INVALID;
     genpk_batch *b = new genpk_batch();
     b->nrbins = nrbins;
+    b->flags = flags;
+    b->dims.assign(dims, dims + nboxes);
     for (int i = 0; i < nboxes; i++) {
         genpk_ctx *c = nullptr;
         const int rc = genpk_ctx_create(dims[i], nrbins, 1, flags, &c);
@@ -2322,6 +2692,8 @@ int64_t genpk_batch_launches(const genpk_batch *b)
     int64_t k = 0;
     for (const genpk_ctx *c : b->box)
         k += c->launches;
+    for (const genpk_batch::Group &g : b->groups)
+        k += g.ctx->launches;
     return k;
 }
 
@@ -2336,36 +2708,17 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
         b->err = "genpk_batch_power: null argument";
         return GENPK_ERR_INVALID;
     }
-    // largest boxes first: their passes start first, the small ones fill in
-    std::vector<int> order((size_t)nb);
-    for (int i = 0; i < nb; i++)
-        order[(size_t)i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
     const int nrb = b->nrbins;
     int first = GENPK_OK;
-    std::vector<bool> issued((size_t)nb, false);
-    auto note = [&](int i, int rc) {
+    auto note_msg = [&](int rc, const std::string &msg) {
         if (rc != GENPK_OK && first == GENPK_OK) {
             first = rc;
-            b->err = "box " + std::to_string(i) + ": " + genpk_last_error(b->box[(size_t)i]);
+            b->err = msg;
         }
     };
-    auto issue = [&](int i) -> int {
-        genpk_ctx *c = b->box[(size_t)i];
-        cudaSetDevice(c->device);
-        c->batch_mode = true;
-        int rc = genpk_zero(c, 0);
-        if (rc == GENPK_OK)
-            rc = genpk_deposit(c, 0, boxsize[i], pos[i], masses ? masses[i] : nullptr, mass[i],
-                               n[i]);
-        if (rc == GENPK_OK) {
-            const int pr[2] = {0, 0};
-            const double pm[2] = {mass_norm[i], mass_norm[i]};
-            rc = power_impl(c, 1, pr, pm, nullptr, nullptr, nullptr, true);
-            issued[(size_t)i] = rc == GENPK_OK;
-        }
-        c->batch_mode = false;
-        return rc;
+    auto note = [&](int i, int rc) {
+        if (rc != GENPK_OK)
+            note_msg(rc, "box " + std::to_string(i) + ": " + genpk_last_error(b->box[(size_t)i]));
     };
 
     // The arguments, for the repeat test of the graph path.
@@ -2387,10 +2740,93 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
     } else {
         b->repeats++;
     }
+
+    // Per box or grouped: as set, or (AUTO) by the trial calls' timings.
+    const bool can_group = b->mode != GENPK_BATCH_PER_BOX &&
+                           groupable(b, boxsize, pos, masses, mass, n);
+    bool want_group = b->mode == GENPK_BATCH_GROUPED;
+    bool trial = false;
+    int timed_slot = -1;
+    if (b->mode == GENPK_BATCH_AUTO && can_group) {
+        genpk_batch::AutoChoice &au = b->au;
+        std::vector<int64_t> key(n, n + nb);
+        for (int i = 0; i < nb; i++)
+            key.push_back(masses && masses[i] ? 1 : 0);
+        if (key != au.key) {
+            au = genpk_batch::AutoChoice{};
+            au.key = key;
+        }
+        trial = au.phase < 4;
+        want_group = trial ? (au.phase & 1) != 0 : au.choice == GENPK_BATCH_GROUPED;
+        if (au.phase >= 2 && au.phase < 4)
+            timed_slot = au.phase - 2;
+    }
+    const auto t_start = std::chrono::steady_clock::now();
+    // The units of work: boxes (largest first, so that their passes start
+    // first and the small ones fill in), or groups of boxes (largest first).
+    const bool grouped = want_group && can_group;
+    if (grouped) {
+        const int rc = make_groups(b);
+        if (rc != GENPK_OK)
+            return rc;
+    }
+    std::vector<int> order;
+    std::vector<genpk_ctx *> unit;
+    if (grouped) {
+        std::vector<int64_t> tot(b->groups.size(), 0);
+        for (size_t g = 0; g < b->groups.size(); g++) {
+            order.push_back((int)g);
+            for (int i : b->groups[g].boxes)
+                tot[g] += n[i];
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return tot[(size_t)x] > tot[(size_t)y]; });
+        for (const genpk_batch::Group &g : b->groups)
+            unit.push_back(g.ctx);
+    } else {
+        for (int i = 0; i < nb; i++)
+            order.push_back(i);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+        unit = b->box;
+    }
+    if (b->exec && b->graph_grouped != grouped)
+        drop_graph(b);
+    const int nu = (int)unit.size();
+    std::vector<bool> issued((size_t)nu, false);
+    auto issue = [&](int u) -> int {
+        genpk_ctx *c = unit[(size_t)u];
+        cudaSetDevice(c->device);
+        int rc;
+        if (grouped) {
+            rc = group_issue(b->groups[(size_t)u], boxsize, pos, masses, mass, n, mass_norm);
+        } else {
+            c->batch_mode = true;
+            rc = genpk_zero(c, 0);
+            if (rc == GENPK_OK)
+                rc = genpk_deposit(c, 0, boxsize[u], pos[u], masses ? masses[u] : nullptr,
+                                   mass[u], n[u]);
+            if (rc == GENPK_OK) {
+                const int pr[2] = {0, 0};
+                const double pm[2] = {mass_norm[u], mass_norm[u]};
+                rc = power_impl(c, 1, pr, pm, nullptr, nullptr, nullptr, true);
+            }
+            c->batch_mode = false;
+        }
+        issued[(size_t)u] = rc == GENPK_OK;
+        return rc;
+    };
+    auto note_unit = [&](int u, int rc) {
+        if (rc == GENPK_OK)
+            return;
+        if (!grouped)
+            return note(u, rc);
+        note_msg(rc, "boxes of grid " + std::to_string(unit[(size_t)u]->dims) + ": " +
+                         genpk_last_error(unit[(size_t)u]));
+    };
+
     // One device, no stage events (a replay does not re-record them), and
     // particles in device memory: host input goes through host-side copies
     // into staging buffers, which a replay would not repeat.
-    bool graphable = b->graph_on && !b->graph_failed;
+    bool graphable = b->graph_on && !b->graph_failed && !trial;
     for (int i = 0; graphable && i < nb; i++) {
         const genpk_ctx *c = b->box[(size_t)i];
         graphable = c->device == b->box[0]->device && !(c->flags & GENPK_FLAG_TIMING) &&
@@ -2398,62 +2834,62 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
                     (!masses || !masses[i] || is_device_ptr(masses[i]));
     }
     if (b->exec) {
-        for (int i = 0; i < nb; i++)
-            if (issue_digest(b->box[(size_t)i]) != b->graph_digest[(size_t)i] ||
-                b->box[(size_t)i]->deferred.active) {
-                drop_graph(b);  // a box was used on its own since the capture
+        for (int u = 0; u < nu; u++)
+            if (issue_digest(unit[(size_t)u]) != b->graph_digest[(size_t)u] ||
+                unit[(size_t)u]->deferred.active) {
+                drop_graph(b);  // a unit was used on its own since the capture
                 break;
             }
     }
     if (graphable && !b->exec && b->repeats >= 1) {
-        // Capture this call: every box's work, forked from `origin`.
-        cudaSetDevice(b->box[0]->device);
+        // Capture this call: every unit's work, forked from `origin`.
+        cudaSetDevice(unit[0]->device);
         bool ok = true;
         if (!b->origin)
             ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
                  cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
-        while (ok && (int)b->join.size() < nb) {
+        while (ok && (int)b->join.size() < nu) {
             cudaEvent_t e;
             ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
             if (ok)
                 b->join.push_back(e);
         }
-        std::vector<uint64_t> before((size_t)nb);
-        std::vector<int64_t> launched((size_t)nb);
+        std::vector<uint64_t> before((size_t)nu);
+        std::vector<int64_t> launched((size_t)nu);
         std::vector<IssueState> saved;
-        for (int i = 0; i < nb; i++) {
-            before[(size_t)i] = issue_digest(b->box[(size_t)i]);
-            launched[(size_t)i] = b->box[(size_t)i]->launches;
-            saved.emplace_back(b->box[(size_t)i]);
+        for (int u = 0; u < nu; u++) {
+            before[(size_t)u] = issue_digest(unit[(size_t)u]);
+            launched[(size_t)u] = unit[(size_t)u]->launches;
+            saved.emplace_back(unit[(size_t)u]);
         }
         ok = ok && cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed) == cudaSuccess;
         bool began = ok;
         ok = ok && cudaEventRecord(b->fork, b->origin) == cudaSuccess;
-        for (int i = 0; ok && i < nb; i++)
-            ok = cudaStreamWaitEvent(b->box[(size_t)i]->stream, b->fork, 0) == cudaSuccess;
-        for (int i : order)
+        for (int u = 0; ok && u < nu; u++)
+            ok = cudaStreamWaitEvent(unit[(size_t)u]->stream, b->fork, 0) == cudaSuccess;
+        for (int u : order)
             if (ok)
-                ok = issue(i) == GENPK_OK;
-        for (int i = 0; ok && i < nb; i++)
-            ok = cudaEventRecord(b->join[(size_t)i], b->box[(size_t)i]->stream) == cudaSuccess &&
-                 cudaStreamWaitEvent(b->origin, b->join[(size_t)i], 0) == cudaSuccess;
+                ok = issue(u) == GENPK_OK;
+        for (int u = 0; ok && u < nu; u++)
+            ok = cudaEventRecord(b->join[(size_t)u], unit[(size_t)u]->stream) == cudaSuccess &&
+                 cudaStreamWaitEvent(b->origin, b->join[(size_t)u], 0) == cudaSuccess;
         cudaGraph_t g = nullptr;
         if (began)
             ok = cudaStreamEndCapture(b->origin, &g) == cudaSuccess && ok;
         const bool cuda_ok = ok;
-        b->graph_launches.assign((size_t)nb, 0);
-        b->graph_deferred.assign((size_t)nb, genpk_ctx::Deferred{});
-        for (int i = 0; i < nb; i++) {
-            genpk_ctx *c = b->box[(size_t)i];
-            b->graph_launches[(size_t)i] = c->launches - launched[(size_t)i];
-            c->launches = launched[(size_t)i];  // nothing ran yet
-            b->graph_deferred[(size_t)i] = c->deferred;
+        b->graph_launches.assign((size_t)nu, 0);
+        b->graph_deferred.assign((size_t)nu, genpk_ctx::Deferred{});
+        for (int u = 0; u < nu; u++) {
+            genpk_ctx *c = unit[(size_t)u];
+            b->graph_launches[(size_t)u] = c->launches - launched[(size_t)u];
+            c->launches = launched[(size_t)u];  // nothing ran yet
+            b->graph_deferred[(size_t)u] = c->deferred;
             c->deferred.active = false;
         }
-        // The call must leave every box as it found it, so that each replay
+        // The call must leave every unit as it found it, so that each replay
         // starts from the state the capture started from.
-        for (int i = 0; ok && i < nb; i++)
-            ok = issue_digest(b->box[(size_t)i]) == before[(size_t)i];
+        for (int u = 0; ok && u < nu; u++)
+            ok = issue_digest(unit[(size_t)u]) == before[(size_t)u];
         if (ok)
             ok = cudaGraphInstantiate(&b->exec, g, 0) == cudaSuccess;
         if (ok)
@@ -2462,22 +2898,23 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
             cudaGraphDestroy(g);
         b->graph_issued = issued;
         b->graph_digest = before;
+        b->graph_grouped = grouped;
         if (!ok) {
-            // Nothing ran: put back each box's record of its device state and
-            // run the call eagerly.  A call that did not leave the boxes as it
+            // Nothing ran: put back each unit's record of its device state and
+            // run the call eagerly.  A call that did not leave the units as it
             // found them may do so the next time (a first pass allocates,
             // tunes, clears); a CUDA error during capture ends the graph path.
             cudaGetLastError();
             b->exec = nullptr;
             if (!cuda_ok || ++b->graph_attempts >= 3)
                 b->graph_failed = true;
-            for (int i = 0; i < nb; i++)
-                saved[(size_t)i].restore(b->box[(size_t)i]);
+            for (int u = 0; u < nu; u++)
+                saved[(size_t)u].restore(unit[(size_t)u]);
             std::fill(issued.begin(), issued.end(), false);
         }
     }
     if (b->exec) {
-        cudaSetDevice(b->box[0]->device);
+        cudaSetDevice(unit[0]->device);
         if (cudaGraphLaunch(b->exec, b->origin) != cudaSuccess ||
             cudaStreamSynchronize(b->origin) != cudaSuccess) {
             b->err = std::string("genpk_batch_power: graph replay failed: ") +
@@ -2486,27 +2923,74 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
             return GENPK_ERR_CUDA;
         }
         b->replays++;
-        for (int i = 0; i < nb; i++) {
-            genpk_ctx *c = b->box[(size_t)i];
-            c->launches += b->graph_launches[(size_t)i];
-            c->deferred = b->graph_deferred[(size_t)i];
+        for (int u = 0; u < nu; u++) {
+            genpk_ctx *c = unit[(size_t)u];
+            c->launches += b->graph_launches[(size_t)u];
+            c->deferred = b->graph_deferred[(size_t)u];
         }
         issued = b->graph_issued;
     } else {
-        for (int i : order)
-            note(i, issue(i));
+        for (int u : order)
+            note_unit(u, issue(u));
     }
-    for (int i : order) {  // every issued box is waited for, even after a failure
-        if (!issued[(size_t)i])
+    std::vector<double> gp, gk;
+    std::vector<int> gc;
+    for (int u : order) {  // every issued unit is waited for, even after a failure
+        if (!issued[(size_t)u])
             continue;
-        genpk_ctx *c = b->box[(size_t)i];
+        genpk_ctx *c = unit[(size_t)u];
         cudaSetDevice(c->device);
-        note(i, power_collect(c, power + (size_t)i * nrb, count ? count + (size_t)i * nrb : nullptr,
-                              keffs ? keffs + (size_t)i * nrb : nullptr));
+        if (!grouped) {
+            note(u, power_collect(c, power + (size_t)u * nrb,
+                                  count ? count + (size_t)u * nrb : nullptr,
+                                  keffs ? keffs + (size_t)u * nrb : nullptr));
+            continue;
+        }
+        const genpk_batch::Group &g = b->groups[(size_t)u];
+        const size_t nf = g.boxes.size();
+        gp.assign(nf * nrb, 0.0);
+        gc.assign((size_t)nrb, 0);
+        gk.assign((size_t)nrb, 0.0);
+        const int rc = power_collect(c, gp.data(), gc.data(), gk.data());
+        note_unit(u, rc);
+        for (size_t f = 0; f < nf; f++) {
+            const int i = g.boxes[f];
+            std::copy(gp.begin() + f * nrb, gp.begin() + (f + 1) * nrb, power + (size_t)i * nrb);
+            if (count)
+                std::copy(gc.begin(), gc.end(), count + (size_t)i * nrb);
+            if (keffs)
+                std::copy(gk.begin(), gk.end(), keffs + (size_t)i * nrb);
+            if (g.bad_host[f])
+                note_msg(GENPK_ERR_BAD_INPUT,
+                         "box " + std::to_string(i) + ": " + std::to_string(g.bad_host[f]) +
+                             " particle(s) with non-finite or out-of-range position/mass were "
+                             "skipped");
+        }
+    }
+    b->last_mode = grouped ? GENPK_BATCH_GROUPED : GENPK_BATCH_PER_BOX;
+    if (b->mode == GENPK_BATCH_AUTO && can_group && first == GENPK_OK && trial) {
+        genpk_batch::AutoChoice &au = b->au;
+        if (timed_slot >= 0)
+            au.ms[timed_slot] = std::chrono::duration<double, std::milli>(
+                                    std::chrono::steady_clock::now() - t_start)
+                                    .count();
+        if (++au.phase == 4)
+            au.choice = au.ms[1] < au.ms[0] ? GENPK_BATCH_GROUPED : GENPK_BATCH_PER_BOX;
     }
     if (first == GENPK_OK)
         b->err.clear();
     return first;
+}
+
+int genpk_batch_auto_times(const genpk_batch *b, double *per_box_ms, double *grouped_ms)
+{
+    if (!b)
+        return -1;
+    if (per_box_ms)
+        *per_box_ms = b->au.ms[0];
+    if (grouped_ms)
+        *grouped_ms = b->au.ms[1];
+    return b->au.phase >= 4 ? b->au.choice : -1;
 }
 
 int genpk_inject_copy_timeout(genpk_ctx *ctx, int64_t chunk, int64_t wait_clocks)

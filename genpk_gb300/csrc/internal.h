@@ -126,6 +126,42 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
                          DeviceStatus *dstat, int sort_ctas, cudaStream_t stream,
                          int64_t *launches, StageHook hook, void *hook_user);
 
+// Grouped sorted-engine pass: the boxes of a batch that share a grid size go
+// through one launch of each kernel of the pass.  Each box has its own
+// particles, box size and mass, and its own clean grid (box b's at
+// grid0 + b * grid_stride), field sums (field_mass0[b], field_sub0[b],
+// field_corner0[b]) and status words (st0[b]).
+constexpr int kMaxGroupBoxes = 32;
+struct GroupBox {
+    const float *pos;     // device [n][3]
+    const float *masses;  // device [n] or nullptr
+    float mass;           // uniform mass when masses == nullptr
+    int64_t n;
+    float units_hi, units_lo;  // dims/boxsize split into two floats
+};
+// Sort CTAs [cta0[b], cta0[b+1]) read box b's particles; its packed records
+// are [rec0[b], rec0[b+1]) of the pass's record array.
+struct GroupLayout {
+    int nbox;
+    int cta0[kMaxGroupBoxes + 1];
+    int64_t rec0[kMaxGroupBoxes + 1];
+};
+// The pass's sort CTAs (deposit_sort_ctas over all the boxes' particles)
+// shared out in proportion to the boxes' particles: at least one for a box
+// with particles, none for an empty box, at most one per 4096 particles.
+GroupLayout deposit_group_layout(int nbox, const GroupBox *boxes, int sort_ctas);
+// Scratch elements a grouped pass needs beyond deposit_scratch_sizes per box:
+// hist cta0[nbox] x ntiles, tile_start nbox x (ntiles + 1), totals
+// nbox x ntiles, sorted rec0[nbox], mass_part cta0[nbox].  Requires
+// deposit_shared_hist(g), nbox <= kMaxGroupBoxes and rec0[nbox] < 2^32.
+// bad_out (device-visible, one word per box, may be null) receives each box's
+// count of skipped particles, and the status word is zeroed for the next pass.
+cudaError_t deposit_group_pass(const DepositGeom &g, const GroupLayout &lay, const GroupBox *boxes,
+                               float *grid0, int64_t grid_stride, double *field_mass0,
+                               double *field_sub0, double *field_corner0, DepositScratch &s,
+                               DeviceStatus *st0, unsigned long long *bad_out, cudaStream_t stream,
+                               int64_t *launches);
+
 // Window engine (deposit_window.cu) for spatially coherent particle order.
 constexpr int kWindowChunks[4] = {4096, 2048, 1024, 512};  // chunk lengths tried, largest first
 // Shared window capacity in cells for a chunk length.
@@ -216,8 +252,9 @@ struct XfftBin {
     float bpu_half;         // 0.5 * binsperunit (first-guess bin)
     const uint32_t *thr;    // [nrbins+1]
     const float *iw;        // [dims]
-    const double *corner;   // exact (N/2,N/2,N/2) value, or null
-    double *partial;        // [ctas][nrbins] FP64 partial sums
+    const double *corner;   // exact (N/2,N/2,N/2) value per binned field, or null
+    double *partial;        // [ctas][fields][nrbins] FP64 partial sums
+    int fields = 1;         // 1, or the batch: each field's auto spectrum
 };
 bool xfft_supported(int dims);
 bool xfft_bin_supported(int dims, int nrbins);
@@ -311,6 +348,13 @@ cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const do
                            double ma, double mb, double *out, cudaStream_t stream,
                            int64_t *launches, const DeviceStatus *st_in = nullptr,
                            DeviceStatus *st_out = nullptr);
+// The same for the auto spectra of nfields fields binned together (partial:
+// [ctas][nfields][nrbins]): out[f][nrbins] normalised by mass[f]^2, in
+// launches of up to kMaxBinPairs fields; the last copies the status words.
+cudaError_t finalize_powers(const double *partial, int ctas, int nrbins, int nfields,
+                            const double *count, const double *mass, double *out,
+                            cudaStream_t stream, int64_t *launches, const DeviceStatus *st_in,
+                            DeviceStatus *st_out);
 // Binning of one kz-major spectrum S[kz][x][y] (after zfft_kz_pass and the
 // batched 2-D C2C): the auto pair's partial sums, one FP64 histogram per CTA
 // (partial: ctas * nrbins doubles), for finalize_power.  When `zero` is not

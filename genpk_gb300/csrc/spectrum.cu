@@ -721,4 +721,29 @@ cudaError_t finalize_power(const double *partial, int ctas, int nrbins, const do
     return cudaGetLastError();
 }
 
+cudaError_t finalize_powers(const double *partial, int ctas, int nrbins, int nfields,
+                            const double *count, const double *mass, double *out,
+                            cudaStream_t stream, int64_t *launches, const DeviceStatus *st_in,
+                            DeviceStatus *st_out)
+{
+    for (int f0 = 0; f0 < nfields; f0 += kMaxBinPairs) {
+        const int k = std::min(kMaxBinPairs, nfields - f0);
+        NormParams mn;
+        mn.npc = nfields;
+        for (int q = 0; q < kMaxBinPairs; q++) {
+            mn.ma[q] = mn.mb[q] = q < k ? mass[f0 + q] : 1.0;
+            mn.src[q] = q < k ? f0 + q : 0;
+        }
+        const bool last = f0 + k >= nfields;
+        k_bin_finalize<<<k * nrbins, kFinalizeThreads, 0, stream>>>(
+            partial, ctas, nrbins, count, mn, out + (size_t)f0 * nrbins, st_in,
+            last ? st_out : nullptr);
+        (*launches)++;
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess)
+            return err;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace genpk

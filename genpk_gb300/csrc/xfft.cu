@@ -65,13 +65,15 @@ struct XParams {
     int ntiles;            // tiles_per_field * nbatch
     int box_rows;          // rows per TMA box
     const float2 *tw;      // [dims] exp(-2 pi i m / dims)
-    // binning of the batch's single field (nrbins == 0: no binning)
+    // binning (nrbins == 0: none) of the batch's single field (bin_fields = 1)
+    // or of each field of the batch (bin_fields = nbatch)
     int nrbins;
+    int bin_fields;
     float bpu_half;
     const uint32_t *thr;   // [nrbins + 1]
     const float *iw;       // [dims]
-    const double *corner;  // exact (N/2,N/2,N/2) value or null
-    double *partial;       // [gridDim.x][nrbins]
+    const double *corner;  // exact (N/2,N/2,N/2) value per binned field, or null
+    double *partial;       // [gridDim.x][bin_fields][nrbins]
     const float *gcoef;    // adjoint: [nrbins] per-bin coefficients G_b
 };
 
@@ -476,7 +478,14 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
         fence_proxy_async();
     }
     __syncthreads();
-    const float corner_val = (BIN && p.corner) ? (float)*p.corner : 0.f;
+    // Binning each field of a batch: a CTA's tiles run through the fields in
+    // order, so its histogram goes out at each field's last tile; fields it
+    // has no tile of get zeros (those before its first tile here).
+    const int bf = p.bin_fields;
+    double *cta_part = (BIN && bf > 1) ? p.partial + (size_t)blockIdx.x * bf * p.nrbins : nullptr;
+    if (BIN && bf > 1)
+        for (int i = tid; i < ((int)blockIdx.x / p.tiles_per_field) * p.nrbins; i += kXThreads)
+            cta_part[i] = 0.0;
     // iw(kx) of the 8 rows this thread's last stage writes: the same in every tile
     float iwr[8];
     {
@@ -571,7 +580,8 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
             const int row = ci.special == 1 ? 0 : N / 2;
             const float p1 = (iw_s[row] * ci.iwj) * ci.iwz;
             const float p2 = p1 * p1;
-            const float pw = ci.special == 1 ? 0.f : corner_val * corner_val;
+            const float cv = ci.special == 2 ? (float)p.corner[bf > 1 ? b : 0] : 0.f;
+            const float pw = ci.special == 1 ? 0.f : cv * cv;
             if (g == 0)  // one thread of the column writes it
                 vals[c * (N + 1) + row] = ci.w * (p2 * p2) * pw;
         }
@@ -639,8 +649,12 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
                     atomicAdd(&whist[wid * p.nrbins + cb], acc);
             }
             // The warps' FP32 histograms go into the CTA's FP64 one every 8
-            // tiles and after the CTA's last tile (the condition is uniform).
-            if ((k & 7) == 7 || t + (int)gridDim.x >= p.ntiles) {
+            // tiles and after the CTA's last tile of a binned field (the
+            // condition is uniform); a field's histogram then goes out.
+            const int tn = t + (int)gridDim.x;
+            const int bn = tn < p.ntiles ? tn / p.tiles_per_field : -1;  // -1: no next tile
+            const bool field_end = bn != b && (bf > 1 || bn < 0);
+            if ((k & 7) == 7 || field_end) {
                 __syncthreads();
                 for (int bb = tid; bb < p.nrbins; bb += kXThreads) {
                     float s = 0.f;
@@ -649,13 +663,22 @@ __global__ void __launch_bounds__(kXThreads, kXCtasPerSm)
                         whist[w * p.nrbins + bb] = 0.f;
                     }
                     chist[bb] += (double)s;
+                    if (bf > 1 && field_end) {
+                        cta_part[(size_t)b * p.nrbins + bb] = chist[bb];
+                        chist[bb] = 0.0;
+                    }
+                }
+                if (bf > 1 && field_end) {  // fields up to the next tile's get zeros
+                    const int upto = bn < 0 ? bf : bn;
+                    for (int i = tid; i < (upto - b - 1) * p.nrbins; i += kXThreads)
+                        cta_part[(size_t)(b + 1) * p.nrbins + i] = 0.0;
                 }
             }
         }
     }
     if (tid == 0)
         asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete
-    if (BIN) {
+    if (BIN && bf == 1) {
         __syncthreads();
         for (int bb = tid; bb < p.nrbins; bb += kXThreads)
             p.partial[(size_t)blockIdx.x * p.nrbins + bb] = chist[bb];
@@ -1234,6 +1257,9 @@ cudaError_t launch_xfft(const GridGeom &g, float *grids, int nbatch, const float
     p.iw = bin ? bin->iw : grad ? grad->iw : nullptr;
     p.corner = bin ? bin->corner : nullptr;
     p.partial = bin ? bin->partial : nullptr;
+    p.bin_fields = bin ? bin->fields : 1;
+    if (bin && bin->fields != 1 && bin->fields != nbatch)
+        return cudaErrorInvalidValue;
     p.gcoef = grad ? grad->gcoef : nullptr;
     p.zero = zero_bytes > 0 ? static_cast<uint4 *>(zero) : nullptr;
     p.zero_units = zero_bytes / 16;

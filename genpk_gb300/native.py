@@ -72,6 +72,11 @@ ABI = {
     "genpk_power_step_use_graph": (ctypes.c_int, [c_void_p, ctypes.c_int]),
     "genpk_power_step_replays": (ctypes.c_int64, [c_void_p]),
     "genpk_batch_graph_replays": (ctypes.c_int64, [c_void_p]),
+    "genpk_batch_set_mode": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "genpk_batch_last_mode": (ctypes.c_int, [c_void_p]),
+    "genpk_batch_auto_times": (ctypes.c_int, [c_void_p, c_f64p, c_f64p]),
+    "genpk_batch_groups": (ctypes.c_int, [c_void_p]),
+    "genpk_batch_group": (c_void_p, [c_void_p, ctypes.c_int, c_i32p, c_i32p]),
     "genpk_power_noalloc": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_double, c_void_p, c_i32p,
                                            c_f64p, c_void_p]),

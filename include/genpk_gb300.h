@@ -302,6 +302,54 @@ int genpk_batch_use_graph(genpk_batch *b, int on);
 /* Calls served by a graph replay since creation, or -1 for a null batch. */
 int64_t genpk_batch_graph_replays(const genpk_batch *b);
 
+/* How genpk_batch_power issues the boxes.
+ * GENPK_BATCH_PER_BOX: each box has its own deposit pass (its engine chosen
+ * as genpk_deposit chooses it), transform and binning.
+ * GENPK_BATCH_GROUPED: the boxes that share a grid size (up to 32; more make
+ * further groups) are the fields of one internal context and go through one
+ * grouped sorted-engine pass -- one launch of each kernel of the pass for all
+ * of them: the sort CTAs shared out over the boxes' particles by a table of
+ * (box, particle range, record range), the per-tile kernels indexed by box --
+ * with a tile shape and sort CTAs per SM tuned per group on its first call
+ * (trials as for genpk_deposit_trials, on the group's context); then one
+ * batched 2-D R2C over every x-plane of the group, and one x pass that bins
+ * every box's auto spectrum (a histogram per box).  A call qualifies when
+ * every array is in device memory, every argument is valid, the grids have at
+ * most 512 cells a side and a group holds fewer than 2^32 particles; any
+ * other call runs per box.  The grids are the per-box sorted engine's bit for
+ * bit; the spectra agree with the per-box path's to FP32 transform rounding.
+ * A skipped particle is reported for its box.
+ * GENPK_BATCH_AUTO (the default): for calls that qualify, the faster of the
+ * two for calls of the same shape (particle counts and mass kinds): the first
+ * four such calls run per box, grouped, per box and grouped (the first two
+ * tune; the last two are timed by wall clock, and none is captured), later
+ * calls the faster way (the per-box path keeps the stream and window engines
+ * for spatially ordered boxes; the grouped pass sorts every box).  A call of
+ * another shape starts the trials again.  Switching modes drops a captured
+ * graph. */
+#define GENPK_BATCH_PER_BOX 0
+#define GENPK_BATCH_GROUPED 1
+#define GENPK_BATCH_AUTO 2
+int genpk_batch_set_mode(genpk_batch *b, int mode);
+
+/* The way the latest call ran (GENPK_BATCH_PER_BOX or GENPK_BATCH_GROUPED),
+ * or -1 before the first call or for a null batch. */
+int genpk_batch_last_mode(const genpk_batch *b);
+
+/* GENPK_BATCH_AUTO's timed trial calls of the current shape (ms, 0 where not
+ * run yet) and its choice, or -1 while the trials run (or for a null batch). */
+int genpk_batch_auto_times(const genpk_batch *b, double *per_box_ms, double *grouped_ms);
+
+/* Groups made by the first grouped call (0 before it), or -1 for a null
+ * batch. */
+int genpk_batch_groups(const genpk_batch *b);
+
+/* Group g's context (for its kernel launches, genpk_deposit_config and
+ * genpk_deposit_trials), or NULL.  nboxes (may be NULL) receives its number
+ * of boxes (at most 32) and boxes (may be NULL, else room for 32) their batch
+ * indices, field 0 first. */
+genpk_ctx *genpk_batch_group(genpk_batch *b, int g, int *nboxes, int *boxes);
+
 /* Testing aid for the bounded device waits (no reference counterpart; the
  * reference has no device code).  The next window- or stream-engine deposit
  * pass on ctx does not issue the bulk copy of its chunk number `chunk`
