@@ -82,6 +82,9 @@ def parse():
                     help="particle order of the Zel'dovich workload: lattice (x slowest), "
                          "morton (a space-filling curve, as snapshots are often written) or "
                          "random (shuffled)")
+    ap.add_argument("--batch-mode", choices=["auto", "per_box", "grouped"], default="auto",
+                    help="boxes workload: how the timed batch calls run (auto: the library's "
+                         "default, per box or grouped by its own timed trials)")
     ap.add_argument("--profile-timed", action="store_true",
                     help="open the CUDA profiler range (cudaProfilerStart/Stop) around the timed "
                          "steps only, for `ncu --profile-from-start off`: set-up, tuning and "
@@ -496,6 +499,7 @@ def boxes(args):
     torch.cuda.synchronize()
     norms = [O.total_mass(c, None, mass) for c, _, _ in batch]
     b = gp.Batch([g for _, g, _ in batch], nrbins)
+    b.set_mode(args.batch_mode)
 
     def step(src):
         return b.power(box, src, norms, mass=mass)
@@ -536,7 +540,8 @@ def boxes(args):
                               "one replay of a captured CUDA graph per call)",
                        "timing": "wall clock per batch, device synchronised on both sides"},
             "gpu_launches": launches,
-            "batch_mode": b.last_mode, "auto_trials": b.auto_times(),
+            "batch_mode": b.last_mode, "batch_mode_set": args.batch_mode,
+            "auto_trials": b.auto_times(),
             "graph_replays": b.graph_replays}
     # the host's launches per timed call: one graph launch once the call is replayed
     line["host_launches_per_step"] = 1 if b.graph_replays >= args.steps else launches
