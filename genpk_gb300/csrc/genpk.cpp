@@ -2764,11 +2764,18 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
     const auto t_start = std::chrono::steady_clock::now();
     // The units of work: boxes (largest first, so that their passes start
     // first and the small ones fill in), or groups of boxes (largest first).
-    const bool grouped = want_group && can_group;
-    if (grouped) {
-        const int rc = make_groups(b);
-        if (rc != GENPK_OK)
-            return rc;
+    bool grouped = want_group && can_group;
+    const int made = grouped ? make_groups(b) : GENPK_OK;
+    if (made != GENPK_OK) {
+        // (the groups' contexts could not be made: the grouped mode reports
+        // it; the automatic one runs per box from now on)
+        if (b->mode == GENPK_BATCH_GROUPED)
+            return made;
+        b->mode = GENPK_BATCH_PER_BOX;
+        b->err.clear();
+        grouped = false;
+        trial = false;
+        timed_slot = -1;
     }
     std::vector<int> order;
     std::vector<genpk_ctx *> unit;
