@@ -125,13 +125,14 @@ struct BoxGroup {
 
 // Sort-CTA rows of each box in the histogram (k_sort_colsum, k_sort_offsets:
 // box = blockIdx.y), and what the scan needs per box (box = blockIdx.x):
-// its rows, uniform mass (< 0: the particles carry masses) and first record.
+// its rows, mass kind, uniform mass and first record.
 struct BoxRows {
     int first[kMaxGroupBoxes + 1];
 };
 
 struct ScanBoxes {
     int first[kMaxGroupBoxes + 1];
+    int var[kMaxGroupBoxes];  // the particles carry masses
     double umass[kMaxGroupBoxes];
     long long rec0[kMaxGroupBoxes];
 };
@@ -344,8 +345,8 @@ __global__ void __launch_bounds__(32 * kColWarps)
 constexpr int kScanThreads = 1024;
 
 // Exclusive scan of tile totals (one CTA per box) and the per-pass constants.
-// A box's tile starts begin at its first record.  uniform_mass >= 0 means
-// every particle of the box weighs uniform_mass.
+// A box's tile starts begin at its first record.  Unless the box's particles
+// carry masses, every one weighs its uniform mass (of either sign).
 __global__ void __launch_bounds__(kScanThreads)
     k_sort_scan(const uint32_t *__restrict__ totals, int ntiles, uint32_t *__restrict__ tile_start,
                 uint32_t *__restrict__ cursor, const double *__restrict__ mass_part,
@@ -358,6 +359,7 @@ __global__ void __launch_bounds__(kScanThreads)
     const int box = blockIdx.x;
     const int nsort = boxes.first[box + 1] - boxes.first[box];
     const double uniform_mass = boxes.umass[box];
+    const bool var = boxes.var[box] != 0;
     const uint32_t rec0 = (uint32_t)boxes.rec0[box];
     totals += (size_t)box * ntiles;
     tile_start += (size_t)box * (ntiles + 1);
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(kScanThreads)
         tile_start[ntiles] = carry;
 
     double m = 0.0;
-    if (uniform_mass < 0.0) {
+    if (var) {
         for (int c = threadIdx.x; c < nsort; c += blockDim.x)
             m += mass_part[c];
         m = warp_sum_d(m);
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(kScanThreads)
         // Scale: the largest |mass| maps into [2^27, 2^28) units of 2^-s, so one
         // CIC weight is below 2^28 (the 32-bit shared accumulators carry at most
         // once per 2^4 adds) and 64-bit cell sums hold 2^35 full-mass particles.
-        const float mref = uniform_mass >= 0.0 ? (float)fabs(uniform_mass)
+        const float mref = !var ? (float)fabs(uniform_mass)
                                                : __uint_as_float(st->max_mass_bits);
         st->max_mass_bits = 0u;  // read: zero again for the next pass
         int s = 0;
@@ -1089,7 +1091,8 @@ cudaError_t deposit_pass(const DepositGeom &g, const DepositArgs &a, DepositScra
     rows.first[1] = sort_ctas;
     ScanBoxes sb = {};
     sb.first[1] = sort_ctas;
-    sb.umass[0] = a.masses ? -1.0 : (double)a.mass;
+    sb.var[0] = a.masses ? 1 : 0;
+    sb.umass[0] = (double)a.mass;
     const bool shared_hist = deposit_shared_hist(g);
     const double n3 = (double)g.grid.dims * g.grid.dims * g.grid.dims;
     cudaError_t err;
@@ -1189,7 +1192,8 @@ cudaError_t deposit_group_pass(const DepositGeom &g, const GroupLayout &lay, con
         const GroupBox &x = boxes[b];
         src.p[b] = sort_params(g, x.pos, x.masses, x.mass, x.n, x.units_hi, x.units_lo,
                                lay.cta0[b + 1] - lay.cta0[b]);
-        sb.umass[b] = x.masses ? -1.0 : (double)x.mass;
+        sb.var[b] = x.masses ? 1 : 0;
+        sb.umass[b] = (double)x.mass;
         sb.rec0[b] = (long long)lay.rec0[b];
     }
     const int ctas = lay.cta0[nbox];

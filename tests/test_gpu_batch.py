@@ -324,3 +324,38 @@ def test_batch_auto_mode_times_both_ways_then_keeps_the_faster(gp):
         out = b.power(box, host, norm, mass=1.0)
         assert b.last_mode == "per_box"
         check(out)
+
+
+def test_batch_grouped_odd_grids_and_negative_masses(gp):
+    """Grouped boxes on odd and non-power-of-two grids (3-D cuFFT and the
+    binning kernel; no corner mode), with a negative uniform mass and signed
+    per-particle masses: the per-box path's spectra and the FP64 oracle's."""
+    import torch
+    from genpk_gb300 import synth
+    box, nrbins = 700.0, 12
+    rng = np.random.default_rng(71)
+    sm = rng.normal(0.0, 1.0, 80_000).astype(np.float32)
+    spec = [(33, synth.uniform(90_000, box, seed=72), None, -0.5),
+            (33, synth.uniform(80_000, box, seed=73), sm, 0.0),
+            (48, synth.uniform(120_000, box, seed=74), None, 2.0),
+            (33, synth.zeldovich(33, box, seed=75), None, 1.0)]
+    dims = [d for d, _, _, _ in spec]
+    pos = [torch.from_numpy(p).cuda() for _, p, _, _ in spec]
+    masses = [None if m is None else torch.from_numpy(m).cuda() for _, _, m, _ in spec]
+    mass = [mu for _, _, _, mu in spec]
+    norm = [O.total_mass(len(p), m, mu) for _, p, m, mu in spec]
+    with gp.Batch(dims, nrbins) as g, gp.Batch(dims, nrbins) as pb:
+        g.set_mode("grouped")
+        pb.set_mode("per_box")
+        out = g.power(box, pos, norm, masses_list=masses, mass=mass)
+        assert g.last_mode == "grouped"
+        assert sorted(len(x["boxes"]) for x in g.groups()) == [1, 3]
+        ref = pb.power(box, pos, norm, masses_list=masses, mass=mass)
+    for i, (d, p, m, mu) in enumerate(spec):
+        pr, cr, _ = O.pk(p, box, d, nrbins, m, mu, m_norm=norm[i])
+        assert np.array_equal(out[1][i], cr) and np.array_equal(ref[1][i], cr)
+        ok = cr > 0
+        for got in (out, ref):
+            rel = np.abs(got[0][i][ok] - pr[ok]) / np.abs(pr[ok])
+            assert rel.max() <= P_RTOL, (i, rel.max())
+        np.testing.assert_allclose(out[0][i], ref[0][i], rtol=1e-6, atol=0)

@@ -952,3 +952,28 @@ def test_empty_inputs(gp):
                                    [(m, m), (1.0, 1.0), (m, 1.0)], mass=[1.0, 1.0])
     assert not ps[1].any() and not ps[2].any() and np.array_equal(cs, cr)
     bins_close(ps[0], pr, cr)
+
+
+def test_negative_uniform_mass_every_engine(gp):
+    """A negative uniform mass (no mass array) through the sorted engine, the
+    windowed mode and the stream mode: the oracle's grid, and the same grid bit
+    for bit from each."""
+    import torch
+    from genpk_gb300 import synth
+    dims, box, mass = 32, 500.0, -0.7
+    pos = synth.zeldovich(32, box, seed=81)
+    dev = torch.from_numpy(pos).cuda()
+    ref = O.deposit(pos, box, dims, None, mass)
+    grids = []
+    with gp.Context(dims, 8) as ctx:
+        for eng in (gp.api.ENGINE_SORTED, gp.api.ENGINE_WINDOW, gp.api.ENGINE_STREAM):
+            ctx.set_engine(eng)
+            ctx.zero(0)
+            ctx.deposit(0, box, dev, None, mass)
+            ctx.sync()
+            assert ctx.last_engine == eng
+            g = ctx.read_field(0)
+            grid_close(g, ref, tol=1e-6)
+            grids.append(g)
+    for g in grids[1:]:
+        assert np.array_equal(g, grids[0])
