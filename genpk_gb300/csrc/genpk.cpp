@@ -2821,11 +2821,13 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
         issued[(size_t)u] = rc == GENPK_OK;
         return rc;
     };
+    bool group_nomem = false;  // a group's scratch did not fit
     auto note_unit = [&](int u, int rc) {
         if (rc == GENPK_OK)
             return;
         if (!grouped)
             return note(u, rc);
+        group_nomem = group_nomem || rc == GENPK_ERR_NOMEM;
         note_msg(rc, "boxes of grid " + std::to_string(unit[(size_t)u]->dims) + ": " +
                          genpk_last_error(unit[(size_t)u]));
     };
@@ -2973,6 +2975,15 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
                              " particle(s) with non-finite or out-of-range position/mass were "
                              "skipped");
         }
+    }
+    if (group_nomem && b->mode == GENPK_BATCH_AUTO) {
+        // A group's scratch does not fit beside everything else: the automatic
+        // mode runs per box from now on, starting with this call.
+        b->mode = GENPK_BATCH_PER_BOX;
+        drop_graph(b);
+        b->have_last = false;
+        b->err.clear();
+        return genpk_batch_power(b, boxsize, pos, masses, mass, n, mass_norm, power, count, keffs);
     }
     b->last_mode = grouped ? GENPK_BATCH_GROUPED : GENPK_BATCH_PER_BOX;
     if (b->mode == GENPK_BATCH_AUTO && can_group && first == GENPK_OK && trial) {

@@ -325,9 +325,10 @@ int64_t genpk_batch_graph_replays(const genpk_batch *b);
  * tune; the last two are timed by wall clock, and none is captured), later
  * calls the faster way (the per-box path keeps the stream and window engines
  * for spatially ordered boxes; the grouped pass sorts every box).  A call of
- * another shape starts the trials again.  Where the groups' contexts cannot be
- * allocated, the automatic mode runs per box from then on (the grouped mode
- * returns the error).  Switching modes drops a captured graph. */
+ * another shape starts the trials again.  Where the groups' contexts or their
+ * scratch cannot be allocated, the automatic mode runs per box from then on,
+ * starting with that call (the grouped mode returns GENPK_ERR_NOMEM).
+ * Switching modes drops a captured graph. */
 #define GENPK_BATCH_PER_BOX 0
 #define GENPK_BATCH_GROUPED 1
 #define GENPK_BATCH_AUTO 2
