@@ -314,9 +314,10 @@ int64_t genpk_batch_graph_replays(const genpk_batch *b);
  * (trials as for genpk_deposit_trials, on the group's context); then one
  * batched 2-D R2C over every x-plane of the group, and one x pass that bins
  * every box's auto spectrum (a histogram per box).  A call qualifies when
- * every array is in device memory, every argument is valid, the grids have at
- * most 512 cells a side and a group holds fewer than 2^32 particles; any
- * other call runs per box.  The grids are the per-box sorted engine's bit for
+ * every array is in device memory, every argument is valid, every grid's
+ * tile histogram fits in shared memory (40960 tiles of 16^3 cells: grids up
+ * to 544 cells a side) and the boxes of a grid size hold fewer than 2^32
+ * particles; any other call runs per box.  The grids are the per-box sorted engine's bit for
  * bit; the spectra agree with the per-box path's to FP32 transform rounding.
  * A skipped particle is reported for its box.
  * GENPK_BATCH_AUTO (the default): for calls that qualify, the faster of the
