@@ -2786,7 +2786,8 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
             for (int i : b->groups[g].boxes)
                 tot[g] += n[i];
         }
-        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return tot[(size_t)x] > tot[(size_t)y]; });
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return tot[(size_t)x] > tot[(size_t)y]; });
         for (const genpk_batch::Group &g : b->groups)
             unit.push_back(g.ctx);
     } else {
