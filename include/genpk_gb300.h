@@ -264,15 +264,17 @@ const char *genpk_batch_last_error(const genpk_batch *b);
  * masses[b] (float[n]) or NULL (masses itself may be NULL) for the uniform
  * mass[b], normalised by mass_norm[b] (powerspectrum.c:102-108).  power,
  * count and keffs are [nboxes][nrbins] host arrays (count and keffs may be
- * NULL).  One host thread issues every box's deposit, transform and binning,
- * largest box first, each on its box's stream, so that the boxes overlap on
- * the GPU, then waits once per box for the results (a repeated call replays a
- * captured CUDA graph of all of it: genpk_batch_use_graph); the deposit engine of each
- * box is chosen as genpk_deposit chooses it (and remembered for the same
- * arrays).  Particle arrays may be host or device memory; pinned host and
- * device arrays are read while other boxes' work runs and must stay valid
- * until the call returns.  Returns the first failure (the message names the
- * box); every issued box is still waited for. */
+ * NULL).  One host thread issues all the work, per box or grouped by grid
+ * size (genpk_batch_set_mode; by default whichever timed faster), then waits
+ * once per box or group for the results (a repeated call replays a captured
+ * CUDA graph of all of it: genpk_batch_use_graph).  Per box, every box's
+ * deposit, transform and binning run on its own stream, largest box first, so
+ * that the boxes overlap on the GPU, and the deposit engine of each box is
+ * chosen as genpk_deposit chooses it (and remembered for the same arrays).
+ * Particle arrays may be host or device memory; pinned host and device
+ * arrays are read while other work runs and must stay valid until the call
+ * returns.  Returns the first failure (the message names the box); all
+ * issued work is still waited for. */
 int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const *pos,
                       const float *const *masses, const double *mass, const int64_t *n,
                       const double *mass_norm, double *power, int *count, double *keffs);
@@ -280,19 +282,19 @@ int genpk_batch_power(genpk_batch *b, const double *boxsize, const float *const 
 /* Box i's context (for its stage times, engine and configuration), or NULL. */
 genpk_ctx *genpk_batch_box(genpk_batch *b, int i);
 
-/* Kernels launched by all the batch's boxes since creation (a graph replay
- * counts the kernels it launches). */
+/* Kernels launched by all the batch's boxes and groups since creation (a
+ * graph replay counts the kernels it launches). */
 int64_t genpk_batch_launches(const genpk_batch *b);
 
 /* CUDA graph of a whole call (on by default).  The second of two
  * consecutive genpk_batch_power calls with the same arguments (the same
  * arrays, counts, box sizes and masses; the arrays' contents may change) is
- * captured: every box's work is forked from one stream onto the boxes'
- * streams and joined back.  Later identical calls replay the graph with one
- * launch; results are identical to the eager path's, bit for bit.  A call
+ * captured: the work of every box (or group) is forked from one stream onto
+ * their streams and joined back.  Later identical calls replay the graph with
+ * one launch; results are identical to the eager path's, bit for bit.  A call
  * with other arguments runs eagerly and drops the graph, and so does any use
  * of a box's context on its own between calls.  The capture is kept only if
- * the call leaves every box's state as it found it; otherwise the call runs
+ * the call leaves every context's state as it found it; otherwise the call runs
  * eagerly and a later identical call tries again (three tries; a CUDA error
  * during capture ends the graph path).  Boxes created with GENPK_FLAG_TIMING
  * always run eagerly (stage events are not re-recorded by a replay).
