@@ -92,3 +92,20 @@ def test_context_creation_fails_cleanly_without_gpu_or_bad_args(native_lib):
     assert native_lib.genpk_status_string(5) == b"bad particle data"
     assert native_lib.genpk_last_error(None) == b"null context"
     assert native.ABI["genpk_deposit"][0] is ctypes.c_int
+
+
+def test_batch_entry_points_reject_null_and_bad_arguments(native_lib):
+    """The batch calls on a null batch or with bad arguments return their
+    error values without touching a GPU."""
+    h = ctypes.c_void_p()
+    dims = (ctypes.c_int64 * 2)(64, 128)
+    assert native_lib.genpk_batch_create(0, dims, 8, 0, ctypes.byref(h)) != 0
+    assert native_lib.genpk_batch_create(2, dims, 0, 0, ctypes.byref(h)) != 0
+    assert native_lib.genpk_batch_set_mode(None, 1) != 0
+    assert native_lib.genpk_batch_last_mode(None) == -1
+    assert native_lib.genpk_batch_groups(None) == -1
+    assert native_lib.genpk_batch_group(None, 0, None, None) is None
+    assert native_lib.genpk_batch_auto_times(None, None, None) == -1
+    assert native_lib.genpk_batch_graph_replays(None) == -1
+    assert native_lib.genpk_batch_launches(None) == -1
+    assert native_lib.genpk_batch_last_error(None) == b"null batch"
